@@ -1,0 +1,161 @@
+/*
+ * gbcc.h -- C ABI of the GB300-native closed-shell CCSD amplitude solver.
+ *
+ * The library replaces the residual engine and the Jacobi/DIIS iteration of
+ * MPQC's closed-shell CCSD (paths relative to the MPQC source tree):
+ *
+ *   gbcc_create      <- CCSD(const KeyVal&)            src/mpqc/chemistry/qc/lcao/cc/ccsd.h:70-115
+ *                       DIISSolver(const KeyVal&)      src/mpqc/chemistry/qc/cc/solvers.h:93-95
+ *   gbcc_set_inputs  <- cc::Integrals<Array> members   src/mpqc/chemistry/qc/lcao/cc/ccsd_r1_r2.h:24-56
+ *                       filled in CCSD::compute_ccsd   src/mpqc/chemistry/qc/lcao/cc/ccsd.h:281-296
+ *                       and the orbital energies of JacobiDIISSolver
+ *                                                      src/mpqc/chemistry/qc/lcao/cc/solvers.h:1128-1136
+ *   gbcc_residual    <- compute_cs_ccsd_r1 + compute_cs_ccsd_r2 (standard method)
+ *                                                      src/mpqc/chemistry/qc/lcao/cc/ccsd_r1_r2.h:70-124, 198-293
+ *   gbcc_energy      <- the residual-augmented energy  src/mpqc/chemistry/qc/lcao/cc/ccsd.h:377-379
+ *                       and Solver::error              src/mpqc/chemistry/qc/cc/solvers.h:60-63
+ *   gbcc_solve       <- CCSD::compute_ccsd loop        src/mpqc/chemistry/qc/lcao/cc/ccsd.h:268-477
+ *   gbcc_destroy     <- ~CCSD / solver_.reset()        src/mpqc/chemistry/qc/lcao/cc/ccsd.h:246
+ *
+ * Conventions
+ *   - All arrays are dense FP64, row-major, in the index order of the MPQC
+ *     annotation: Fia[i][a], Fij[i][j], Fab[a][b], Gijab[i][j][a][b] = <ij|ab>,
+ *     Gijkl[i][j][k][l], Giajb[i][a][j][b], Gijka[i][j][k][a],
+ *     Giabc[i][a][b][c], Gabcd[a][b][c][d], t1[a][i], t2[a][b][i][j].
+ *     o counts the active (correlated) occupied orbitals, v the virtuals.
+ *   - Every pointer argument may point to host memory or to device memory of
+ *     the handle's GPU; the library detects which.
+ *   - The caller owns every array.  gbcc_set_inputs copies the integrals into
+ *     handle-owned device memory; no pointer is retained after a call returns.
+ *   - One handle per host thread; a handle is not internally locked.
+ *   - Every call returns a gbcc_status; no C++ exception crosses the ABI.
+ *     gbcc_last_error() gives the message of the last failing call.
+ */
+#ifndef GBCC_H_
+#define GBCC_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBCC_ABI_VERSION 1
+
+typedef enum gbcc_status {
+  GBCC_OK = 0,
+  GBCC_ERR_INVALID_ARG = 1,  /* bad size, NULL pointer, non-finite input   (InputError)       */
+  GBCC_ERR_OOM = 2,          /* device allocation failed                                       */
+  GBCC_ERR_CUDA = 3,         /* a CUDA call failed                         (ProgrammingError)  */
+  GBCC_ERR_NOT_CONVERGED = 4,/* max_iter reached; results are still written (ccsd.h:469-472)   */
+  GBCC_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up                             */
+  GBCC_ERR_STATE = 6,        /* call out of order (e.g. residual before set_inputs)            */
+  GBCC_ERR_NUMERIC = 7       /* non-finite energy or residual during the iteration             */
+} gbcc_status;
+
+typedef enum gbcc_precision {
+  GBCC_PREC_FP64 = 0,        /* every contraction in plain FP64                                */
+  GBCC_PREC_MIXED = 1        /* split-BF16 tensor-core contractions, FP64 elsewhere            */
+} gbcc_precision;
+
+typedef struct gbcc_config {
+  int64_t o;                   /* active occupied orbitals                                     */
+  int64_t v;                   /* virtual orbitals                                             */
+  int32_t precision;           /* gbcc_precision                                               */
+  int32_t slices_ladder;       /* BF16 slices per operand, particle-particle ladder (1..3)     */
+  int32_t slices_ring;         /* ... o^3 v^3 ring terms and the ladder's T1 part (1..3)       */
+  int32_t slices_other;        /* ... every remaining contraction (1..3)                       */
+  int32_t refine_iters;        /* plain-FP64 iterations after the mixed phase                  */
+  double mixed_switch_precision; /* mixed phase ends once converged to this precision          */
+  int32_t max_iter;            /* "max_iter", default 30 (ccsd.h:104)                          */
+  double target_precision;     /* Energy precision, default 1e-9 (energy.h:45)                 */
+  int32_t diis_start;          /* "diis_start", default 1      (cc/solvers.h:93)               */
+  int32_t n_diis;              /* "n_diis", default 8                                          */
+  double diis_damp;            /* "diis_damp", default 0                                       */
+  int32_t diis_ngroup;         /* "diis_ngroup", default 1                                     */
+  int32_t diis_group_nstart;   /* "diis_group_nstart", default 1                               */
+  int32_t verbose;             /* print the iteration table (ccsd.h:28-46)                     */
+  int32_t device;              /* CUDA device ordinal                                          */
+} gbcc_config;
+
+typedef struct gbcc_inputs {
+  const double* eps_o;   /* [o] active occupied orbital energies (diag of the MO Fock)  */
+  const double* eps_v;   /* [v] virtual orbital energies                                 */
+  const double* Fia;     /* [o][v] */
+  const double* Fij;     /* [o][o] */
+  const double* Fab;     /* [v][v] */
+  const double* Gijab;   /* [o][o][v][v] */
+  const double* Gijkl;   /* [o][o][o][o] */
+  const double* Giajb;   /* [o][v][o][v] */
+  const double* Gijka;   /* [o][o][o][v] */
+  const double* Giabc;   /* [o][v][v][v] */
+  const double* Gabcd;   /* [v][v][v][v] */
+} gbcc_inputs;
+
+typedef struct gbcc_report {
+  int32_t iters;            /* residual evaluations performed                     */
+  int32_t converged;        /* 1 if the convergence test of cc/solvers.h:150 held */
+  int32_t mixed_iters;      /* of which in mixed precision                        */
+  int32_t fp64_iters;       /* of which in plain FP64                             */
+  double e_corr;            /* final correlation energy                           */
+  double last_dE;
+  double last_error;        /* Solver::error of the last residual                 */
+  double seconds_total;
+  double seconds_residual_mixed;  /* mean seconds per mixed residual              */
+  double seconds_residual_fp64;   /* mean seconds per FP64 residual               */
+} gbcc_report;
+
+typedef struct gbcc_handle gbcc_handle;
+
+/* Library ABI version (GBCC_ABI_VERSION of the build). */
+int gbcc_abi_version(void);
+
+/* Human-readable name of a status code. */
+const char* gbcc_status_string(gbcc_status s);
+
+/* Fill *cfg with the reference's defaults (precision FP64, 3/3/3 slices). */
+void gbcc_config_default(gbcc_config* cfg);
+
+/* Create a handle on cfg->device.  Replaces the KeyVal constructors. */
+gbcc_status gbcc_create(gbcc_handle** out, const gbcc_config* cfg);
+
+/* Copy Fock blocks, orbital energies and MO integrals onto the device and
+ * prepare every contraction (split copies of the constant integrals in the
+ * mixed mode).  May be called again to replace the inputs. */
+gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in);
+
+/* One residual: tau = t2 + t1 t1, R1 then R2 (R1 sets the FIJ/FAB
+ * intermediates R2 reads), in the handle's precision. */
+gbcc_status gbcc_residual(gbcc_handle* h, const double* t1_ai, const double* t2_abij,
+                          double* r1_ai, double* r2_abij);
+
+/* As gbcc_residual with an explicit precision (gbcc_precision). */
+gbcc_status gbcc_residual_ex(gbcc_handle* h, int32_t precision, const double* t1_ai,
+                             const double* t2_abij, double* r1_ai, double* r2_abij);
+
+/* Residual-augmented energy E = 2<f_ai + r1, t1> + <g_abij + r2, 2 tau - tau(b,a,i,j)>
+ * and Solver::error = sqrt(|r1|^2 + |r2|^2) / (size(r1) + size(r2)), with FP64
+ * deterministic reductions.  Either output pointer may be NULL. */
+gbcc_status gbcc_energy(gbcc_handle* h, const double* t1_ai, const double* t2_abij,
+                        const double* r1_ai, const double* r2_abij, double* energy,
+                        double* error);
+
+/* Full solve from t = 0: Jacobi + DIIS iterations until converged or
+ * max_iter.  Writes converged t1/t2 (either may be NULL), E_corr and the
+ * report (may be NULL).  Returns GBCC_ERR_NOT_CONVERGED (outputs written) if
+ * max_iter was reached, mirroring the reference's warning. */
+gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e_corr,
+                       gbcc_report* report);
+
+/* Release the handle and all its device memory.  NULL is accepted. */
+gbcc_status gbcc_destroy(gbcc_handle* h);
+
+/* Message of the last failing call on this handle ("" if none); with a NULL
+ * handle, the message of the last failed gbcc_create on this thread. */
+const char* gbcc_last_error(const gbcc_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBCC_H_ */

@@ -1,0 +1,13 @@
+"""GB300-native closed-shell CCSD amplitude solver (drop-in for MPQC's CCSD
+residual engine and Jacobi/DIIS loop).
+
+The compute path is ``libgbcc.so`` (hand-written sm_103a CUDA behind the C
+ABI of include/gbcc.h); this package is its host-side mirror of the
+reference interface.  Build the library with ``python -m mpqc_gb300.build``.
+"""
+from . import synth  # noqa: F401
+from ._lib import LIB_PATH, GbccError, load  # noqa: F401
+from .ccsd import CCSD, FeatureDisabled, InputError, Solver, compute_cs_ccsd_r1_r2  # noqa: F401
+
+__all__ = ["CCSD", "Solver", "compute_cs_ccsd_r1_r2", "GbccError", "InputError", "FeatureDisabled",
+           "load", "LIB_PATH", "synth"]

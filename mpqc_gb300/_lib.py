@@ -1,0 +1,103 @@
+"""ctypes binding of ``libgbcc.so`` (declarations in include/gbcc.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libgbcc.so"
+
+GBCC_OK = 0
+GBCC_ERR_INVALID_ARG = 1
+GBCC_ERR_OOM = 2
+GBCC_ERR_CUDA = 3
+GBCC_ERR_NOT_CONVERGED = 4
+GBCC_ERR_TIMEOUT = 5
+GBCC_ERR_STATE = 6
+GBCC_ERR_NUMERIC = 7
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# every symbol include/gbcc.h declares
+EXPORTS = (
+    "gbcc_abi_version", "gbcc_status_string", "gbcc_config_default", "gbcc_create",
+    "gbcc_set_inputs", "gbcc_residual", "gbcc_residual_ex", "gbcc_energy", "gbcc_solve",
+    "gbcc_destroy", "gbcc_last_error",
+)
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("o", C.c_int64), ("v", C.c_int64),
+        ("precision", C.c_int32), ("slices_ladder", C.c_int32), ("slices_ring", C.c_int32),
+        ("slices_other", C.c_int32), ("refine_iters", C.c_int32),
+        ("mixed_switch_precision", C.c_double),
+        ("max_iter", C.c_int32), ("target_precision", C.c_double),
+        ("diis_start", C.c_int32), ("n_diis", C.c_int32), ("diis_damp", C.c_double),
+        ("diis_ngroup", C.c_int32), ("diis_group_nstart", C.c_int32),
+        ("verbose", C.c_int32), ("device", C.c_int32),
+    ]
+
+
+class Inputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in
+                ("eps_o", "eps_v", "Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc", "Gabcd")]
+
+
+class Report(C.Structure):
+    _fields_ = [
+        ("iters", C.c_int32), ("converged", C.c_int32), ("mixed_iters", C.c_int32), ("fp64_iters", C.c_int32),
+        ("e_corr", C.c_double), ("last_dE", C.c_double), ("last_error", C.c_double),
+        ("seconds_total", C.c_double), ("seconds_residual_mixed", C.c_double),
+        ("seconds_residual_fp64", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load the library; raises if it has not been built (there is no
+    fallback implementation)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with `python -m mpqc_gb300.build` "
+                           "(the CUDA extension is required; there is no CPU path)")
+    lib = C.CDLL(str(p))
+    vp, i32, i64, dp = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)
+    lib.gbcc_abi_version.restype = C.c_int
+    lib.gbcc_status_string.restype = C.c_char_p
+    lib.gbcc_status_string.argtypes = [C.c_int]
+    lib.gbcc_config_default.restype = None
+    lib.gbcc_config_default.argtypes = [C.POINTER(Config)]
+    lib.gbcc_create.restype = C.c_int
+    lib.gbcc_create.argtypes = [C.POINTER(vp), C.POINTER(Config)]
+    lib.gbcc_set_inputs.restype = C.c_int
+    lib.gbcc_set_inputs.argtypes = [vp, C.POINTER(Inputs)]
+    lib.gbcc_residual.restype = C.c_int
+    lib.gbcc_residual.argtypes = [vp, vp, vp, vp, vp]
+    lib.gbcc_residual_ex.restype = C.c_int
+    lib.gbcc_residual_ex.argtypes = [vp, i32, vp, vp, vp, vp]
+    lib.gbcc_energy.restype = C.c_int
+    lib.gbcc_energy.argtypes = [vp, vp, vp, vp, vp, dp, dp]
+    lib.gbcc_solve.restype = C.c_int
+    lib.gbcc_solve.argtypes = [vp, vp, vp, dp, C.POINTER(Report)]
+    lib.gbcc_destroy.restype = C.c_int
+    lib.gbcc_destroy.argtypes = [vp]
+    lib.gbcc_last_error.restype = C.c_char_p
+    lib.gbcc_last_error.argtypes = [vp]
+    del i64
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class GbccError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"gbcc status {status}: {msg}")
+        self.status = status

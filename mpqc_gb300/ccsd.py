@@ -1,0 +1,234 @@
+"""Host-side mirror of MPQC's closed-shell CCSD interface over ``libgbcc``.
+
+* ``CCSD(kv)`` mirrors the KeyVal constructor of ``lcao::CCSD``
+  (src/mpqc/chemistry/qc/lcao/cc/ccsd.h:70-115) and of ``cc::DIISSolver``
+  (src/mpqc/chemistry/qc/cc/solvers.h:84-95): same keywords, defaults and
+  input errors.  ``compute(integrals)`` replaces ``CCSD::compute_ccsd``
+  (ccsd.h:268-477) and returns E_corr; ``t1()`` / ``t2()`` return the
+  converged amplitudes as ``CCSD::t1()/t2()`` (ccsd.h:165-179) do.
+* ``compute_cs_ccsd_r1_r2(t1, t2, ints)`` evaluates both residuals of
+  ccsd_r1_r2.h:70-124 and 198-293 (R1 then R2, as the reference requires).
+
+Arrays are numpy (host) or torch CUDA tensors (device), FP64, C-contiguous,
+in MPQC annotation order (t1[a,i], t2[a,b,i,j], Gijab[i,j,a,b], ...).
+Every call goes to the CUDA library; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+INTEGRAL_NAMES = ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc", "Gabcd")
+
+
+class InputError(ValueError):
+    """Counterpart of mpqc::InputError (src/mpqc/util/core/exception.h)."""
+
+
+class FeatureDisabled(RuntimeError):
+    """Counterpart of mpqc::FeatureDisabled: a reference option this drop-in does not provide."""
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, np.ndarray):
+        if x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise InputError("arrays must be C-contiguous float64")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):  # torch tensor
+        import torch
+        if x.dtype != torch.float64 or not x.is_contiguous():
+            raise InputError("tensors must be contiguous float64")
+        return x.data_ptr()
+    raise InputError(f"unsupported array type {type(x)!r}")
+
+
+def _check(lib, h, status):
+    if status in (L.GBCC_OK,):
+        return status
+    msg = lib.gbcc_last_error(h).decode() if h else lib.gbcc_last_error(None).decode()
+    raise L.GbccError(status, msg or lib.gbcc_status_string(status).decode())
+
+
+@dataclass
+class Report:
+    iters: int
+    converged: bool
+    mixed_iters: int
+    fp64_iters: int
+    e_corr: float
+    last_dE: float
+    last_error: float
+    seconds_total: float
+    seconds_residual_mixed: float
+    seconds_residual_fp64: float
+
+
+class Solver:
+    """One ``gbcc_handle``: device-resident integrals, residual engine and
+    Jacobi+DIIS loop for fixed (o, v)."""
+
+    def __init__(self, o, v, precision="fp64", slices=(3, 3, 3), refine_iters=2,
+                 mixed_switch_precision=1e-7, max_iter=30, target_precision=1e-9,
+                 diis_start=1, n_diis=8, diis_damp=0.0, diis_ngroup=1, diis_group_nstart=1,
+                 verbose=False, device=0):
+        self.lib = L.load()
+        cfg = L.Config()
+        self.lib.gbcc_config_default(C.byref(cfg))
+        cfg.o, cfg.v = int(o), int(v)
+        cfg.precision = {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}[precision]
+        cfg.slices_ladder, cfg.slices_ring, cfg.slices_other = (int(s) for s in slices)
+        cfg.refine_iters = int(refine_iters)
+        cfg.mixed_switch_precision = float(mixed_switch_precision)
+        cfg.max_iter = int(max_iter)
+        cfg.target_precision = float(target_precision)
+        cfg.diis_start, cfg.n_diis = int(diis_start), int(n_diis)
+        cfg.diis_damp = float(diis_damp)
+        cfg.diis_ngroup, cfg.diis_group_nstart = int(diis_ngroup), int(diis_group_nstart)
+        cfg.verbose = int(bool(verbose))
+        cfg.device = int(device)
+        self.cfg = cfg
+        self.o, self.v = int(o), int(v)
+        h = C.c_void_p()
+        _check(self.lib, None, self.lib.gbcc_create(C.byref(h), C.byref(cfg)))
+        self.h = h
+        self._keep = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbcc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_inputs(self, eps_o, eps_v, **ints):
+        missing = [n for n in INTEGRAL_NAMES if n not in ints]
+        if missing:
+            raise InputError(f"missing integrals: {missing}")
+        inp = L.Inputs()
+        inp.eps_o, inp.eps_v = _ptr(eps_o), _ptr(eps_v)
+        for n in INTEGRAL_NAMES:
+            setattr(inp, n, _ptr(ints[n]))
+        self._keep = (eps_o, eps_v, ints)
+        _check(self.lib, self.h, self.lib.gbcc_set_inputs(self.h, C.byref(inp)))
+        self._keep = None
+
+    def residual(self, t1, t2, r1=None, r2=None, precision=None):
+        o, v = self.o, self.v
+        if r1 is None:
+            r1 = np.empty((v, o)) if isinstance(t1, np.ndarray) else t1.new_empty((v, o))
+        if r2 is None:
+            r2 = np.empty((v, v, o, o)) if isinstance(t2, np.ndarray) else t2.new_empty((v, v, o, o))
+        prec = self.cfg.precision if precision is None else {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}[precision]
+        _check(self.lib, self.h, self.lib.gbcc_residual_ex(self.h, prec, _ptr(t1), _ptr(t2), _ptr(r1), _ptr(r2)))
+        return r1, r2
+
+    def energy(self, t1, t2, r1, r2):
+        e, err = C.c_double(), C.c_double()
+        _check(self.lib, self.h, self.lib.gbcc_energy(self.h, _ptr(t1), _ptr(t2), _ptr(r1), _ptr(r2),
+                                                      C.byref(e), C.byref(err)))
+        return e.value, err.value
+
+    def solve(self, want_amplitudes=True):
+        o, v = self.o, self.v
+        t1 = np.empty((v, o)) if want_amplitudes else None
+        t2 = np.empty((v, v, o, o)) if want_amplitudes else None
+        e = C.c_double()
+        rep = L.Report()
+        st = self.lib.gbcc_solve(self.h, _ptr(t1), _ptr(t2), C.byref(e), C.byref(rep))
+        if st not in (L.GBCC_OK, L.GBCC_ERR_NOT_CONVERGED):
+            _check(self.lib, self.h, st)
+        r = Report(rep.iters, bool(rep.converged), rep.mixed_iters, rep.fp64_iters, rep.e_corr,
+                   rep.last_dE, rep.last_error, rep.seconds_total, rep.seconds_residual_mixed,
+                   rep.seconds_residual_fp64)
+        return e.value, t1, t2, r
+
+
+def compute_cs_ccsd_r1_r2(t1, t2, ints, eps_o, eps_v, precision="fp64", **kw):
+    """R1 and R2 of the standard closed-shell method (ccsd_r1_r2.h:70-124,
+    198-293) for one amplitude set; ``ints`` maps the cc::Integrals names
+    (Fia ... Gabcd) to arrays."""
+    v, o = t1.shape
+    with Solver(o, v, precision=precision, **kw) as s:
+        s.set_inputs(eps_o, eps_v, **ints)
+        return s.residual(t1, t2)
+
+
+class CCSD:
+    """KeyVal-compatible CCSD front end (standard method, Jacobi+DIIS solver).
+
+    Recognised keys (reference defaults): ``method`` ("standard"),
+    ``max_iter`` (30), ``solver`` ("jacobi_diis"), ``verbose`` (False),
+    ``reduced_abcd_memory`` (True; no effect for the dense standard method),
+    ``diis_start`` (1), ``n_diis`` (8), ``diis_damp`` (0.0), ``diis_ngroup`` (1),
+    ``diis_group_nstart`` (1), ``precision`` (the Energy property precision,
+    1e-9).  Additional keys of this implementation: ``gbcc_precision``
+    ("fp64" | "mixed"), ``slices`` ([ladder, ring, other], default [3,3,3]),
+    ``refine_iters`` (2), ``mixed_switch_precision`` (1e-7), ``device`` (0).
+    """
+
+    def __init__(self, kv: dict):
+        kv = dict(kv)
+        if "ref" not in kv:
+            raise InputError("Default Ref in CCSD is not support!")
+        method = kv.get("method", "standard")
+        if method not in ("standard", "df", "direct", "direct_df"):
+            raise InputError(f"invalid method {method!r}")
+        if method != "standard":
+            raise FeatureDisabled(f"method {method!r} is not provided by this solver (standard only)")
+        solver = kv.get("solver", "jacobi_diis")
+        if solver not in ("jacobi_diis", "pno"):
+            raise InputError(f"invalid solver {solver!r}")
+        if solver != "jacobi_diis":
+            raise FeatureDisabled("the PNO solver is not provided by this solver")
+        if kv.get("cp_ccsd", False):
+            raise FeatureDisabled("CP-CCSD is not provided by this solver")
+        self.kv = kv
+        self.max_iter = int(kv.get("max_iter", 30))
+        self.verbose = bool(kv.get("verbose", False))
+        self.precision = float(kv.get("precision", 1e-9))
+        self._t1 = self._t2 = None
+        self.report = None
+        self.energy = None
+
+    def compute(self, eps_o, eps_v, ints) -> float:
+        o, v = np.asarray(eps_o).size if isinstance(eps_o, np.ndarray) else eps_o.numel(), \
+            np.asarray(eps_v).size if isinstance(eps_v, np.ndarray) else eps_v.numel()
+        kv = self.kv
+        with Solver(o, v, precision=kv.get("gbcc_precision", "fp64"), slices=kv.get("slices", (3, 3, 3)),
+                    refine_iters=kv.get("refine_iters", 2),
+                    mixed_switch_precision=kv.get("mixed_switch_precision", 1e-7),
+                    max_iter=self.max_iter, target_precision=self.precision,
+                    diis_start=kv.get("diis_start", 1), n_diis=kv.get("n_diis", 8),
+                    diis_damp=kv.get("diis_damp", 0.0), diis_ngroup=kv.get("diis_ngroup", 1),
+                    diis_group_nstart=kv.get("diis_group_nstart", 1), verbose=self.verbose,
+                    device=kv.get("device", 0)) as s:
+            s.set_inputs(eps_o, eps_v, **ints)
+            e, t1, t2, rep = s.solve()
+        self._t1, self._t2, self.report, self.energy = t1, t2, rep, e
+        return e
+
+    def t1(self):
+        if self._t1 is None:
+            raise RuntimeError("CCSD T1 amplitudes have not been computed")
+        return self._t1
+
+    def t2(self):
+        if self._t2 is None:
+            raise RuntimeError("CCSD T2 amplitudes have not been computed")
+        return self._t2

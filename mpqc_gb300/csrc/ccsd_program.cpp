@@ -1,0 +1,163 @@
+// The closed-shell CCSD residual as a program of engine operations.
+//
+// One statement per einstein-index expression of the reference (paths
+// relative to the MPQC source tree):
+//   compute_cs_ccsd_r1  src/mpqc/chemistry/qc/lcao/cc/ccsd_r1_r2.h:70-124
+//   compute_cs_ccsd_r2  src/mpqc/chemistry/qc/lcao/cc/ccsd_r1_r2.h:198-293
+//   intermediates       src/mpqc/chemistry/qc/lcao/cc/ccsd_intermediates.h:57-193
+// Tensor storage follows the MPQC annotation order (t1[a][i], t2[a][b][i][j],
+// Gijab[i][j][a][b], ...); a label string names the stored dimensions in
+// order, so Giabc("kadc") is <k a|d c> stored as Giabc[k][a][d][c].
+//
+// Two expressions are regrouped to avoid materialising an o v^3 temporary:
+// the reference's (Giabc(i,c,a,b) - Giajb(k,b,i,c) t1(a,k)) t1(c,j) is
+// evaluated as Giabc(i,c,a,b) t1(c,j) - (Giajb(k,b,i,c) t1(c,j)) t1(a,k), and
+// (Gijka(j,i,k,a) + Gijab(i,k,a,c) t1(c,j)) t1(b,k) as two products.  Both are
+// exact rearrangements of the same sums.
+#include "ccsd_program.h"
+
+namespace gbcc {
+
+void CcsdTensors::create(Engine& E, int64_t o, int64_t v) {
+  Fia = &E.tensor("Fia", {o, v}, true);
+  Fij = &E.tensor("Fij", {o, o}, true);
+  Fab = &E.tensor("Fab", {v, v}, true);
+  Gijab = &E.tensor("Gijab", {o, o, v, v}, true);
+  Gijkl = &E.tensor("Gijkl", {o, o, o, o}, true);
+  Giajb = &E.tensor("Giajb", {o, v, o, v}, true);
+  Gijka = &E.tensor("Gijka", {o, o, o, v}, true);
+  Giabc = &E.tensor("Giabc", {o, v, v, v}, true);
+  Gabcd = &E.tensor("Gabcd", {v, v, v, v}, true);
+  eps_o = &E.tensor("eps_o", {o}, true);
+  eps_v = &E.tensor("eps_v", {v}, true);
+  f_ai = &E.tensor("f_ai", {v, o}, true);
+  g_abij = &E.tensor("g_abij", {v, v, o, o}, true);
+  t1 = &E.tensor("t1", {v, o});
+  t2 = &E.tensor("t2", {v, v, o, o});
+  tau = &E.tensor("tau", {v, v, o, o});
+  r1 = &E.tensor("r1", {v, o});
+  r2 = &E.tensor("r2", {v, v, o, o});
+  tki = &E.tensor("tki", {o, o});
+  FAB = &E.tensor("FAB", {v, v});
+  FIJ = &E.tensor("FIJ", {o, o});
+  hkc = &E.tensor("hkc", {o, v});
+  X1 = &E.tensor("X1", {v, v, o, o});
+  r2u = &E.tensor("r2u", {v, v, o, o});
+  Y1 = &E.tensor("Y1", {o, v, o, o});
+  Y2 = &E.tensor("Y2", {o, o, v, o});
+  gki = &E.tensor("gki", {o, o});
+  gac = &E.tensor("gac", {v, v});
+  T = &E.tensor("T", {v, v, o, o});
+  J = &E.tensor("J", {v, o, o, v});
+  K = &E.tensor("K", {o, v, o, v});
+  tmp = &E.tensor("tmp", {v, v, o, o});
+  W = &E.tensor("W", {o, o, o, o});
+  tmp2 = &E.tensor("tmp2", {o, v, o, o});
+}
+
+// f_ai(a,i) = Fia(i,a), g_abij(a,b,i,j) = Gijab(i,j,a,b)  (ccsd.h:325-330)
+void setup_program(Engine& E, const CcsdTensors& S) {
+  E.assign(ix(*S.f_ai, "ai"), 0.0, {f1(1.0, ix(*S.Fia, "ia"))});
+  E.assign(ix(*S.g_abij, "abij"), 0.0, {f1(1.0, ix(*S.Gijab, "ijab"))});
+}
+
+void residual_program(Engine& E, const CcsdTensors& S) {
+  const Tensor &Fia = *S.Fia, &Fij = *S.Fij, &Fab = *S.Fab, &Gijab = *S.Gijab, &Gijkl = *S.Gijkl,
+               &Giajb = *S.Giajb, &Gijka = *S.Gijka, &Giabc = *S.Giabc, &Gabcd = *S.Gabcd;
+  const Tensor &t1 = *S.t1, &t2 = *S.t2, &tau = *S.tau;
+  const Tensor &r1 = *S.r1, &r2 = *S.r2;
+  const TermClass O = kClassOther, R = kClassRing, L = kClassLadder;
+
+  // ----- R1 (ccsd_r1_r2.h:70-124) -----
+  // r1(a,i) = Fia(i,a) - 2 (Fia(k,c) t1(c,i)) t1(a,k)
+  E.contract(ix(*S.tki, "ki"), 0.0, 1.0, {{1.0, ix(Fia, "kc")}}, {{1.0, ix(t1, "ci")}}, O);
+  E.assign(ix(r1, "ai"), 0.0, {f1(1.0, ix(Fia, "ia"))});
+  E.contract(ix(r1, "ai"), 1.0, -2.0, {{1.0, ix(*S.tki, "ki")}}, {{1.0, ix(t1, "ak")}}, O);
+  // h_ac = F_vv(Fab, gbar, tau); FAB = h_ac; r1 += h_ac(a,c) t1(c,i)
+  // gbar(k,l,c,d) = 2 Gijab(k,l,c,d) - Gijab(l,k,c,d)
+  E.assign(ix(*S.FAB, "ac"), 0.0, {f1(1.0, ix(Fab, "ac"))});
+  E.contract(ix(*S.FAB, "ac"), 1.0, -1.0, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "lkcd")}},
+             {{1.0, ix(tau, "adkl")}}, O);
+  E.contract(ix(r1, "ai"), 1.0, 1.0, {{1.0, ix(*S.FAB, "ac")}}, {{1.0, ix(t1, "ci")}}, O);
+  // h_ki = F_oo(Fij, gbar, tau); FIJ = h_ki; r1 -= t1(a,k) h_ki(k,i)
+  E.assign(ix(*S.FIJ, "ki"), 0.0, {f1(1.0, ix(Fij, "ki"))});
+  E.contract(ix(*S.FIJ, "ki"), 1.0, 1.0, {{2.0, ix(Gijab, "klab")}, {-1.0, ix(Gijab, "lkab")}},
+             {{1.0, ix(tau, "abil")}}, O);
+  E.contract(ix(r1, "ai"), 1.0, -1.0, {{1.0, ix(t1, "ak")}}, {{1.0, ix(*S.FIJ, "ki")}}, O);
+  // h_kc = F_ov(Fia, gbar, t1); r1 += h_kc(k,c) (2 t2(c,a,k,i) - t2(c,a,i,k) + t1(c,i) t1(a,k))
+  E.assign(ix(*S.hkc, "kc"), 0.0, {f1(1.0, ix(Fia, "kc"))});
+  E.contract(ix(*S.hkc, "kc"), 1.0, 1.0, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "lkcd")}},
+             {{1.0, ix(t1, "dl")}}, O);
+  E.assign(ix(*S.X1, "caki"), 0.0,
+           {f1(2.0, ix(t2, "caki")), f1(-1.0, ix(t2, "caik")), f2(1.0, ix(t1, "ci"), ix(t1, "ak"))});
+  E.contract(ix(r1, "ai"), 1.0, 1.0, {{1.0, ix(*S.hkc, "kc")}}, {{1.0, ix(*S.X1, "caki")}}, O);
+  // r1 += (2 Gijab(k,i,c,a) - Giajb(k,a,i,c)) t1(c,k)
+  E.contract(ix(r1, "ai"), 1.0, 1.0, {{2.0, ix(Gijab, "kica")}, {-1.0, ix(Giajb, "kaic")}},
+             {{1.0, ix(t1, "ck")}}, O);
+  // r1 += (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i)
+  E.contract(ix(r1, "ai"), 1.0, 1.0, {{2.0, ix(Giabc, "kacd")}, {-1.0, ix(Giabc, "kadc")}},
+             {{1.0, ix(tau, "cdki")}}, O);
+  // r1 -= (2 Gijka(l,k,i,c) - Gijka(k,l,i,c)) tau(c,a,k,l)
+  E.contract(ix(r1, "ai"), 1.0, -1.0, {{2.0, ix(Gijka, "lkic")}, {-1.0, ix(Gijka, "klic")}},
+             {{1.0, ix(tau, "cakl")}}, O);
+
+  // ----- R2 (ccsd_r1_r2.h:198-293) -----
+  const Tensor& r2u = *S.r2u;
+  // permutation part (:206-212)
+  E.contract(ix(r2u, "abij"), 0.0, 1.0, {{1.0, ix(Giabc, "icab")}}, {{1.0, ix(t1, "cj")}}, O);
+  E.contract(ix(*S.Y1, "kbij"), 0.0, 1.0, {{1.0, ix(Giajb, "kbic")}}, {{1.0, ix(t1, "cj")}}, O);
+  E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(*S.Y1, "kbij")}}, {{1.0, ix(t1, "ak")}}, O);
+  E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(Gijka, "jika")}}, {{1.0, ix(t1, "bk")}}, O);
+  E.contract(ix(*S.Y2, "ikaj"), 0.0, 1.0, {{1.0, ix(Gijab, "ikac")}}, {{1.0, ix(t1, "cj")}}, O);
+  E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(*S.Y2, "ikaj")}}, {{1.0, ix(t1, "bk")}}, O);
+  // g_ki = F_OO(FIJ, Fia, gbar_ijka, t1), gbar_ijka(k,l,i,c) = 2 Gijka(k,l,i,c) - Gijka(l,k,i,c)
+  E.assign(ix(*S.gki, "ki"), 0.0, {f1(1.0, ix(*S.FIJ, "ki"))});
+  E.contract(ix(*S.gki, "ki"), 1.0, 1.0, {{1.0, ix(Fia, "kc")}}, {{1.0, ix(t1, "ci")}}, O);
+  E.contract(ix(*S.gki, "ki"), 1.0, 1.0, {{2.0, ix(Gijka, "klic")}, {-1.0, ix(Gijka, "lkic")}},
+             {{1.0, ix(t1, "cl")}}, O);
+  // g_ac = F_VV(FAB, Fia, gbar_iabc, t1), gbar_iabc(k,a,d,c) = 2 Giabc(k,a,d,c) - Giabc(k,a,c,d)
+  // (the reference's 4-argument F_VV adds + Fia(k,c) t1(a,k); kept as written)
+  E.assign(ix(*S.gac, "ac"), 0.0, {f1(1.0, ix(*S.FAB, "ac"))});
+  E.contract(ix(*S.gac, "ac"), 1.0, 1.0, {{1.0, ix(Fia, "kc")}}, {{1.0, ix(t1, "ak")}}, O);
+  E.contract(ix(*S.gac, "ac"), 1.0, 1.0, {{2.0, ix(Giabc, "kadc")}, {-1.0, ix(Giabc, "kacd")}},
+             {{1.0, ix(t1, "dk")}}, O);
+  // r2 += g_ac(a,c) t2(c,b,i,j) - g_ki(k,i) t2(a,b,k,j)
+  E.contract(ix(r2u, "abij"), 1.0, 1.0, {{1.0, ix(*S.gac, "ac")}}, {{1.0, ix(t2, "cbij")}}, O);
+  E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(*S.gki, "ki")}}, {{1.0, ix(t2, "abkj")}}, O);
+  // j and k intermediates (:229-249), T(d,b,i,l) = 0.5 t2(d,b,i,l) + t1(d,i) t1(b,l)
+  E.assign(ix(*S.T, "dbil"), 0.0, {f1(0.5, ix(t2, "dbil")), f2(1.0, ix(t1, "di"), ix(t1, "bl"))});
+  const Tensor &J = *S.J, &K = *S.K;
+  E.assign(ix(J, "akic"), 0.0, {f1(1.0, ix(Gijab, "ikac"))});
+  E.contract(ix(J, "akic"), 1.0, -1.0, {{1.0, ix(Gijka, "lkic")}}, {{1.0, ix(t1, "al")}}, O);
+  E.contract(ix(J, "akic"), 1.0, 1.0, {{1.0, ix(Giabc, "kacd")}}, {{1.0, ix(t1, "di")}}, O);
+  E.contract(ix(J, "akic"), 1.0, -1.0, {{1.0, ix(Gijab, "klcd")}}, {{1.0, ix(*S.T, "dail")}}, R);
+  E.contract(ix(J, "akic"), 1.0, 0.5, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "kldc")}},
+             {{1.0, ix(t2, "adil")}}, R);
+  E.assign(ix(K, "kaic"), 0.0, {f1(1.0, ix(Giajb, "kaic"))});
+  E.contract(ix(K, "kaic"), 1.0, -1.0, {{1.0, ix(Gijka, "klic")}}, {{1.0, ix(t1, "al")}}, O);
+  E.contract(ix(K, "kaic"), 1.0, 1.0, {{1.0, ix(Giabc, "kadc")}}, {{1.0, ix(t1, "di")}}, O);
+  E.contract(ix(K, "kaic"), 1.0, -1.0, {{1.0, ix(Gijab, "kldc")}}, {{1.0, ix(*S.T, "dail")}}, R);
+  // r2 += 0.5 (2 j(a,k,i,c) - k(k,a,i,c)) (2 t2(c,b,k,j) - t2(b,c,k,j))   (:251-252)
+  E.contract(ix(r2u, "abij"), 1.0, 0.5, {{2.0, ix(J, "akic")}, {-1.0, ix(K, "kaic")}},
+             {{2.0, ix(t2, "cbkj")}, {-1.0, ix(t2, "bckj")}}, R);
+  // tmp(a,b,i,j) = k(k,a,i,c) t2(c,b,j,k); r2 -= 0.5 tmp(a,b,i,j) + tmp(b,a,i,j)   (:254-256)
+  E.contract(ix(*S.tmp, "abij"), 0.0, 1.0, {{1.0, ix(K, "kaic")}}, {{1.0, ix(t2, "cbjk")}}, R);
+  E.assign(ix(r2u, "abij"), 1.0, {f1(-0.5, ix(*S.tmp, "abij")), f1(-1.0, ix(*S.tmp, "baij"))});
+  // r2(a,b,i,j) = r2(a,b,i,j) + r2(b,a,j,i) + Gijab(i,j,a,b)   (:260-262)
+  E.assign(ix(r2, "abij"), 0.0,
+           {f1(1.0, ix(r2u, "abij")), f1(1.0, ix(r2u, "baji")), f1(1.0, ix(Gijab, "ijab"))});
+  // hole-hole ladder: W_oooo (intermediates :182-193), r2 += W(k,l,i,j) tau(a,b,k,l)
+  const Tensor& W = *S.W;
+  E.assign(ix(W, "klij"), 0.0, {f1(1.0, ix(Gijkl, "klij"))});
+  E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijka, "klic")}}, {{1.0, ix(t1, "cj")}}, O);
+  E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijka, "lkjc")}}, {{1.0, ix(t1, "ci")}}, O);
+  E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijab, "klcd")}}, {{1.0, ix(tau, "cdij")}}, O);
+  E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(W, "klij")}}, {{1.0, ix(tau, "abkl")}}, O);
+  // particle-particle ladder (:272-280)
+  E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(tau, "cdij")}}, {{1.0, ix(Gabcd, "abcd")}}, L);
+  E.contract(ix(*S.tmp2, "kaij"), 0.0, 1.0, {{1.0, ix(Giabc, "kacd")}}, {{1.0, ix(tau, "cdij")}}, R);
+  E.contract(ix(r2, "abij"), 1.0, -1.0, {{1.0, ix(*S.tmp2, "kaji")}}, {{1.0, ix(t1, "bk")}}, O);
+  E.contract(ix(r2, "abij"), 1.0, -1.0, {{1.0, ix(*S.tmp2, "kbij")}}, {{1.0, ix(t1, "ak")}}, O);
+}
+
+}  // namespace gbcc

@@ -1,0 +1,22 @@
+// The CCSD residual program and the device tensors it works on.
+#pragma once
+
+#include "engine.h"
+
+namespace gbcc {
+
+struct CcsdTensors {
+  // inputs (constant after set_inputs), MPQC annotation order
+  Tensor *Fia, *Fij, *Fab, *Gijab, *Gijkl, *Giajb, *Gijka, *Giabc, *Gabcd, *eps_o, *eps_v;
+  Tensor *f_ai, *g_abij;  // Fia("i,a") as (a,i); Gijab("i,j,a,b") as (a,b,i,j)
+  // amplitudes and residuals
+  Tensor *t1, *t2, *tau, *r1, *r2;
+  // intermediates
+  Tensor *tki, *FAB, *FIJ, *hkc, *X1, *r2u, *Y1, *Y2, *gki, *gac, *T, *J, *K, *tmp, *W, *tmp2;
+  void create(Engine& E, int64_t o, int64_t v);
+};
+
+void setup_program(Engine& E, const CcsdTensors& S);
+void residual_program(Engine& E, const CcsdTensors& S);
+
+}  // namespace gbcc

@@ -1,0 +1,612 @@
+// Contraction planner and executor (see engine.h).
+#include "engine.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <sstream>
+
+namespace gbcc {
+
+void* dev_alloc(size_t bytes) {
+  if (bytes == 0) bytes = 256;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(GBCC_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                  cudaGetErrorString(e));
+  }
+  return p;
+}
+
+void dev_free(void* p) {
+  if (p) cudaFree(p);
+}
+
+namespace {
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+using Extents = std::map<char, int64_t>;
+
+int label_pos(const std::string& lab, char c) {
+  auto p = lab.find(c);
+  return p == std::string::npos ? -1 : static_cast<int>(p);
+}
+
+void check_ix(const Ix& x) {
+  if (!x.t) throw Error(GBCC_ERR_STATE, "engine: null tensor");
+  if (static_cast<int>(x.lab.size()) != x.t->rank)
+    throw Error(GBCC_ERR_STATE, "engine: label count mismatch for " + x.t->name + "(" + x.lab + ")");
+}
+
+void add_extents(Extents& e, const Ix& x) {
+  check_ix(x);
+  for (int k = 0; k < x.t->rank; ++k) {
+    char c = x.lab[k];
+    auto it = e.find(c);
+    if (it == e.end())
+      e[c] = x.t->dim[k];
+    else if (it->second != x.t->dim[k])
+      throw Error(GBCC_ERR_STATE, std::string("engine: extent mismatch for index ") + c + " in " +
+                                      x.t->name);
+  }
+}
+
+int64_t extent_of(const Extents& e, const std::string& labs) {
+  int64_t n = 1;
+  for (char c : labs) n *= e.at(c);
+  return n;
+}
+
+int64_t stride_in(const Ix& x, char c) {
+  int p = label_pos(x.lab, c);
+  return p < 0 ? 0 : x.t->stride(p);
+}
+
+// offsets of the composite index over `order` (row-major) into tensor x
+std::vector<int64_t> offsets(const std::string& order, const Extents& e, const Ix& x) {
+  const int64_t n = extent_of(e, order);
+  std::vector<int64_t> out(static_cast<size_t>(n));
+  const int d = static_cast<int>(order.size());
+  std::vector<int64_t> ext(d), str(d), idx(d, 0);
+  for (int k = 0; k < d; ++k) {
+    ext[k] = e.at(order[k]);
+    str[k] = stride_in(x, order[k]);
+  }
+  int64_t off = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    out[static_cast<size_t>(i)] = off;
+    for (int k = d - 1; k >= 0; --k) {
+      ++idx[k];
+      off += str[k];
+      if (idx[k] < ext[k]) break;
+      off -= str[k] * ext[k];
+      idx[k] = 0;
+    }
+  }
+  return out;
+}
+
+// labels of `set` in the order they appear in `ref`
+std::string order_by(const std::string& set, const std::string& ref) {
+  std::string out;
+  for (char c : ref)
+    if (set.find(c) != std::string::npos) out.push_back(c);
+  return out;
+}
+
+std::string set_minus(const std::string& a, const std::string& b) {
+  std::string out;
+  for (char c : a)
+    if (b.find(c) == std::string::npos) out.push_back(c);
+  return out;
+}
+
+std::string set_and(const std::string& a, const std::string& b) {
+  std::string out;
+  for (char c : a)
+    if (b.find(c) != std::string::npos) out.push_back(c);
+  return out;
+}
+
+bool same_set(const std::string& a, const std::string& b) {
+  std::string x = a, y = b;
+  std::sort(x.begin(), x.end());
+  std::sort(y.begin(), y.end());
+  return x == y;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+struct OperandPlan {
+  std::vector<Lin> terms;
+  std::string ext;    // ordered external labels (GEMM rows)
+  std::string kord;   // ordered contracted labels
+  int64_t rows = 0, K = 0;
+  bool constant = false;
+  bool direct = false;  // FP64: tensor storage used as the panel
+  const double* dptr = nullptr;
+  int64_t ld = 0;
+  GatherArgs gather{};  // packing (FP64 panel or split slices)
+  int slices = 0;
+  int64_t rows_pad = 0, Kpad = 0;
+  __nv_bfloat16* packed = nullptr;  // dedicated split buffer (constants)
+  size_t pack_elems = 0;
+};
+
+struct GemmPlan {
+  bool use_tc = false;
+  bool a_is_first = true;  // GEMM M side is the call's A operand
+  int64_t M = 0, N = 0, K = 0;
+  OperandPlan P[2];        // [0] = M side, [1] = N side
+  const int64_t* cm = nullptr;
+  const int64_t* cn = nullptr;
+  double alpha = 1.0, beta = 0.0;
+  double* C = nullptr;
+  int slices = 0, npairs = 0, bn = 0;
+  int pa[kMaxPairs] = {}, pb[kMaxPairs] = {};
+  double flops = 0.0;
+};
+
+struct Site {
+  int kind = 0;  // 0 assign, 1 contract
+  std::string sig;
+  GatherArgs gather{};
+  GemmPlan plan[2];
+};
+
+Engine::Engine() = default;
+
+Engine::~Engine() {
+  for (void* p : owned_) dev_free(p);
+  for (auto& kv : tensors_) dev_free(kv.second->d);
+  dev_free(w64a_);
+  dev_free(w64b_);
+  dev_free(wbfa_);
+  dev_free(wbfb_);
+}
+
+Tensor& Engine::tensor(const std::string& name, std::initializer_list<int64_t> dims, bool constant) {
+  auto it = tensors_.find(name);
+  if (it != tensors_.end()) {
+    Tensor& t = *it->second;
+    int k = 0;
+    bool same = static_cast<int>(dims.size()) == t.rank;
+    for (int64_t dval : dims) same = same && (k < t.rank && t.dim[k++] == dval);
+    if (!same) throw Error(GBCC_ERR_STATE, "engine: tensor " + name + " re-requested with new shape");
+    return t;
+  }
+  auto t = std::make_unique<Tensor>();
+  t->name = name;
+  t->rank = static_cast<int>(dims.size());
+  int k = 0;
+  for (int64_t dval : dims) t->dim[k++] = dval;
+  t->constant = constant;
+  const size_t bytes = static_cast<size_t>(t->size()) * sizeof(double);
+  t->d = static_cast<double*>(dev_alloc(bytes));
+  GBCC_CK(cudaMemsetAsync(t->d, 0, bytes, stream_));
+  bytes_ += bytes;
+  Tensor& ref = *t;
+  tensors_[name] = std::move(t);
+  return ref;
+}
+
+Tensor* Engine::find(const std::string& name) {
+  auto it = tensors_.find(name);
+  return it == tensors_.end() ? nullptr : it->second.get();
+}
+
+void Engine::reset_plans() {
+  sites_.clear();
+  for (void* p : owned_) dev_free(p);
+  owned_.clear();
+  planned_ = false;
+  ws64_a_ = ws64_b_ = wsbf_a_ = wsbf_b_ = 0;
+  dev_free(w64a_);
+  dev_free(w64b_);
+  dev_free(wbfa_);
+  dev_free(wbfb_);
+  w64a_ = w64b_ = nullptr;
+  wbfa_ = wbfb_ = nullptr;
+}
+
+void Engine::begin(Mode m, int precision) {
+  if (m == Mode::kExec && !planned_) throw Error(GBCC_ERR_STATE, "engine: EXEC before PLAN");
+  mode_ = m;
+  prec_ = precision;
+  cursor_ = 0;
+  flops_ = 0.0;
+  n_tc_ = 0;
+  n_launch_ = 0;
+}
+
+void Engine::end() {
+  if (mode_ == Mode::kPlan) {
+    planned_ = true;
+  } else if (cursor_ != sites_.size()) {
+    throw Error(GBCC_ERR_STATE, "engine: program ended early");
+  }
+}
+
+Site& Engine::site() {
+  if (mode_ == Mode::kPlan) {
+    sites_.push_back(std::make_unique<Site>());
+    ++cursor_;
+    return *sites_.back();
+  }
+  if (cursor_ >= sites_.size()) throw Error(GBCC_ERR_STATE, "engine: program longer than its plan");
+  return *sites_[cursor_++];
+}
+
+DevTable Engine::upload(const std::vector<int64_t>& v) {
+  DevTable t;
+  t.n = static_cast<int64_t>(v.size());
+  const size_t bytes = std::max<size_t>(v.size(), 1) * sizeof(int64_t);
+  t.d = static_cast<int64_t*>(dev_alloc(bytes));
+  owned_.push_back(t.d);
+  bytes_ += bytes;
+  if (!v.empty()) GBCC_CK(cudaMemcpy(t.d, v.data(), v.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  return t;
+}
+
+int Engine::slices_for(TermClass cls, double flops) const {
+  // contractions this small are cheaper in FP64 than a tensor-core launch
+  if (flops < 1.0e6) return 0;
+  return slices_[cls];
+}
+
+// ---------------------------------------------------------------------------
+
+void Engine::assign(const Ix& c, double beta, const std::vector<Factor>& terms) {
+  Site& s = site();
+  if (mode_ == Mode::kExec) {
+    if (s.kind != 0) throw Error(GBCC_ERR_STATE, "engine: site kind mismatch");
+    launch_gather(s.gather, stream_);
+    ++n_launch_;
+    return;
+  }
+  s.kind = 0;
+  check_ix(c);
+  if (terms.empty() || terms.size() > static_cast<size_t>(kMaxTerms))
+    throw Error(GBCC_ERR_STATE, "engine: assign needs 1..4 terms");
+  Extents e;
+  add_extents(e, c);
+  for (const auto& f : terms) {
+    add_extents(e, f.a);
+    if (f.b.t) add_extents(e, f.b);
+    for (char ch : f.a.lab)
+      if (c.lab.find(ch) == std::string::npos)
+        throw Error(GBCC_ERR_STATE, std::string("engine: assign index ") + ch + " not in output");
+    for (char ch : f.b.lab)
+      if (c.lab.find(ch) == std::string::npos)
+        throw Error(GBCC_ERR_STATE, std::string("engine: assign index ") + ch + " not in output");
+  }
+  // split output dims into rows [0,split) and columns [split,rank)
+  const int rank = c.t->rank;
+  int split = rank;
+  int64_t cols = 1;
+  while (split > 0 && cols < 1024) {
+    --split;
+    cols *= c.t->dim[split];
+  }
+  const std::string rlab = c.lab.substr(0, split), clab = c.lab.substr(split);
+  GatherArgs& g = s.gather;
+  std::memset(&g, 0, sizeof(g));
+  g.nterms = static_cast<int>(terms.size());
+  for (size_t t = 0; t < terms.size(); ++t) {
+    GatherTerm& T = g.t[t];
+    T.coef = terms[t].coef;
+    T.a = terms[t].a.t->d;
+    T.ra = upload(offsets(rlab, e, terms[t].a)).d;
+    T.ca = upload(offsets(clab, e, terms[t].a)).d;
+    if (terms[t].b.t) {
+      T.b = terms[t].b.t->d;
+      T.rb = upload(offsets(rlab, e, terms[t].b)).d;
+      T.cb = upload(offsets(clab, e, terms[t].b)).d;
+    }
+  }
+  g.R = g.Rpad = extent_of(e, rlab);
+  g.C = g.Cpad = extent_of(e, clab);
+  g.out = c.t->d;
+  g.ldo = g.C;
+  g.beta = beta;
+}
+
+// ---------------------------------------------------------------------------
+
+namespace {
+
+bool storage_is_panel(const Ix& x, const std::string& ext) {
+  // storage order = [ext labels...][K labels...]
+  const int ne = static_cast<int>(ext.size());
+  for (int k = 0; k < x.t->rank; ++k) {
+    const bool is_ext = ext.find(x.lab[k]) != std::string::npos;
+    if ((k < ne) != is_ext) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<Lin>& A,
+                      const std::vector<Lin>& B, TermClass cls) {
+  Site& s = site();
+  if (mode_ == Mode::kExec) {
+    if (s.kind != 1) throw Error(GBCC_ERR_STATE, "engine: site kind mismatch");
+    GemmPlan& p = s.plan[prec_ == GBCC_PREC_MIXED ? 1 : 0];
+    flops_ += p.flops;
+    if (p.use_tc) {
+      __nv_bfloat16* panel[2];
+      for (int side = 0; side < 2; ++side) {
+        OperandPlan& op = p.P[side];
+        if (op.constant) {
+          if (!op.packed) throw Error(GBCC_ERR_STATE, "engine: constant operand not packed");
+          panel[side] = op.packed;
+        } else {
+          panel[side] = side == 0 ? wbfa_ : wbfb_;
+          GatherArgs g = op.gather;
+          g.outs = panel[side];
+          launch_gather(g, stream_);
+          ++n_launch_;
+        }
+      }
+      GemmTcArgs t{};
+      t.M = p.M;
+      t.N = p.N;
+      t.Mpad = p.P[0].rows_pad;
+      t.Npad = p.P[1].rows_pad;
+      t.Kpad = p.P[0].Kpad;
+      t.A = panel[0];
+      t.a_slices = p.slices;
+      t.B = panel[1];
+      t.b_slices = p.slices;
+      t.npairs = p.npairs;
+      for (int q = 0; q < p.npairs; ++q) {
+        t.pa[q] = p.pa[q];
+        t.pb[q] = p.pb[q];
+      }
+      t.C = p.C;
+      t.cm = p.cm;
+      t.cn = p.cn;
+      t.alpha = p.alpha;
+      t.beta = p.beta;
+      t.bn = p.bn;
+      t.err = err_;
+      if (!launch_gemm_tc(t, stream_))
+        throw Error(GBCC_ERR_CUDA, "tcgen05 GEMM launch rejected (tensor map or size)");
+      ++n_tc_;
+      ++n_launch_;
+    } else {
+      const double* panel[2];
+      for (int side = 0; side < 2; ++side) {
+        OperandPlan& op = p.P[side];
+        if (op.direct) {
+          panel[side] = op.dptr;
+        } else {
+          double* w = side == 0 ? w64a_ : w64b_;
+          GatherArgs g = op.gather;
+          g.out = w;
+          launch_gather(g, stream_);
+          ++n_launch_;
+          panel[side] = w;
+        }
+      }
+      GemmF64Args f{};
+      f.M = p.M;
+      f.N = p.N;
+      f.K = p.K;
+      f.A = panel[0];
+      f.lda = p.P[0].direct ? p.P[0].ld : p.K;
+      f.B = panel[1];
+      f.ldb = p.P[1].direct ? p.P[1].ld : p.K;
+      f.C = p.C;
+      f.cm = p.cm;
+      f.cn = p.cn;
+      f.alpha = p.alpha;
+      f.beta = p.beta;
+      launch_gemm_f64(f, stream_);
+      ++n_launch_;
+    }
+    return;
+  }
+
+  // ---------------- PLAN ----------------
+  s.kind = 1;
+  check_ix(c);
+  if (A.empty() || B.empty() || A.size() > static_cast<size_t>(kMaxTerms) ||
+      B.size() > static_cast<size_t>(kMaxTerms))
+    throw Error(GBCC_ERR_STATE, "engine: contract needs 1..4 terms per operand");
+  Extents e;
+  add_extents(e, c);
+  for (const auto& l : A) add_extents(e, l.x);
+  for (const auto& l : B) add_extents(e, l.x);
+  for (const auto& l : A)
+    if (!same_set(l.x.lab, A[0].x.lab)) throw Error(GBCC_ERR_STATE, "engine: A terms differ in indices");
+  for (const auto& l : B)
+    if (!same_set(l.x.lab, B[0].x.lab)) throw Error(GBCC_ERR_STATE, "engine: B terms differ in indices");
+  const std::string la = A[0].x.lab, lb = B[0].x.lab;
+  const std::string kset = set_and(la, lb);
+  const std::string aext = set_minus(la, kset), bext = set_minus(lb, kset);
+  for (char ch : kset)
+    if (c.lab.find(ch) != std::string::npos)
+      throw Error(GBCC_ERR_STATE, "engine: Hadamard indices are not supported");
+  if (!same_set(aext + bext, c.lab))
+    throw Error(GBCC_ERR_STATE, "engine: output indices must be exactly the external ones (" + c.lab + ")");
+  const int64_t rowsA = extent_of(e, aext), rowsB = extent_of(e, bext), K = extent_of(e, kset);
+  bool constA = true, constB = true;
+  for (const auto& l : A) constA = constA && l.x.t->constant;
+  for (const auto& l : B) constB = constB && l.x.t->constant;
+  const double flops = 2.0 * static_cast<double>(rowsA) * rowsB * K;
+
+  for (int pm = 0; pm < 2; ++pm) {
+    GemmPlan& p = s.plan[pm];
+    p = GemmPlan{};
+    p.flops = flops;
+    p.a_is_first = rowsA >= rowsB;
+    const std::vector<Lin>& Ms = p.a_is_first ? A : B;
+    const std::vector<Lin>& Ns = p.a_is_first ? B : A;
+    const std::string mext = p.a_is_first ? aext : bext;
+    const std::string next = p.a_is_first ? bext : aext;
+    const bool constM = p.a_is_first ? constA : constB;
+    const bool constN = p.a_is_first ? constB : constA;
+    p.M = extent_of(e, mext);
+    p.N = extent_of(e, next);
+    p.K = K;
+    p.beta = beta;
+    p.C = c.t->d;
+    int slices = pm == 1 ? slices_for(cls, flops) : 0;
+    p.use_tc = slices > 0;
+    OperandPlan& PM = p.P[0];
+    OperandPlan& PN = p.P[1];
+    PM.terms = Ms;
+    PN.terms = Ns;
+    PM.constant = constM;
+    PN.constant = constN;
+    PM.rows = p.M;
+    PN.rows = p.N;
+    PM.K = PN.K = K;
+    PM.ext = order_by(mext, c.lab);
+    PN.ext = order_by(next, c.lab);
+    // contracted-index order
+    const Ix& bigM = Ms[0].x;
+    const Ix& bigN = Ns[0].x;
+    if (!p.use_tc) {
+      const bool dM = Ms.size() == 1 && storage_is_panel(bigM, mext);
+      const bool dN = Ns.size() == 1 && storage_is_panel(bigN, next);
+      if (dM && (!dN || bigM.t->size() >= bigN.t->size())) {
+        PM.direct = true;
+        PM.ext = order_by(mext, bigM.lab);
+        PM.kord = order_by(kset, bigM.lab);
+        if (dN && order_by(kset, bigN.lab) == PM.kord) {
+          PN.direct = true;
+          PN.ext = order_by(next, bigN.lab);
+        }
+      } else if (dN) {
+        PN.direct = true;
+        PN.ext = order_by(next, bigN.lab);
+        PM.kord = order_by(kset, bigN.lab);
+      } else {
+        const Ix& ref = bigM.t->size() >= bigN.t->size() ? bigM : bigN;
+        PM.kord = order_by(kset, ref.lab);
+      }
+    } else {
+      // pack reads are cheapest along the storage order of the per-iteration operand
+      const Ix* ref = nullptr;
+      if (!constM && !constN) ref = bigM.t->size() >= bigN.t->size() ? &bigM : &bigN;
+      else if (!constM) ref = &bigM;
+      else if (!constN) ref = &bigN;
+      else ref = &bigM;
+      PM.kord = order_by(kset, ref->lab);
+    }
+    PN.kord = PM.kord;
+    double coef_direct = 1.0;
+    for (int side = 0; side < 2; ++side) {
+      OperandPlan& op = p.P[side];
+      if (op.direct) {
+        op.dptr = op.terms[0].x.t->d;
+        op.ld = op.K;
+        coef_direct *= op.terms[0].coef;
+        continue;
+      }
+      GatherArgs& g = op.gather;
+      std::memset(&g, 0, sizeof(g));
+      g.nterms = static_cast<int>(op.terms.size());
+      for (size_t t = 0; t < op.terms.size(); ++t) {
+        g.t[t].coef = op.terms[t].coef;
+        g.t[t].a = op.terms[t].x.t->d;
+        g.t[t].ra = upload(offsets(op.ext, e, op.terms[t].x)).d;
+        g.t[t].ca = upload(offsets(op.kord, e, op.terms[t].x)).d;
+      }
+      g.R = op.rows;
+      g.C = op.K;
+      if (!p.use_tc) {
+        g.Rpad = op.rows;
+        g.Cpad = op.K;
+        g.ldo = op.K;
+        g.beta = 0.0;
+        size_t need = static_cast<size_t>(op.rows * op.K);
+        if (side == 0) ws64_a_ = std::max(ws64_a_, need);
+        else ws64_b_ = std::max(ws64_b_, need);
+      }
+    }
+    p.alpha = alpha * coef_direct;
+    {
+      Ix cx = c;
+      p.cm = upload(offsets(p.P[0].ext, e, cx)).d;
+      p.cn = upload(offsets(p.P[1].ext, e, cx)).d;
+    }
+    if (p.use_tc) {
+      p.slices = slices;
+      p.bn = gemm_tc_pick_bn(p.N);
+      p.npairs = 0;
+      for (int a = 0; a < slices; ++a)
+        for (int b = 0; b < slices; ++b)
+          if (a + b < slices) {
+            p.pa[p.npairs] = a;
+            p.pb[p.npairs] = b;
+            ++p.npairs;
+          }
+      const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kTcBK);
+      for (int side = 0; side < 2; ++side) {
+        OperandPlan& op = p.P[side];
+        op.slices = slices;
+        op.Kpad = Kpad;
+        op.rows_pad = round_up(op.rows, side == 0 ? kTcBM : p.bn);
+        GatherArgs& g = op.gather;
+        g.Rpad = op.rows_pad;
+        g.Cpad = Kpad;
+        g.ldo = Kpad;
+        g.out = nullptr;
+        g.nslices = slices;
+        g.slice_stride = op.rows_pad * Kpad;
+        const size_t need = static_cast<size_t>(slices) * op.rows_pad * Kpad;
+        if (op.constant) {
+          op.pack_elems = need;  // allocated and packed by finalize(true)
+        } else if (side == 0) {
+          wsbf_a_ = std::max(wsbf_a_, need);
+        } else {
+          wsbf_b_ = std::max(wsbf_b_, need);
+        }
+      }
+    }
+  }
+}
+
+void Engine::finalize(bool prepack_mixed) {
+  if (!planned_) throw Error(GBCC_ERR_STATE, "engine: finalize before PLAN");
+  dev_free(w64a_);
+  dev_free(w64b_);
+  dev_free(wbfa_);
+  dev_free(wbfb_);
+  w64a_ = static_cast<double*>(dev_alloc(ws64_a_ * sizeof(double)));
+  w64b_ = static_cast<double*>(dev_alloc(ws64_b_ * sizeof(double)));
+  wbfa_ = static_cast<__nv_bfloat16*>(dev_alloc(wsbf_a_ * sizeof(__nv_bfloat16)));
+  wbfb_ = static_cast<__nv_bfloat16*>(dev_alloc(wsbf_b_ * sizeof(__nv_bfloat16)));
+  bytes_ += (ws64_a_ + ws64_b_) * sizeof(double) + (wsbf_a_ + wsbf_b_) * sizeof(__nv_bfloat16);
+  if (prepack_mixed) {
+    for (auto& sp : sites_) {
+      if (sp->kind != 1) continue;
+      GemmPlan& p = sp->plan[1];
+      if (!p.use_tc) continue;
+      for (int side = 0; side < 2; ++side) {
+        OperandPlan& op = p.P[side];
+        if (!op.constant) continue;
+        if (!op.packed) {
+          op.packed = static_cast<__nv_bfloat16*>(dev_alloc(op.pack_elems * sizeof(__nv_bfloat16)));
+          owned_.push_back(op.packed);
+          bytes_ += op.pack_elems * sizeof(__nv_bfloat16);
+        }
+        GatherArgs g = op.gather;
+        g.outs = op.packed;
+        launch_gather(g, stream_);
+      }
+    }
+    GBCC_CK(cudaGetLastError());
+  }
+}
+
+}  // namespace gbcc

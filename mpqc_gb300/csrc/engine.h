@@ -1,0 +1,168 @@
+// Tensor-contraction engine of the CCSD residual.
+//
+// A residual is written as a fixed sequence of two operations on dense FP64
+// device tensors addressed through index labels (the einstein notation of the
+// reference's TiledArray expressions, one character per index):
+//
+//   assign(C("a,b,i,j"), beta, {coef * X("...") [* Y("...")], ...})
+//   contract(C("a,b,i,j"), beta, alpha, A-terms("k,l,c,d"), B-terms("d,a,i,l"), class)
+//
+// The first pass over the program (PLAN) builds, for every call site, the
+// offset tables that map labels to strides, chooses GEMM geometry and sizes
+// the workspaces; later passes (EXEC) only launch kernels, so an EXEC pass can
+// be captured into a CUDA graph.  Every contraction runs as
+//   pack A, pack B (gather + linear combination, FP64 or split-BF16 slices)
+//   -> GEMM (FP64 DFMA kernel or tcgen05 split-BF16 kernel)
+//   -> scattered epilogue straight into C.
+// Constant operands (integrals) are packed once per input set.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gbcc.h"
+#include "kernels.h"
+
+namespace gbcc {
+
+struct Error : std::runtime_error {
+  gbcc_status status;
+  Error(gbcc_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define GBCC_CK(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      throw ::gbcc::Error(e_ == cudaErrorMemoryAllocation ? GBCC_ERR_OOM : GBCC_ERR_CUDA,  \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));           \
+  } while (0)
+
+void* dev_alloc(size_t bytes);
+void dev_free(void* p);
+
+struct Tensor {
+  std::string name;
+  double* d = nullptr;
+  int rank = 0;
+  int64_t dim[4] = {1, 1, 1, 1};
+  bool constant = false;  // never written after the inputs are set
+  int64_t size() const {
+    int64_t n = 1;
+    for (int k = 0; k < rank; ++k) n *= dim[k];
+    return n;
+  }
+  int64_t stride(int k) const {
+    int64_t s = 1;
+    for (int q = rank - 1; q > k; --q) s *= dim[q];
+    return s;
+  }
+};
+
+// A tensor with index labels, e.g. Ix(G, "klcd").
+struct Ix {
+  const Tensor* t = nullptr;
+  std::string lab;
+};
+inline Ix ix(const Tensor& t, const char* lab) { return Ix{&t, std::string(lab)}; }
+
+// coef * a [* b]
+struct Factor {
+  double coef;
+  Ix a;
+  Ix b;  // b.t == nullptr: single factor
+};
+inline Factor f1(double c, const Ix& a) { return Factor{c, a, Ix{}}; }
+inline Factor f2(double c, const Ix& a, const Ix& b) { return Factor{c, a, b}; }
+
+struct Lin {
+  double coef;
+  Ix x;
+};
+
+enum TermClass { kClassLadder = 0, kClassRing = 1, kClassOther = 2 };
+
+enum class Mode { kPlan, kExec };
+
+struct DevTable {
+  int64_t* d = nullptr;
+  int64_t n = 0;
+};
+
+struct Site;  // per call site plan
+
+class Engine {
+ public:
+  Engine();
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  void set_stream(cudaStream_t s) { stream_ = s; }
+  cudaStream_t stream() const { return stream_; }
+  void set_slices(int ladder, int ring, int other) {
+    slices_[0] = ladder;
+    slices_[1] = ring;
+    slices_[2] = other;
+  }
+  void set_error_word(int* err) { err_ = err; }
+
+  // Persistent device tensor owned by the engine (allocated on first request).
+  Tensor& tensor(const std::string& name, std::initializer_list<int64_t> dims, bool constant = false);
+  Tensor* find(const std::string& name);
+
+  // Program passes.  precision: GBCC_PREC_FP64 or GBCC_PREC_MIXED.
+  void begin(Mode m, int precision);
+  void end();
+  bool planned() const { return planned_; }
+  void reset_plans();  // inputs changed: rebuild everything on the next PLAN
+  // After a PLAN pass: allocate workspaces; pack constant operands for MIXED.
+  void finalize(bool prepack_mixed);
+
+  // C = beta*C + sum_t coef_t * a_t (* b_t); labels of each factor must be a
+  // subset of C's labels (missing labels broadcast).
+  void assign(const Ix& c, double beta, const std::vector<Factor>& terms);
+  // C = beta*C + alpha * sum_K (sum_s a_s A_s)(sum_t b_t B_t)
+  void contract(const Ix& c, double beta, double alpha, const std::vector<Lin>& A,
+                const std::vector<Lin>& B, TermClass cls);
+
+  // Statistics of the last EXEC pass (FLOPs of the contractions as planned).
+  double flops() const { return flops_; }
+  size_t device_bytes() const { return bytes_; }
+  int gemm_tc_launches() const { return n_tc_; }
+  int kernel_launches() const { return n_launch_; }
+
+ private:
+  Site& site();
+  DevTable upload(const std::vector<int64_t>& v);
+  int slices_for(TermClass cls, double flops) const;
+
+  cudaStream_t stream_ = nullptr;
+  Mode mode_ = Mode::kPlan;
+  int prec_ = GBCC_PREC_FP64;
+  int slices_[3] = {3, 3, 3};
+  size_t cursor_ = 0;
+  bool planned_ = false;
+  std::vector<std::unique_ptr<Site>> sites_;
+  std::unordered_map<std::string, std::unique_ptr<Tensor>> tensors_;
+  std::vector<void*> owned_;  // tables and constant-pack buffers
+  // shared workspaces (sized during PLAN)
+  size_t ws64_a_ = 0, ws64_b_ = 0, wsbf_a_ = 0, wsbf_b_ = 0;
+  double* w64a_ = nullptr;
+  double* w64b_ = nullptr;
+  __nv_bfloat16* wbfa_ = nullptr;
+  __nv_bfloat16* wbfb_ = nullptr;
+  int* err_ = nullptr;
+  double flops_ = 0.0;
+  size_t bytes_ = 0;
+  int n_tc_ = 0;
+  int n_launch_ = 0;
+};
+
+}  // namespace gbcc

@@ -1,0 +1,149 @@
+// Device kernels of the CCSD engine and their host-side launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace gbcc {
+
+// Error word written by bounded device-side waits; read by the host after a step.
+enum DeviceError : int { kDevOk = 0, kDevTimeout = 1, kDevBadArg = 2 };
+
+// ---------------------------------------------------------------------------
+// Gather / linear-combination kernel.
+//
+// The output is viewed as a 2-D array [R][C].  Element (r, c) of the result is
+//   sum_t coef_t * a_t[ra_t[r] + ca_t[c]] * (b_t ? b_t[rb_t[r] + cb_t[c]] : 1)
+// where ra/ca (rb/cb) are offset tables built on the host from the index
+// labels.  The same kernel permutes tensors, forms linear combinations such as
+// 2 G(k,l,c,d) - G(k,l,d,c), outer products t1(a,i) t1(b,j), and packs GEMM
+// operands as K-contiguous [M][K] panels (FP64 or split BF16 slices).
+// ---------------------------------------------------------------------------
+constexpr int kMaxTerms = 4;
+
+struct GatherTerm {
+  double coef;
+  const double* a;
+  const int64_t* ra;
+  const int64_t* ca;
+  const double* b;   // nullptr: single factor
+  const int64_t* rb;
+  const int64_t* cb;
+};
+
+struct GatherArgs {
+  int nterms;
+  GatherTerm t[kMaxTerms];
+  int64_t R, C;        // logical extent
+  int64_t Rpad, Cpad;  // written extent (zero outside R x C)
+  // FP64 output (out != nullptr): out[r*ldo + c] = beta*out + value
+  double* out;
+  int64_t ldo;
+  double beta;
+  // split output (outs != nullptr): nslices BF16 slices, slice s at outs + s*slice_stride
+  __nv_bfloat16* outs;
+  int nslices;
+  int64_t slice_stride;
+};
+
+void launch_gather(const GatherArgs& args, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// FP64 GEMM with scattered epilogue:
+//   C[cm[m] + cn[n]] = beta * C[...] + alpha * sum_k A[m*lda + k] * B[n*ldb + k]
+// for m < M, n < N (bounds-checked; operands need no padding).
+// ---------------------------------------------------------------------------
+struct GemmF64Args {
+  int64_t M, N, K;
+  const double* A;
+  int64_t lda;
+  const double* B;
+  int64_t ldb;
+  double* C;
+  const int64_t* cm;
+  const int64_t* cn;
+  double alpha, beta;
+};
+void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Split-BF16 tcgen05 GEMM (sm_103a):
+//   C[cm[m] + cn[n]] = beta*C + alpha * sum_{(p,q) in pairs} A_p[m][:] . B_q[n][:]
+// A_p: slice p of A, [Mpad][Kpad] bf16 K-contiguous; B_q likewise [Npad][Kpad].
+// Accumulation in FP32 (TMEM), recombination to FP64 in the epilogue.
+// ---------------------------------------------------------------------------
+constexpr int kMaxPairs = 9;
+struct GemmTcArgs {
+  int64_t M, N;          // logical
+  int64_t Mpad, Npad, Kpad;
+  const __nv_bfloat16* A; int a_slices;  // [a_slices][Mpad][Kpad]
+  const __nv_bfloat16* B; int b_slices;  // [b_slices][Npad][Kpad]
+  int npairs;
+  int pa[kMaxPairs], pb[kMaxPairs];
+  double* C;
+  const int64_t* cm;
+  const int64_t* cn;
+  double alpha, beta;
+  int bn;                // N tile (32, 64, 128 or 256)
+  int* err;              // device error word
+};
+// Returns false if the tensor maps could not be encoded (bad alignment / size).
+bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st);
+int gemm_tc_pick_bn(int64_t N);
+constexpr int kTcBM = 128;
+constexpr int kTcBK = 64;
+
+// ---------------------------------------------------------------------------
+// Deterministic FP64 reductions for the residual-augmented energy and the
+// residual norm (two passes, fixed grid, fixed order).
+//   out[0] = sum r1^2, out[1] = sum r2^2,
+//   out[2] = sum (f_ai + r1) t1, out[3] = sum (g_abij + r2)(2 tau - tau(b,a,i,j))
+// partial: scratch of kReduceBlocks * 4 doubles.
+// ---------------------------------------------------------------------------
+constexpr int kReduceBlocks = 608;
+void launch_energy_terms(int64_t o, int64_t v, const double* r1, const double* r2,
+                         const double* f_ai, const double* g_abij, const double* t1,
+                         const double* tau, double* partial, double* out, cudaStream_t st);
+
+// tau(a,b,i,j) = t2(a,b,i,j) + t1(a,i) t1(b,j)
+void launch_make_tau(int64_t o, int64_t v, const double* t1, const double* t2, double* tau,
+                     cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Jacobi update + DIIS bookkeeping (FP64).
+//   x_new = t + r / D stored in DIIS slot `slot`, e_new = r stored likewise,
+//   dots[j] = <e_new, e_j> for the nvec slots listed in `slots` (partials in
+//   scratch, reduced into Bmat row/column `slot`).
+// ---------------------------------------------------------------------------
+struct DiisArgs {
+  int64_t o, v;
+  const double* eps_o;
+  const double* eps_v;
+  const double* t1;
+  const double* t2;
+  const double* r1;
+  const double* r2;
+  double* x1;          // [ndiis][v*o]
+  double* x2;          // [ndiis][v*v*o*o]
+  double* e1;
+  double* e2;
+  int ndiis;
+  int slot;            // slot receiving the new pair
+  int nvec;            // stored pairs after insertion
+  int slots[16];       // age order, oldest first; slots[nvec-1] == slot
+  double* partial;     // scratch [kReduceBlocks][16]
+  double* Bmat;        // [ndiis][ndiis] by slot
+  double* coef;        // [ndiis] by slot (output of the solve)
+  double damping;
+  int extrapolate;     // 0: coefficients select the newest vector only
+  int* nskip_out;      // device int
+};
+void launch_diis_step(const DiisArgs& d, cudaStream_t st);
+
+// t1 = sum_j coef[j] x1_j, t2 = sum_j coef[j] x2_j, tau = t2 + t1 t1
+void launch_diis_extrapolate(int64_t o, int64_t v, const double* x1, const double* x2,
+                             const double* coef, int ndiis, const int* slots, int nvec,
+                             double* t1, double* t2, double* tau, cudaStream_t st);
+
+}  // namespace gbcc

@@ -1,0 +1,146 @@
+// Test hooks (include/gbcc_testing.h): single-kernel GEMM runs and an FP64
+// throughput probe.  Not used by the solver itself.
+#include <cstdio>
+#include <vector>
+
+#include "../../include/gbcc.h"
+#include "../../include/gbcc_testing.h"
+#include "engine.h"
+#include "kernels.h"
+
+namespace {
+
+int64_t rup(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+__global__ void fp64_fma_probe(double* out, int iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double m = 0.999999, c = 1e-7;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+  }
+  const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) out[0] = s;  // keeps the loop alive
+}
+
+}  // namespace
+
+extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
+                                 double* Cout, int slices, int repeat, float* ms) {
+  using namespace gbcc;
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1)
+    return GBCC_ERR_INVALID_ARG;
+  std::vector<void*> owned;
+  auto alloc = [&](size_t bytes) {
+    void* p = dev_alloc(bytes);
+    owned.push_back(p);
+    return p;
+  };
+  int status = GBCC_OK;
+  try {
+    cudaStream_t st = nullptr;
+    double* dA = static_cast<double*>(alloc(M * K * sizeof(double)));
+    double* dB = static_cast<double*>(alloc(N * K * sizeof(double)));
+    double* dC = static_cast<double*>(alloc(M * N * sizeof(double)));
+    int* err = static_cast<int*>(alloc(sizeof(int)));
+    GBCC_CK(cudaMemset(err, 0, sizeof(int)));
+    GBCC_CK(cudaMemcpy(dA, A, M * K * sizeof(double), cudaMemcpyDefault));
+    GBCC_CK(cudaMemcpy(dB, B, N * K * sizeof(double), cudaMemcpyDefault));
+    GBCC_CK(cudaMemset(dC, 0, M * N * sizeof(double)));
+    auto table = [&](int64_t n, int64_t stride) {
+      std::vector<int64_t> h(n);
+      for (int64_t i = 0; i < n; ++i) h[i] = i * stride;
+      int64_t* d = static_cast<int64_t*>(alloc(n * sizeof(int64_t)));
+      GBCC_CK(cudaMemcpy(d, h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
+      return d;
+    };
+    const int64_t* cm = table(M, N);
+    const int64_t* cn = table(N, 1);
+    cudaEvent_t e0, e1;
+    GBCC_CK(cudaEventCreate(&e0));
+    GBCC_CK(cudaEventCreate(&e1));
+    if (slices == 0) {
+      GemmF64Args g{};
+      g.M = M; g.N = N; g.K = K;
+      g.A = dA; g.lda = K; g.B = dB; g.ldb = K;
+      g.C = dC; g.cm = cm; g.cn = cn; g.alpha = 1.0; g.beta = 0.0;
+      launch_gemm_f64(g, st);
+      GBCC_CK(cudaEventRecord(e0, st));
+      for (int r = 0; r < repeat; ++r) launch_gemm_f64(g, st);
+      GBCC_CK(cudaEventRecord(e1, st));
+    } else {
+      const int bn = gemm_tc_pick_bn(N);
+      const int64_t Mpad = rup(M, kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
+      auto* sa = static_cast<__nv_bfloat16*>(alloc(slices * Mpad * Kpad * sizeof(__nv_bfloat16)));
+      auto* sb = static_cast<__nv_bfloat16*>(alloc(slices * Npad * Kpad * sizeof(__nv_bfloat16)));
+      auto pack = [&](const double* src, int64_t rows, int64_t rows_pad, __nv_bfloat16* dst) {
+        GatherArgs g{};
+        g.nterms = 1;
+        g.t[0].coef = 1.0;
+        g.t[0].a = src;
+        g.t[0].ra = table(rows, K);
+        g.t[0].ca = table(K, 1);
+        g.R = rows; g.C = K; g.Rpad = rows_pad; g.Cpad = Kpad; g.ldo = Kpad;
+        g.outs = dst; g.nslices = slices; g.slice_stride = rows_pad * Kpad;
+        launch_gather(g, st);
+      };
+      pack(dA, M, Mpad, sa);
+      pack(dB, N, Npad, sb);
+      GemmTcArgs t{};
+      t.M = M; t.N = N; t.Mpad = Mpad; t.Npad = Npad; t.Kpad = Kpad;
+      t.A = sa; t.a_slices = slices; t.B = sb; t.b_slices = slices;
+      for (int a = 0; a < slices; ++a)
+        for (int b = 0; b < slices; ++b)
+          if (a + b < slices) { t.pa[t.npairs] = a; t.pb[t.npairs] = b; ++t.npairs; }
+      t.C = dC; t.cm = cm; t.cn = cn; t.alpha = 1.0; t.beta = 0.0; t.bn = bn; t.err = err;
+      if (!launch_gemm_tc(t, st)) throw Error(GBCC_ERR_CUDA, "tcgen05 launch rejected");
+      GBCC_CK(cudaEventRecord(e0, st));
+      for (int r = 0; r < repeat; ++r) launch_gemm_tc(t, st);
+      GBCC_CK(cudaEventRecord(e1, st));
+    }
+    GBCC_CK(cudaEventSynchronize(e1));
+    GBCC_CK(cudaGetLastError());
+    float t_ms = 0.f;
+    GBCC_CK(cudaEventElapsedTime(&t_ms, e0, e1));
+    if (ms) *ms = t_ms / repeat;
+    int herr = 0;
+    GBCC_CK(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr != kDevOk) status = GBCC_ERR_TIMEOUT;
+    GBCC_CK(cudaMemcpy(Cout, dC, M * N * sizeof(double), cudaMemcpyDefault));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  } catch (const Error& e) {
+    std::fprintf(stderr, "gbcc_testing_gemm: %s\n", e.what());
+    status = e.status;
+  }
+  for (void* p : owned) dev_free(p);
+  return status;
+}
+
+extern "C" int gbcc_testing_fp64_peak(double* gflops) {
+  using namespace gbcc;
+  if (!gflops) return GBCC_ERR_INVALID_ARG;
+  try {
+    int dev = 0, sms = 0;
+    GBCC_CK(cudaGetDevice(&dev));
+    GBCC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* out = static_cast<double*>(dev_alloc(sizeof(double)));
+    const int blocks = sms * 8, threads = 256, iters = 1 << 16;
+    fp64_fma_probe<<<blocks, threads>>>(out, 1024);
+    cudaEvent_t e0, e1;
+    GBCC_CK(cudaEventCreate(&e0));
+    GBCC_CK(cudaEventCreate(&e1));
+    GBCC_CK(cudaEventRecord(e0));
+    fp64_fma_probe<<<blocks, threads>>>(out, iters);
+    GBCC_CK(cudaEventRecord(e1));
+    GBCC_CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    GBCC_CK(cudaEventElapsedTime(&ms, e0, e1));
+    dev_free(out);
+    *gflops = 2.0 * 8.0 * iters * static_cast<double>(blocks) * threads / (ms * 1e-3) / 1e9;
+    return GBCC_OK;
+  } catch (const Error& e) {
+    return e.status;
+  }
+}

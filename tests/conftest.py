@@ -1,0 +1,49 @@
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+GOLDEN = ROOT / "tests" / "golden"
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 (sm_103a) device and the built libgbcc")
+
+
+def load_golden(name):
+    """Fixture inputs rebuilt from the stored DF factor, plus stored outputs."""
+    from mpqc_gb300 import synth
+    z = np.load(GOLDEN / f"{name}.npz")
+    o, v = int(z["o"]), int(z["v"])
+    t1 = z["t1"] if "t1" in z else np.zeros((v, o))
+    t2 = z["t2"] if "t2" in z else np.zeros((v, v, o, o))
+    inp = synth.inputs_from_factor(z["B"], z["eps_o"], z["eps_v"], t1, t2)
+    return inp, {k: z[k] for k in z.files}
+
+
+def ints_dict(inp):
+    return {k: np.ascontiguousarray(getattr(inp, k)) for k in
+            ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc", "Gabcd")}
+
+
+def oracle_ints(inp):
+    from oracle import ccsd_ref as R
+    return R.Integrals(**ints_dict(inp))
+
+
+def rel_err(x, ref):
+    scale = max(float(np.max(np.abs(ref))), 1e-300)
+    return float(np.max(np.abs(np.asarray(x) - ref))) / scale
+
+
+@pytest.fixture(scope="session")
+def gbcc_lib():
+    """Build (if stale) and load libgbcc; GPU tests only."""
+    from mpqc_gb300 import build
+    build.build()
+    from mpqc_gb300 import _lib
+    return _lib.load()

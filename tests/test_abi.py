@@ -1,0 +1,107 @@
+"""CPU checks of the C-ABI library: it builds for sm_103a, loads, exports
+every symbol include/gbcc.h declares, and rejects bad input with a status
+code (no compute calls: there is no GPU on this host)."""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mpqc_gb300 import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "gbcc.h").read_text()
+    body = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gbcc_[a-z_]+)\s*\(", body)))
+
+
+def test_header_and_binding_agree():
+    from mpqc_gb300 import _lib
+    assert declared_symbols() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    assert lib.gbcc_abi_version() == 1
+
+
+def test_defaults_follow_the_reference(lib):
+    from mpqc_gb300._lib import Config
+    c = Config()
+    lib.gbcc_config_default(C.byref(c))
+    # ccsd.h:104 max_iter 30; cc/solvers.h:93-95 DIIS; energy.h:45 precision 1e-9
+    assert c.max_iter == 30 and c.n_diis == 8 and c.diis_start == 1
+    assert c.diis_damp == 0.0 and c.diis_ngroup == 1 and c.diis_group_nstart == 1
+    assert c.target_precision == 1e-9 and c.precision == 0
+
+
+@pytest.mark.parametrize("field,value", [("o", 0), ("v", -1), ("n_diis", 0), ("n_diis", 17),
+                                         ("slices_ladder", 4), ("precision", 7), ("max_iter", 0),
+                                         ("target_precision", 0.0), ("diis_damp", -1.0)])
+def test_create_rejects_bad_config(lib, field, value):
+    from mpqc_gb300._lib import Config, GBCC_ERR_INVALID_ARG
+    c = Config()
+    lib.gbcc_config_default(C.byref(c))
+    c.o, c.v = 4, 8
+    setattr(c, field, value)
+    h = C.c_void_p()
+    assert lib.gbcc_create(C.byref(h), C.byref(c)) == GBCC_ERR_INVALID_ARG
+    assert not h.value
+    assert lib.gbcc_last_error(None).decode().startswith("gbcc_create")
+
+
+def test_null_arguments(lib):
+    from mpqc_gb300._lib import GBCC_ERR_INVALID_ARG, GBCC_OK
+    assert lib.gbcc_create(None, None) == GBCC_ERR_INVALID_ARG
+    assert lib.gbcc_destroy(None) == GBCC_OK
+    assert lib.gbcc_residual(None, None, None, None, None) == GBCC_ERR_INVALID_ARG
+    assert lib.gbcc_solve(None, None, None, None, None) == GBCC_ERR_INVALID_ARG
+    assert lib.gbcc_status_string(4).decode() == "not converged"
+
+
+def test_create_without_gpu_fails_cleanly(lib):
+    from mpqc_gb300._lib import Config, GBCC_ERR_CUDA, GBCC_OK
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    c = Config()
+    lib.gbcc_config_default(C.byref(c))
+    c.o, c.v = 2, 3
+    h = C.c_void_p()
+    st = lib.gbcc_create(C.byref(h), C.byref(c))
+    assert st == GBCC_ERR_CUDA and not h.value
+    assert lib.gbcc_last_error(None)
+
+
+def test_keyval_front_end_validation():
+    from mpqc_gb300 import CCSD, FeatureDisabled, InputError
+    with pytest.raises(InputError):
+        CCSD({})
+    with pytest.raises(InputError):
+        CCSD({"ref": "scf", "method": "bogus"})
+    with pytest.raises(FeatureDisabled):
+        CCSD({"ref": "scf", "method": "df"})
+    with pytest.raises(FeatureDisabled):
+        CCSD({"ref": "scf", "solver": "pno"})
+    c = CCSD({"ref": "scf"})
+    assert c.max_iter == 30 and c.precision == 1e-9
+    with pytest.raises(RuntimeError):
+        c.t1()
+
+
+def test_array_checks():
+    from mpqc_gb300.ccsd import _ptr, InputError
+    with pytest.raises(InputError):
+        _ptr(np.zeros(3, dtype=np.float32))
+    with pytest.raises(InputError):
+        _ptr(np.zeros((3, 4))[:, ::2])
+    assert _ptr(np.zeros(3)) != 0

@@ -1,0 +1,61 @@
+"""GPU checks of the two GEMM kernels in isolation (FP64 DFMA kernel and the
+split-BF16 tcgen05 kernel) against a NumPy FP64 product, through the
+library's test hook."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(1, 1, 1), (128, 64, 64), (200, 100, 70), (300, 33, 500), (129, 257, 1000), (64, 256, 128),
+          (1000, 32, 40), (96, 1024, 64)]
+
+# max |C - C_ref| / max |C_ref| allowed per slice count (0 = FP64 kernel)
+TOL = {0: 1e-13, 1: 3e-2, 2: 2e-4, 3: 5e-6}
+
+
+@pytest.fixture(scope="module")
+def tlib(gbcc_lib):
+    lib = gbcc_lib
+    lib.gbcc_testing_gemm.restype = C.c_int
+    lib.gbcc_testing_gemm.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_int, C.c_int, C.POINTER(C.c_float)]
+    lib.gbcc_testing_fp64_peak.restype = C.c_int
+    lib.gbcc_testing_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    return lib
+
+
+def run(tlib, A, B, slices):
+    M, K = A.shape
+    N = B.shape[0]
+    out = np.empty((M, N))
+    ms = C.c_float()
+    st = tlib.gbcc_testing_gemm(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, slices, 1, C.byref(ms))
+    assert st == 0, st
+    return out
+
+
+@pytest.mark.parametrize("slices", [0, 1, 2, 3])
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_gemm_matches_fp64(tlib, M, N, K, slices):
+    rng = np.random.default_rng(M * 7 + N * 3 + K)
+    A = rng.normal(size=(M, K)) * np.exp(rng.uniform(-3, 3, size=(M, K)))
+    B = rng.normal(size=(N, K))
+    ref = A @ B.T
+    out = run(tlib, A, B, slices)
+    scale = np.max(np.abs(ref))
+    assert np.max(np.abs(out - ref)) <= TOL[slices] * scale
+
+
+def test_gemm_repeat_is_deterministic(tlib):
+    rng = np.random.default_rng(1)
+    A = rng.normal(size=(257, 300))
+    B = rng.normal(size=(130, 300))
+    assert np.array_equal(run(tlib, A, B, 3), run(tlib, A, B, 3))
+
+
+def test_fp64_probe_runs(tlib):
+    g = C.c_double()
+    assert tlib.gbcc_testing_fp64_peak(C.byref(g)) == 0
+    assert g.value > 10.0

@@ -1,0 +1,139 @@
+"""Parity of the CUDA residual engine and solver with the FP64 oracle,
+called through the C ABI (mpqc_gb300.Solver -> libgbcc)."""
+import numpy as np
+import pytest
+
+from conftest import ints_dict, load_golden, oracle_ints, rel_err
+from mpqc_gb300 import Solver, synth
+from mpqc_gb300._lib import GbccError
+from oracle import ccsd_ref as R
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12          # max|dr| / max|r_ref|, plain FP64 path
+MIXED_TOL = {3: 2e-5, 2: 5e-4, 1: 5e-2}   # split-BF16 path, by slice count
+
+
+def _solver(inp, precision="fp64", slices=(3, 3, 3), **kw):
+    s = Solver(inp.o, inp.v, precision=precision, slices=slices, **kw)
+    s.set_inputs(inp.eps_o, inp.eps_v, **ints_dict(inp))
+    return s
+
+
+@pytest.mark.parametrize("name", ["residual_o3_v7", "residual_o5_v19"])
+def test_residual_fp64_golden(name):
+    inp, g = load_golden(name)
+    with _solver(inp) as s:
+        r1, r2 = s.residual(g["t1"], g["t2"])
+    assert rel_err(r1, g["r1"]) < FP64_TOL
+    assert rel_err(r2, g["r2"]) < FP64_TOL
+
+
+@pytest.mark.parametrize("o,v,naux", [(1, 1, 3), (1, 2, 4), (2, 3, 5), (4, 9, 12), (3, 33, 20),
+                                      (7, 12, 16), (8, 40, 30)])
+def test_residual_fp64_random(o, v, naux):
+    inp = synth.make_inputs(o, v, naux, seed=o * 100 + v, t1_scale=1e-2)
+    r1_ref, r2_ref = R.residual(inp.t1, inp.t2, oracle_ints(inp))
+    with _solver(inp) as s:
+        r1, r2 = s.residual(inp.t1, inp.t2)
+    assert rel_err(r1, r1_ref) < FP64_TOL
+    assert rel_err(r2, r2_ref) < FP64_TOL
+    assert np.allclose(r2, r2.transpose(1, 0, 3, 2), rtol=0, atol=1e-14 * np.max(np.abs(r2)))
+
+
+@pytest.mark.parametrize("slices", [3, 2, 1])
+@pytest.mark.parametrize("o,v,naux", [(4, 9, 12), (8, 40, 30), (12, 70, 60)])
+def test_residual_mixed(o, v, naux, slices):
+    inp = synth.make_inputs(o, v, naux, seed=o * 10 + v, t1_scale=1e-2)
+    r1_ref, r2_ref = R.residual(inp.t1, inp.t2, oracle_ints(inp))
+    with _solver(inp, precision="mixed", slices=(slices,) * 3) as s:
+        r1, r2 = s.residual(inp.t1, inp.t2)
+        f1, f2 = s.residual(inp.t1, inp.t2, precision="fp64")
+    assert rel_err(r2, r2_ref) < MIXED_TOL[slices]
+    assert rel_err(r1, r1_ref) < MIXED_TOL[slices]
+    assert rel_err(f2, r2_ref) < FP64_TOL
+
+
+def test_residual_repeat_identical():
+    inp = synth.make_inputs(5, 20, 16, seed=3, t1_scale=1e-2)
+    with _solver(inp, precision="mixed") as s:
+        a = s.residual(inp.t1, inp.t2)
+        b = s.residual(inp.t1, inp.t2)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_energy_matches_oracle():
+    inp = synth.make_inputs(4, 11, 12, seed=9, t1_scale=1e-2)
+    r1, r2 = R.residual(inp.t1, inp.t2, oracle_ints(inp))
+    with _solver(inp) as s:
+        e, err = s.energy(inp.t1, inp.t2, r1, r2)
+    tau = R.make_tau(inp.t1, inp.t2)
+    g = inp.Gijab.transpose(2, 3, 0, 1)
+    e_ref = 2 * np.vdot(inp.Fia.T + r1, inp.t1) + np.vdot(g + r2, 2 * tau - tau.transpose(1, 0, 2, 3))
+    assert abs(e - e_ref) < 1e-13 * max(1.0, abs(e_ref))
+    assert abs(err - R.solver_error(r1, r2)) < 1e-15 + 1e-12 * err
+
+
+def test_solve_fp64_golden():
+    inp, g = load_golden("solve_o3_v8")
+    with _solver(inp, target_precision=1e-11, max_iter=60) as s:
+        e, t1, t2, rep = s.solve()
+    assert rep.converged and rep.iters == int(g["iters"])
+    assert abs(e - float(g["e_corr"])) < 1e-10
+    assert np.max(np.abs(t2 - g["t2"])) < 1e-9
+    assert np.max(np.abs(t1 - g["t1"])) < 1e-9
+
+
+@pytest.mark.parametrize("o,v,naux,seed", [(3, 10, 14, 21), (5, 19, 30, 22), (6, 30, 40, 23)])
+def test_solve_fp64_random(o, v, naux, seed):
+    inp = synth.make_inputs(o, v, naux, seed=seed)
+    ref = R.solve_ccsd(oracle_ints(inp), inp.eps_o, inp.eps_v, target_precision=1e-10, max_iter=60)
+    with _solver(inp, target_precision=1e-10, max_iter=60) as s:
+        e, t1, t2, rep = s.solve()
+    assert rep.converged == ref.converged and rep.iters == ref.iters
+    assert abs(e - ref.e_corr) < 1e-9
+    assert np.max(np.abs(t2 - ref.t2)) < 1e-7
+
+
+def test_solve_mixed_with_fp64_refinement():
+    inp = synth.make_inputs(8, 40, 40, seed=31)
+    ref = R.solve_ccsd(oracle_ints(inp), inp.eps_o, inp.eps_v, target_precision=1e-10, max_iter=60)
+    with _solver(inp, precision="mixed", target_precision=1e-10, max_iter=60, refine_iters=2) as s:
+        e, t1, t2, rep = s.solve()
+    assert rep.converged and rep.mixed_iters > 0 and rep.fp64_iters >= 2
+    assert abs(e - ref.e_corr) < 1e-6
+    assert np.max(np.abs(t2 - ref.t2)) < 1e-6
+
+
+def test_device_pointers_match_host():
+    torch = pytest.importorskip("torch")
+    inp = synth.make_inputs(4, 13, 12, seed=5, t1_scale=1e-2)
+    with _solver(inp) as s:
+        h1, h2 = s.residual(inp.t1, inp.t2)
+        d1, d2 = s.residual(torch.from_numpy(inp.t1).cuda(), torch.from_numpy(inp.t2).cuda())
+    assert np.array_equal(h1, d1.cpu().numpy()) and np.array_equal(h2, d2.cpu().numpy())
+
+
+def test_call_order_and_argument_errors():
+    inp = synth.make_inputs(2, 5, 6, seed=1)
+    s = Solver(2, 5)
+    with pytest.raises(GbccError) as e:
+        s.residual(inp.t1, inp.t2)
+    assert e.value.status == 6  # GBCC_ERR_STATE
+    bad = dict(ints_dict(inp))
+    eps_o = inp.eps_o.copy()
+    eps_o[0] = np.nan
+    with pytest.raises(GbccError) as e:
+        s.set_inputs(eps_o, inp.eps_v, **bad)
+    assert e.value.status == 1  # GBCC_ERR_INVALID_ARG
+    s.set_inputs(inp.eps_o, inp.eps_v, **bad)
+    r1, r2 = s.residual(inp.t1, inp.t2)
+    assert np.all(np.isfinite(r2))
+    s.close()
+
+
+def test_max_iter_reports_not_converged():
+    inp = synth.make_inputs(3, 8, 10, seed=2)
+    with _solver(inp, max_iter=2) as s:
+        e, t1, t2, rep = s.solve()
+    assert not rep.converged and rep.iters == 2 and np.isfinite(e)
