@@ -1,0 +1,382 @@
+"""Benchmark: CCSD residual throughput on one GB300 (one JSON line on stdout).
+
+Workload: the synthetic CCSD doubles residual -- one R1 + R2 evaluation, no
+molecule -- with o = 32 occupied and v = 320 virtual orbitals and a density-
+fitted integral set of naux = 1200 auxiliary functions.  The integrals are
+built on the device from a seeded DF factor B[Q,p,q] ~ N(0, 0.05) (symmetrised)
+as <pq|rs> = sum_Q B[Q,p,r] B[Q,q,s] (the v^4 block (ab|cd) alone is 84 GB in
+FP64); t2 ~ N(0, 1e-2) symmetrised, t1 ~ N(0, 1e-3); eps_occ ~ U(-1.5,-0.3),
+eps_virt ~ U(0.1,3.0).  Inputs (about 150 GB touched per residual) exceed the
+129 MB L2 many times over, so no L2 flush is needed between steps.
+
+Reported (one JSON line):
+  value      algorithmic TFLOP/s of the mixed-precision residual, F(o,v) / (s/iter),
+             F = 2o^2v^4 + 12o^3v^3 + 4o^4v^2 + 14o^2v^3 + 18o^3v^2, inputs resident in HBM
+  e2e        the same through the C ABI with host (pinned) t1/t2 in and r1/r2 out
+  fp64       the plain-FP64 residual on the same inputs (s/iter, TFLOP/s)
+  roofline   the particle-particle ladder GEMM (dominant kernel) against the BF16 tensor peak
+  cpu_baseline  the FP64 oracle on the host cores on a bounded sample (o=32, v=96)
+
+--impl reference times the FP64 CPU oracle (the restatement of the reference's
+CPU path; the reference itself cannot be built here) on that bounded sample.
+Multi-GPU (torchrun): every rank runs an independent replica ("replicas only",
+weak scaling); value = sum of all ranks' FLOPs / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "CCSD s/iter and residual TFLOP/s, mixed vs plain-FP64 on 1 GB300 at |ΔE|≤1e-6 Eh"
+CPU_SAMPLE = (32, 96, 200)   # o, v, naux of the bounded CPU sample
+
+
+def flop_count(o, v):
+    return 2 * o**2 * v**4 + 12 * o**3 * v**3 + 4 * o**4 * v**2 + 14 * o**2 * v**3 + 18 * o**3 * v**2
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline / reference arm: the FP64 oracle on a bounded sample
+
+def cpu_residual_rate(steps, warmup):
+    from mpqc_gb300 import synth
+    from oracle import ccsd_ref as R
+    o, v, naux = CPU_SAMPLE
+    inp = synth.make_inputs(o, v, naux, seed=1, t1_scale=1e-3)
+    ints = R.Integrals(inp.Fia, inp.Fij, inp.Fab, inp.Gijab, inp.Gijkl, inp.Giajb, inp.Gijka,
+                       inp.Giabc, inp.Gabcd)
+    for _ in range(warmup):
+        R.residual(inp.t1, inp.t2, ints)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        R.residual(inp.t1, inp.t2, ints)
+    dt = (time.perf_counter() - t0) / steps
+    return flop_count(o, v) / dt / 1e12, dt
+
+
+def cpu_threads():
+    try:
+        from threadpoolctl import threadpool_info
+        n = [i.get("num_threads") for i in threadpool_info() if i.get("user_api") == "blas"]
+        if n:
+            return int(max(n))
+    except Exception:
+        pass
+    return os.cpu_count() or 1
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if ws > 1 and rank != 0:
+        return 0
+    o, v, naux = CPU_SAMPLE
+    rate, dt = cpu_residual_rate(max(1, args.steps), max(0, args.warmup))
+    line = {
+        "metric": METRIC, "value": rate, "unit": "TFLOP/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "synthetic CCSD doubles residual, one R1+R2 evaluation",
+                   "o": o, "v": v, "naux": naux, "note": "bounded CPU sample of the o=32 v=320 workload"},
+        "cpu_baseline": {"value": rate, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
+                         "sample": f"one FP64 R1+R2 residual at o={o} v={v} naux={naux} per step "
+                                   "(numpy/OpenBLAS restatement of the reference's CPU CCSD)"},
+        "e2e": {"value": rate, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# device-side input generation
+
+class _DevArray:
+    """Zero-copy torch view of a device buffer owned by the library."""
+
+    def __init__(self, ptr, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(int(s) for s in shape), "typestr": "<f8",
+                                         "data": (int(ptr), False), "version": 3, "strides": None}
+
+
+def build_inputs(torch, solver, o, v, naux, seed, dev):
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    n = o + v
+    B = torch.randn((naux, n, n), generator=g, device=dev, dtype=torch.float64) * 0.05
+    B = (B + B.transpose(1, 2)) * (0.5 ** 0.5)
+    eps_o = torch.sort(torch.rand(o, generator=g, device=dev, dtype=torch.float64) * 1.2 - 1.5).values
+    eps_v = torch.sort(torch.rand(v, generator=g, device=dev, dtype=torch.float64) * 2.9 + 0.1).values
+    t2 = torch.randn((v, v, o, o), generator=g, device=dev, dtype=torch.float64) * 1e-2
+    t2 = 0.5 * (t2 + t2.permute(1, 0, 3, 2))
+    t1 = torch.randn((v, o), generator=g, device=dev, dtype=torch.float64) * 1e-3
+    ptr = solver.device_inputs()
+    view = lambda name, shape: torch.as_tensor(_DevArray(ptr[name], shape), device=dev)  # noqa: E731
+    view("eps_o", (o,)).copy_(eps_o)
+    view("eps_v", (v,)).copy_(eps_v)
+    view("Fia", (o, v)).zero_()
+    view("Fij", (o, o)).copy_(torch.diag(eps_o))
+    view("Fab", (v, v)).copy_(torch.diag(eps_v))
+    Bf = B.float()
+    Boo, Bov, Bvv = Bf[:, :o, :o], Bf[:, :o, o:], Bf[:, o:, o:]
+
+    def blk(x, y):  # <pq|rs> = sum_Q x[Q,p,r] y[Q,q,s], built in FP32, stored FP64
+        return torch.einsum("Qpr,Qqs->pqrs", x, y).double()
+
+    view("Gijab", (o, o, v, v)).copy_(blk(Bov, Bov))
+    view("Gijkl", (o, o, o, o)).copy_(blk(Boo, Boo))
+    view("Giajb", (o, v, o, v)).copy_(blk(Boo, Bvv))
+    view("Gijka", (o, o, o, v)).copy_(blk(Boo, Bov))
+    Giabc = view("Giabc", (o, v, v, v))
+    for i in range(o):
+        Giabc[i].copy_(torch.einsum("Qr,Qqs->qrs", Bov[:, i, :], Bvv).double())
+    Gabcd = view("Gabcd", (v, v, v, v))
+    Y = Bvv.reshape(naux, v * v)                      # (Q, b d)
+    step = 8
+    for a0 in range(0, v, step):
+        a1 = min(v, a0 + step)
+        X = Bvv[:, a0:a1, :].permute(1, 2, 0).reshape((a1 - a0) * v, naux)   # (a c, Q)
+        P = (X @ Y).reshape(a1 - a0, v, v, v)                                # (a, c, b, d)
+        Gabcd[a0:a1].copy_(P.permute(0, 2, 1, 3))
+    del X, Y, P, B, Bf
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    solver.commit_inputs()
+    return t1.contiguous(), t2.contiguous()
+
+
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"gbcc_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in self.path.read_text().strip().splitlines() if r.strip()]
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if len(r) > 5 + k and "Active" in r[5 + k]
+                          and "Not" not in r[5 + k]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        return {}
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the ladder GEMM from the committed ncu summary."""
+    p = ROOT / "profiles" / "ladder_gemm_o32_v320.md"
+    try:
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except Exception:
+        pass
+    return None
+
+
+def ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    from mpqc_gb300 import build as gb
+    gb.build()
+    from mpqc_gb300 import Solver
+    o, v, naux = args.o, args.v, args.naux
+    F = flop_count(o, v)
+    log(f"[bench] rank {rank}: building inputs o={o} v={v} naux={naux} on {torch.cuda.get_device_name(dev)}")
+    t_setup = time.perf_counter()
+    s = Solver(o, v, precision="mixed", slices=(args.slices,) * 3, device=local)
+    t1, t2 = build_inputs(torch, s, o, v, naux, args.seed, dev)
+    log(f"[bench] inputs + split packing ready in {time.perf_counter() - t_setup:.1f} s")
+    r1 = torch.empty_like(t1)
+    r2 = torch.empty_like(t2)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- mixed precision, device-resident inputs
+    for _ in range(args.warmup):
+        s.residual(t1, t2, r1, r2, precision="mixed")
+    launches = s.last_launches()
+    barrier()
+    with ClockSampler(local) as clk:
+        s.record(0)
+        for _ in range(args.steps):
+            s.residual(t1, t2, r1, r2, precision="mixed")
+        s.record(1)
+        ms = s.elapsed_ms(0, 1)
+    barrier()
+    ms_step = ms / args.steps
+    if ws > 1:
+        tt = torch.tensor([ms_step], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(tt.item())
+    value = ws * F / (ms_step * 1e-3) / 1e12
+    r2_mixed = r2.clone()
+
+    # ---- end to end through the C ABI: pinned host buffers, copies inside the timed region
+    h_t1 = torch.empty(t1.shape, dtype=torch.float64, pin_memory=True)
+    h_t2 = torch.empty(t2.shape, dtype=torch.float64, pin_memory=True)
+    h_r1 = torch.empty(t1.shape, dtype=torch.float64, pin_memory=True)
+    h_r2 = torch.empty(t2.shape, dtype=torch.float64, pin_memory=True)
+    h_t1.copy_(t1)
+    h_t2.copy_(t2)
+    a_t1, a_t2, a_r1, a_r2 = (x.numpy() for x in (h_t1, h_t2, h_r1, h_r2))
+    s.residual(a_t1, a_t2, a_r1, a_r2, precision="mixed")
+    barrier()
+    e2e_steps = max(1, min(args.steps, 3))
+    s.record(2)
+    for _ in range(e2e_steps):
+        s.residual(a_t1, a_t2, a_r1, a_r2, precision="mixed")
+    s.record(3)
+    e2e_ms = s.elapsed_ms(2, 3) / e2e_steps
+    e2e_value = ws * F / (e2e_ms * 1e-3) / 1e12
+    bytes_io = (t1.numel() + t2.numel()) * 8
+
+    # ---- per-term profile and roofline of the dominant kernel (ladder GEMM)
+    prof = s.profile_residual(precision="mixed")
+    pk = peaks()
+    ladder = [p for p in prof if p["cls"] == 0]
+    roof = None
+    if ladder and ladder[0]["gemm_ms"] > 0:
+        lp = ladder[0]
+        executed = lp["pairs"] * lp["flops"]
+        peak = pk.get("bf16_tflops_sustained") or 1700.0
+        ach = executed / (lp["gemm_ms"] * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": ncu_traffic(), "kernel": "gemm_tc_kernel (particle-particle ladder)",
+                "executed_flops_per_launch": executed, "launch_ms": lp["gemm_ms"],
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"}
+    terms = {}
+    for p in prof:
+        key = {0: "ladder", 1: "ring", 2: "other", -1: "elementwise"}[p["cls"]]
+        terms[key] = terms.get(key, 0.0) + p["ms"]
+
+    # ---- plain FP64 residual on the same inputs
+    fp64 = None
+    if args.fp64_steps > 0:
+        s.residual(t1, t2, r1, r2, precision="fp64")
+        barrier()
+        s.record(4)
+        for _ in range(args.fp64_steps):
+            s.residual(t1, t2, r1, r2, precision="fp64")
+        s.record(5)
+        f_ms = s.elapsed_ms(4, 5) / args.fp64_steps
+        err = float((r2_mixed - r2).abs().max() / r2.abs().max())
+        fp64 = {"s_per_iter": f_ms * 1e-3, "tflops": F / (f_ms * 1e-3) / 1e12, "steps": args.fp64_steps,
+                "warmup": 1, "mixed_speedup": f_ms / ms_step,
+                "mixed_vs_fp64_max_rel_err_r2": err}
+    s.close()
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu:
+        rate, dt = cpu_residual_rate(1, 1)
+        o_, v_, n_ = CPU_SAMPLE
+        cpu = {"value": rate, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"one FP64 R1+R2 residual of the oracle at o={o_} v={v_} naux={n_} ({dt:.2f} s)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "s_per_iter": ms_step * 1e-3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "synthetic CCSD doubles residual, one R1+R2 evaluation",
+                   "o": o, "v": v, "naux": naux, "parallelism": f"replicas{ws}",
+                   "precision": f"split-BF16 x{args.slices} slices, float-float chunk accumulation",
+                   "flops_per_step": F, "l2": "inputs larger than L2 (no flush)"},
+        "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": bytes_io,
+                "d2h_bytes_per_step": bytes_io, "ms_per_step": e2e_ms},
+        "fp64": fp64,
+        "roofline": roof,
+        "term_ms": terms,
+        "gpu_launches": launches * args.steps,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--o", type=int, default=32)
+    ap.add_argument("--v", type=int, default=320)
+    ap.add_argument("--naux", type=int, default=1200)
+    ap.add_argument("--slices", type=int, default=3)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -124,6 +124,16 @@ gbcc_status gbcc_create(gbcc_handle** out, const gbcc_config* cfg);
  * mixed mode).  May be called again to replace the inputs. */
 gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in);
 
+/* Zero-copy alternative to gbcc_set_inputs for integrals too large to hold
+ * twice in device memory (the v^4 (ab|cd) block is 84 GB at v = 320):
+ * gbcc_device_inputs returns, in *out, device pointers to the handle's own
+ * input arrays (writable, same layouts as gbcc_inputs); the caller fills
+ * them on the device and then calls gbcc_commit_inputs, which validates the
+ * orbital energies and prepares the contractions as gbcc_set_inputs does.
+ * No counterpart in the reference (its integrals live in TiledArray arrays). */
+gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out);
+gbcc_status gbcc_commit_inputs(gbcc_handle* h);
+
 /* One residual: tau = t2 + t1 t1, R1 then R2 (R1 sets the FIJ/FAB
  * intermediates R2 reads), in the handle's precision. */
 gbcc_status gbcc_residual(gbcc_handle* h, const double* t1_ai, const double* t2_abij,

@@ -25,6 +25,35 @@ int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const do
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);
 
+/* One residual on the device-resident amplitudes of handle h (t1/t2 as left
+ * by the previous gbcc_residual / gbcc_solve call) with CUDA events around
+ * every operation of the residual program.  For each of the first
+ * max_sites operations writes: its time in ms, its algorithmic FLOPs
+ * (2 M N K, 0 for elementwise operations), the number of BF16 slice
+ * products it executed on the tensor cores (0: FP64 kernel or elementwise)
+ * and its term class (0 ladder, 1 ring, 2 other, -1 elementwise).
+ * *nsites receives the number of operations. */
+struct gbcc_handle;
+int gbcc_testing_profile_residual(struct gbcc_handle* h, int precision, int max_sites, double* ms,
+                                  double* flops, int* pairs, int* cls, int* nsites);
+
+/* Kernel launches of the last residual (every kernel of this library). */
+int gbcc_testing_last_launches(struct gbcc_handle* h, int* launches);
+
+/* Record timing event `slot` (0..7) on the handle's CUDA stream, and read the
+ * milliseconds between two recorded slots (waits for the second). */
+int gbcc_testing_record(struct gbcc_handle* h, int slot);
+int gbcc_testing_elapsed(struct gbcc_handle* h, int slot0, int slot1, float* ms);
+
+/* GEMM-kernel-only time (ms) of each operation in the last profiled residual
+ * (0 for elementwise operations); same indexing as
+ * gbcc_testing_profile_residual. */
+int gbcc_testing_profile_gemm_ms(struct gbcc_handle* h, int max_sites, double* ms);
+
+/* GEMM shape (M, N, K) of each operation of the last profiled residual,
+ * three int64 per operation (elementwise operations: rows, columns, 0). */
+int gbcc_testing_profile_dims(struct gbcc_handle* h, int max_sites, int64_t* mnk);
+
 #ifdef __cplusplus
 }
 #endif

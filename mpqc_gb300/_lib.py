@@ -23,9 +23,13 @@ PREC_MIXED = 1
 # every symbol include/gbcc.h declares
 EXPORTS = (
     "gbcc_abi_version", "gbcc_status_string", "gbcc_config_default", "gbcc_create",
-    "gbcc_set_inputs", "gbcc_residual", "gbcc_residual_ex", "gbcc_energy", "gbcc_solve",
-    "gbcc_destroy", "gbcc_last_error",
+    "gbcc_set_inputs", "gbcc_device_inputs", "gbcc_commit_inputs", "gbcc_residual",
+    "gbcc_residual_ex", "gbcc_energy", "gbcc_solve", "gbcc_destroy", "gbcc_last_error",
 )
+# test hooks of include/gbcc_testing.h
+TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
+                   "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
+                   "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims")
 
 
 class Config(C.Structure):
@@ -79,6 +83,28 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_create.argtypes = [C.POINTER(vp), C.POINTER(Config)]
     lib.gbcc_set_inputs.restype = C.c_int
     lib.gbcc_set_inputs.argtypes = [vp, C.POINTER(Inputs)]
+    lib.gbcc_device_inputs.restype = C.c_int
+    lib.gbcc_device_inputs.argtypes = [vp, C.POINTER(Inputs)]
+    lib.gbcc_commit_inputs.restype = C.c_int
+    lib.gbcc_commit_inputs.argtypes = [vp]
+    lib.gbcc_testing_gemm.restype = C.c_int
+    lib.gbcc_testing_gemm.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp, C.c_int, C.c_int,
+                                      C.POINTER(C.c_float)]
+    lib.gbcc_testing_fp64_peak.restype = C.c_int
+    lib.gbcc_testing_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    ip = C.POINTER(C.c_int)
+    lib.gbcc_testing_profile_residual.restype = C.c_int
+    lib.gbcc_testing_profile_residual.argtypes = [vp, C.c_int, C.c_int, dp, dp, ip, ip, ip]
+    lib.gbcc_testing_last_launches.restype = C.c_int
+    lib.gbcc_testing_last_launches.argtypes = [vp, ip]
+    lib.gbcc_testing_record.restype = C.c_int
+    lib.gbcc_testing_record.argtypes = [vp, C.c_int]
+    lib.gbcc_testing_elapsed.restype = C.c_int
+    lib.gbcc_testing_elapsed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
+    lib.gbcc_testing_profile_gemm_ms.restype = C.c_int
+    lib.gbcc_testing_profile_gemm_ms.argtypes = [vp, C.c_int, dp]
+    lib.gbcc_testing_profile_dims.restype = C.c_int
+    lib.gbcc_testing_profile_dims.argtypes = [vp, C.c_int, C.POINTER(C.c_int64)]
     lib.gbcc_residual.restype = C.c_int
     lib.gbcc_residual.argtypes = [vp, vp, vp, vp, vp]
     lib.gbcc_residual_ex.restype = C.c_int

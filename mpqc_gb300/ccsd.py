@@ -128,6 +128,48 @@ class Solver:
         _check(self.lib, self.h, self.lib.gbcc_set_inputs(self.h, C.byref(inp)))
         self._keep = None
 
+    def device_inputs(self):
+        """Device pointers (ints) of the handle's own input arrays, to be filled
+        on the device before ``commit_inputs()`` (zero-copy set-up)."""
+        inp = L.Inputs()
+        _check(self.lib, self.h, self.lib.gbcc_device_inputs(self.h, C.byref(inp)))
+        return {n: getattr(inp, n) for n in ("eps_o", "eps_v") + INTEGRAL_NAMES}
+
+    def commit_inputs(self):
+        _check(self.lib, self.h, self.lib.gbcc_commit_inputs(self.h))
+
+    def profile_residual(self, precision=None, max_sites=256):
+        """Per-operation CUDA-event times of one residual on the device-resident
+        amplitudes: list of dicts (ms, flops, pairs, cls)."""
+        prec = self.cfg.precision if precision is None else {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}[precision]
+        ms = (C.c_double * max_sites)()
+        fl = (C.c_double * max_sites)()
+        pr = (C.c_int * max_sites)()
+        cl = (C.c_int * max_sites)()
+        n = C.c_int()
+        _check(self.lib, self.h, self.lib.gbcc_testing_profile_residual(self.h, prec, max_sites, ms, fl, pr, cl,
+                                                                        C.byref(n)))
+        gm = (C.c_double * max_sites)()
+        self.lib.gbcc_testing_profile_gemm_ms(self.h, max_sites, gm)
+        mnk = (C.c_int64 * (3 * max_sites))()
+        self.lib.gbcc_testing_profile_dims(self.h, max_sites, mnk)
+        return [dict(ms=ms[i], gemm_ms=gm[i], flops=fl[i], pairs=pr[i], cls=cl[i],
+                     M=mnk[3 * i], N=mnk[3 * i + 1], K=mnk[3 * i + 2])
+                for i in range(min(n.value, max_sites))]
+
+    def record(self, slot):
+        _check(self.lib, self.h, self.lib.gbcc_testing_record(self.h, slot))
+
+    def elapsed_ms(self, slot0, slot1):
+        ms = C.c_float()
+        _check(self.lib, self.h, self.lib.gbcc_testing_elapsed(self.h, slot0, slot1, C.byref(ms)))
+        return ms.value
+
+    def last_launches(self):
+        n = C.c_int()
+        self.lib.gbcc_testing_last_launches(self.h, C.byref(n))
+        return n.value
+
     def residual(self, t1, t2, r1=None, r2=None, precision=None):
         o, v = self.o, self.v
         if r1 is None:

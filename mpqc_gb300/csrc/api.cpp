@@ -5,6 +5,7 @@
 // ccsd.h:331-477): t = 0 start with r1 = f_ai and r2 = g_abij, then per
 // iteration error -> residual-augmented energy -> convergence test ->
 // Jacobi update + DIIS extrapolation -> tau -> R1 -> R2.
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <utility>
@@ -15,6 +16,7 @@
 #include <vector>
 
 #include "../../include/gbcc.h"
+#include "../../include/gbcc_testing.h"
 #include "ccsd_program.h"
 #include "engine.h"
 #include "kernels.h"
@@ -40,6 +42,10 @@ struct gbcc_handle {
   int* d_nskip = nullptr;
   int ndiis_alloc = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int last_launches = 0;  // kernels launched by the last residual
+  cudaEvent_t slots[8] = {};
+  std::vector<double> prof_gemm_ms;
+  std::vector<std::array<int64_t, 3>> prof_dims;
 };
 
 namespace {
@@ -117,6 +123,7 @@ void run_residual(gbcc_handle* h, int precision) {
   h->eng->begin(gbcc::Mode::kExec, precision);
   gbcc::residual_program(*h->eng, h->S);
   h->eng->end();
+  h->last_launches = 1 + h->eng->kernel_launches();
 }
 
 // E and error of the current t/tau/r (device-resident); returns {E, error}
@@ -154,6 +161,41 @@ void print_iter(int iter, double dE, double error, double E, double t) {
                 "total time/s");
   std::printf("%3i \t %10.5e \t %10.5e \t %15.12f \t %10.1f \n", iter, dE, error, E, t);
   std::fflush(stdout);
+}
+
+void validate_eps(const double* eps_o, const double* eps_v, int64_t o, int64_t v) {
+  std::vector<double> eo(o), ev(v);
+  GBCC_CK(cudaMemcpy(eo.data(), eps_o, o * sizeof(double), cudaMemcpyDefault));
+  GBCC_CK(cudaMemcpy(ev.data(), eps_v, v * sizeof(double), cudaMemcpyDefault));
+  for (int64_t i = 0; i < o; ++i)
+    for (int64_t a = 0; a < v; ++a)
+      if (!std::isfinite(eo[i]) || !std::isfinite(ev[a]) || eo[i] - ev[a] == 0.0)
+        throw Error(GBCC_ERR_INVALID_ARG,
+                    "orbital energies non-finite or degenerate across the gap (zero Jacobi denominator)");
+}
+
+// Derived constants, the residual plan for both precisions and (mixed
+// handles) the split copies of the constant operands.
+void commit_inputs(gbcc_handle* h) {
+  gbcc::CcsdTensors& S = h->S;
+  h->aux->reset_plans();
+  h->aux->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
+  gbcc::setup_program(*h->aux, S);
+  h->aux->end();
+  h->aux->finalize(false);
+  h->aux->begin(gbcc::Mode::kExec, GBCC_PREC_FP64);
+  gbcc::setup_program(*h->aux, S);
+  h->aux->end();
+  h->eng->reset_plans();
+  h->prepacked = false;
+  h->eng->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
+  gbcc::residual_program(*h->eng, S);
+  h->eng->end();
+  const bool mixed = h->cfg.precision == GBCC_PREC_MIXED;
+  h->eng->finalize(mixed);
+  h->prepacked = mixed;
+  sync_check(h);
+  h->inputs_set = true;
 }
 
 }  // namespace
@@ -252,15 +294,10 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
     for (const double* p : ptrs)
       if (!p) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_inputs: NULL input array");
     const int64_t o = h->cfg.o, v = h->cfg.v;
-    std::vector<double> eo(o), ev(v);
-    GBCC_CK(cudaMemcpy(eo.data(), in->eps_o, o * sizeof(double), cudaMemcpyDefault));
-    GBCC_CK(cudaMemcpy(ev.data(), in->eps_v, v * sizeof(double), cudaMemcpyDefault));
-    for (int64_t i = 0; i < o; ++i)
-      for (int64_t a = 0; a < v; ++a)
-        if (!std::isfinite(eo[i]) || !std::isfinite(ev[a]) || eo[i] - ev[a] == 0.0)
-          throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_inputs: orbital energies non-finite or degenerate across the gap");
+    validate_eps(in->eps_o, in->eps_v, o, v);
     if (!h->S.t1) h->S.create(*h->eng, o, v);
     gbcc::CcsdTensors& S = h->S;
+    h->inputs_set = false;
     copy_in(S.eps_o->d, in->eps_o, o, h->stream);
     copy_in(S.eps_v->d, in->eps_v, v, h->stream);
     copy_in(S.Fia->d, in->Fia, o * v, h->stream);
@@ -272,26 +309,39 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
     copy_in(S.Gijka->d, in->Gijka, o * o * o * v, h->stream);
     copy_in(S.Giabc->d, in->Giabc, o * v * v * v, h->stream);
     copy_in(S.Gabcd->d, in->Gabcd, v * v * v * v, h->stream);
-    // derived constants
-    h->aux->reset_plans();
-    h->aux->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
-    gbcc::setup_program(*h->aux, S);
-    h->aux->end();
-    h->aux->finalize(false);
-    h->aux->begin(gbcc::Mode::kExec, GBCC_PREC_FP64);
-    gbcc::setup_program(*h->aux, S);
-    h->aux->end();
-    // plan the residual for both precisions
-    h->eng->reset_plans();
-    h->prepacked = false;
-    h->eng->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
-    gbcc::residual_program(*h->eng, S);
-    h->eng->end();
-    const bool mixed = h->cfg.precision == GBCC_PREC_MIXED;
-    h->eng->finalize(mixed);
-    h->prepacked = mixed;
-    sync_check(h);
-    h->inputs_set = true;
+    commit_inputs(h);
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!out) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_device_inputs: NULL output");
+    if (!h->S.t1) h->S.create(*h->eng, h->cfg.o, h->cfg.v);
+    GBCC_CK(cudaStreamSynchronize(h->stream));  // zero-initialisation done
+    const gbcc::CcsdTensors& S = h->S;
+    out->eps_o = S.eps_o->d;
+    out->eps_v = S.eps_v->d;
+    out->Fia = S.Fia->d;
+    out->Fij = S.Fij->d;
+    out->Fab = S.Fab->d;
+    out->Gijab = S.Gijab->d;
+    out->Gijkl = S.Gijkl->d;
+    out->Giajb = S.Giajb->d;
+    out->Gijka = S.Gijka->d;
+    out->Giabc = S.Giabc->d;
+    out->Gabcd = S.Gabcd->d;
+    h->inputs_set = false;
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_commit_inputs(gbcc_handle* h) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!h->S.t1) throw Error(GBCC_ERR_STATE, "gbcc_commit_inputs: call gbcc_device_inputs first");
+    GBCC_CK(cudaStreamSynchronize(h->stream));
+    validate_eps(h->S.eps_o->d, h->S.eps_v->d, h->cfg.o, h->cfg.v);
+    commit_inputs(h);
     return GBCC_OK;
   });
 }
@@ -477,6 +527,8 @@ gbcc_status gbcc_destroy(gbcc_handle* h) {
   if (h->h_out) cudaFreeHost(h->h_out);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  for (cudaEvent_t e : h->slots)
+    if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return GBCC_OK;
@@ -485,6 +537,78 @@ gbcc_status gbcc_destroy(gbcc_handle* h) {
 const char* gbcc_last_error(const gbcc_handle* h) {
   if (!h) return g_create_error.c_str();
   return h->last_error.c_str();
+}
+
+
+int gbcc_testing_profile_residual(gbcc_handle* h, int precision, int max_sites, double* ms, double* flops,
+                                  int* pairs, int* cls, int* nsites) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "profile: inputs not set");
+    if (precision != GBCC_PREC_FP64 && precision != GBCC_PREC_MIXED)
+      throw Error(GBCC_ERR_INVALID_ARG, "profile: bad precision");
+    h->eng->set_profile(true);
+    try {
+      run_residual(h, precision);
+      sync_check(h);
+    } catch (...) {
+      h->eng->set_profile(false);
+      throw;
+    }
+    h->eng->set_profile(false);
+    const auto st = h->eng->site_stats(precision);
+    h->prof_gemm_ms.clear();
+    h->prof_dims.clear();
+    for (const auto& x : st) {
+      h->prof_gemm_ms.push_back(x.gemm_ms);
+      h->prof_dims.push_back({x.M, x.N, x.K});
+    }
+    if (nsites) *nsites = static_cast<int>(st.size());
+    for (int i = 0; i < max_sites && i < static_cast<int>(st.size()); ++i) {
+      if (ms) ms[i] = st[i].ms;
+      if (flops) flops[i] = st[i].flops;
+      if (pairs) pairs[i] = st[i].pairs;
+      if (cls) cls[i] = st[i].cls;
+    }
+    return GBCC_OK;
+  });
+}
+
+int gbcc_testing_profile_gemm_ms(gbcc_handle* h, int max_sites, double* ms) {
+  if (!h || !ms) return GBCC_ERR_INVALID_ARG;
+  for (int i = 0; i < max_sites && i < static_cast<int>(h->prof_gemm_ms.size()); ++i) ms[i] = h->prof_gemm_ms[i];
+  return GBCC_OK;
+}
+
+int gbcc_testing_profile_dims(gbcc_handle* h, int max_sites, int64_t* mnk) {
+  if (!h || !mnk) return GBCC_ERR_INVALID_ARG;
+  for (int i = 0; i < max_sites && i < static_cast<int>(h->prof_dims.size()); ++i)
+    for (int k = 0; k < 3; ++k) mnk[3 * i + k] = h->prof_dims[i][k];
+  return GBCC_OK;
+}
+
+int gbcc_testing_record(gbcc_handle* h, int slot) {
+  if (!h || slot < 0 || slot >= 8) return GBCC_ERR_INVALID_ARG;
+  return guarded(h, [&]() -> gbcc_status {
+    if (!h->slots[slot]) GBCC_CK(cudaEventCreate(&h->slots[slot]));
+    GBCC_CK(cudaEventRecord(h->slots[slot], h->stream));
+    return GBCC_OK;
+  });
+}
+
+int gbcc_testing_elapsed(gbcc_handle* h, int slot0, int slot1, float* ms) {
+  if (!h || !ms || slot0 < 0 || slot0 >= 8 || slot1 < 0 || slot1 >= 8) return GBCC_ERR_INVALID_ARG;
+  return guarded(h, [&]() -> gbcc_status {
+    if (!h->slots[slot0] || !h->slots[slot1]) throw Error(GBCC_ERR_STATE, "event slot not recorded");
+    GBCC_CK(cudaEventSynchronize(h->slots[slot1]));
+    GBCC_CK(cudaEventElapsedTime(ms, h->slots[slot0], h->slots[slot1]));
+    return GBCC_OK;
+  });
+}
+
+int gbcc_testing_last_launches(gbcc_handle* h, int* launches) {
+  if (!h || !launches) return GBCC_ERR_INVALID_ARG;
+  *launches = h->last_launches;
+  return GBCC_OK;
 }
 
 }  // extern "C"

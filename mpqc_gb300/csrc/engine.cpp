@@ -154,10 +154,67 @@ struct GemmPlan {
 
 struct Site {
   int kind = 0;  // 0 assign, 1 contract
-  std::string sig;
+  TermClass cls = kClassOther;
   GatherArgs gather{};
   GemmPlan plan[2];
+  cudaEvent_t e0 = nullptr, e1 = nullptr, eg = nullptr;  // profiling: start, end, GEMM start
+  bool has_gemm = false;
+  ~Site() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (eg) cudaEventDestroy(eg);
+  }
 };
+
+void Engine::prof_begin(Site& s) {
+  if (!profile_) return;
+  if (!s.e0) GBCC_CK(cudaEventCreate(&s.e0));
+  if (!s.e1) GBCC_CK(cudaEventCreate(&s.e1));
+  if (!s.eg) GBCC_CK(cudaEventCreate(&s.eg));
+  GBCC_CK(cudaEventRecord(s.e0, stream_));
+  s.has_gemm = false;
+}
+
+void Engine::prof_gemm(Site& s) {
+  if (!profile_) return;
+  GBCC_CK(cudaEventRecord(s.eg, stream_));
+  s.has_gemm = true;
+}
+
+void Engine::prof_end(Site& s) {
+  if (profile_) GBCC_CK(cudaEventRecord(s.e1, stream_));
+}
+
+std::vector<SiteStat> Engine::site_stats(int precision) {
+  std::vector<SiteStat> out;
+  GBCC_CK(cudaStreamSynchronize(stream_));
+  for (auto& sp : sites_) {
+    SiteStat st;
+    if (sp->e0 && sp->e1) {
+      float ms = 0.f;
+      GBCC_CK(cudaEventElapsedTime(&ms, sp->e0, sp->e1));
+      st.ms = ms;
+      if (sp->has_gemm) {
+        GBCC_CK(cudaEventElapsedTime(&ms, sp->eg, sp->e1));
+        st.gemm_ms = ms;
+      }
+    }
+    if (sp->kind == 1) {
+      const GemmPlan& p = sp->plan[precision == GBCC_PREC_MIXED ? 1 : 0];
+      st.flops = p.flops;
+      st.pairs = p.use_tc ? p.npairs : 0;
+      st.cls = sp->cls;
+      st.M = p.M;
+      st.N = p.N;
+      st.K = p.K;
+    } else {
+      st.M = sp->gather.R;
+      st.N = sp->gather.C;
+    }
+    out.push_back(st);
+  }
+  return out;
+}
 
 Engine::Engine() = default;
 
@@ -265,8 +322,10 @@ void Engine::assign(const Ix& c, double beta, const std::vector<Factor>& terms) 
   Site& s = site();
   if (mode_ == Mode::kExec) {
     if (s.kind != 0) throw Error(GBCC_ERR_STATE, "engine: site kind mismatch");
+    prof_begin(s);
     launch_gather(s.gather, stream_);
     ++n_launch_;
+    prof_end(s);
     return;
   }
   s.kind = 0;
@@ -339,6 +398,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     if (s.kind != 1) throw Error(GBCC_ERR_STATE, "engine: site kind mismatch");
     GemmPlan& p = s.plan[prec_ == GBCC_PREC_MIXED ? 1 : 0];
     flops_ += p.flops;
+    prof_begin(s);
     if (p.use_tc) {
       __nv_bfloat16* panel[2];
       for (int side = 0; side < 2; ++side) {
@@ -375,7 +435,9 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       t.alpha = p.alpha;
       t.beta = p.beta;
       t.bn = p.bn;
+      t.chunk = chunk_;
       t.err = err_;
+      prof_gemm(s);
       if (!launch_gemm_tc(t, stream_))
         throw Error(GBCC_ERR_CUDA, "tcgen05 GEMM launch rejected (tensor map or size)");
       ++n_tc_;
@@ -408,14 +470,17 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       f.cn = p.cn;
       f.alpha = p.alpha;
       f.beta = p.beta;
+      prof_gemm(s);
       launch_gemm_f64(f, stream_);
       ++n_launch_;
     }
+    prof_end(s);
     return;
   }
 
   // ---------------- PLAN ----------------
   s.kind = 1;
+  s.cls = cls;
   check_ix(c);
   if (A.empty() || B.empty() || A.size() > static_cast<size_t>(kMaxTerms) ||
       B.size() > static_cast<size_t>(kMaxTerms))

@@ -97,6 +97,15 @@ struct DevTable {
 
 struct Site;  // per call site plan
 
+struct SiteStat {
+  double ms = 0.0;     // event time of the site's launches (profiling on)
+  double gemm_ms = 0.0;  // of which the GEMM kernel
+  double flops = 0.0;  // 2 M N K of a contraction, 0 for an assignment
+  int pairs = 0;       // BF16 slice products on the tensor cores (0: FP64 / elementwise)
+  int cls = -1;        // TermClass of a contraction, -1 for an assignment
+  int64_t M = 0, N = 0, K = 0;  // GEMM shape (assignment: rows, columns, 0)
+};
+
 class Engine {
  public:
   Engine();
@@ -112,6 +121,10 @@ class Engine {
     slices_[2] = other;
   }
   void set_error_word(int* err) { err_ = err; }
+  void set_chunk(int k) { chunk_ = k; }
+  // Record CUDA events around every operation of EXEC passes.
+  void set_profile(bool on) { profile_ = on; }
+  std::vector<SiteStat> site_stats(int precision);
 
   // Persistent device tensor owned by the engine (allocated on first request).
   Tensor& tensor(const std::string& name, std::initializer_list<int64_t> dims, bool constant = false);
@@ -140,6 +153,9 @@ class Engine {
 
  private:
   Site& site();
+  void prof_begin(Site& s);
+  void prof_end(Site& s);
+  void prof_gemm(Site& s);
   DevTable upload(const std::vector<int64_t>& v);
   int slices_for(TermClass cls, double flops) const;
 
@@ -159,6 +175,8 @@ class Engine {
   __nv_bfloat16* wbfa_ = nullptr;
   __nv_bfloat16* wbfb_ = nullptr;
   int* err_ = nullptr;
+  int chunk_ = 4;  // k-blocks per TMEM accumulation in the tensor-core GEMM
+  bool profile_ = false;
   double flops_ = 0.0;
   size_t bytes_ = 0;
   int n_tc_ = 0;

@@ -4,19 +4,33 @@
 //
 // A FP64 operand x is stored as BF16 slices x = x_0 + x_1 + x_2 (each slice the
 // round-to-nearest BF16 of the remainder).  The product of two split operands
-// is the sum of the slice products A_p B_q over the chosen pairs (p + q below
-// the slice count drops the terms beneath the working precision, as in the
-// Ozaki splitting of Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59 (2012)).
-// All slice products accumulate into one FP32 TMEM accumulator; the epilogue
-// converts to FP64 and scatters through the output offset tables.
+// is the sum of the slice products A_p B_q over the pairs with p + q below the
+// slice count (the terms beneath the working precision are dropped, as in the
+// error-free splitting of Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59,
+// 95 (2012)).
 //
-// Pipeline (one 128 x BN output tile per CTA, 6 warps):
-//   warp 0     : TMA producer (one thread) -> STAGES-deep smem ring
-//   warp 1     : TMEM allocator + MMA issuer (one thread), tcgen05.mma kind::f16
-//   warps 2..5 : epilogue, tcgen05.ld 32x32b (warp w reads TMEM lanes 32*(w%4)...)
+// Accumulation.  The tensor core accumulates in FP32 and loses about one
+// FP32 ulp of the running sum per MMA instruction, so a long K loop in one
+// accumulator would lose accuracy in proportion to K.  Here every TMEM
+// accumulation covers only a chunk of `chunk` k-blocks (4 * chunk MMAs).  The
+// epilogue warps add each finished chunk to an FP32 register partial p and,
+// every `fold` chunks, fold p into a float-float (hi + lo) accumulator kept in
+// TMEM with Knuth's TwoSum; the error is that of one chunk plus `fold` FP32
+// additions, independent of K.  TMEM holds two accumulators, so the MMAs of
+// the next chunk run while the epilogue drains the previous one.
+//
+// Persistent kernel: one CTA per SM walks the 128 x BN output tiles
+// (N-tile index fastest, so CTAs running together share the A panel in L2).
+//   warp 0     : TMA producer (one thread), STAGES-deep smem ring
+//   warp 1     : TMEM allocator + MMA issuer (one thread), kind::f16
+//   warps 4..11: epilogue; warp w reads TMEM lanes 32*(w%4).. and the column
+//                half (w-4)/4 of the tile (warps 2 and 3 only pad the
+//                block to three warps per scheduler, which leaves 168
+//                registers per thread for the float-float accumulators)
 // Operand tiles are K-major with the 128-byte swizzle (TMA box 64 x rows).
 // Every mbarrier wait is bounded: on timeout the kernel records kDevTimeout in
-// *err, drains its own copies in flight, frees its TMEM and returns.
+// *err, drains its own copies in flight, waits for its MMAs, frees its TMEM
+// and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -31,7 +45,9 @@ namespace {
 
 constexpr int BM = kTcBM;   // 128
 constexpr int BK = kTcBK;   // 64 bf16 = 128 bytes = one swizzle row
-constexpr int kThreadsTc = 192;
+constexpr int kEpiWarps = 8;
+constexpr int kEpiWarp0 = 4;  // epilogue warps are 4..11 (warps 2,3 idle)
+constexpr int kThreadsTc = 32 * (kEpiWarp0 + kEpiWarps);
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -54,6 +70,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -67,7 +87,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase of `parity` to complete.  Gives up (false) after
-// kWaitNs, or early once another CTA has recorded an error.
+// kWaitNs, or early once any CTA has recorded an error.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const int* err) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
@@ -77,6 +97,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const 
       if (globaltimer() - t0 > kWaitNs) return false;
       if (*reinterpret_cast<const volatile int*>(err) != kDevOk) return false;
     }
+  }
+}
+
+// Bounded wait that ignores the error word (teardown paths).
+__device__ __forceinline__ void mbar_wait_teardown(uint64_t* bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer();
+  while (!mbar_try_wait(bar, parity) && globaltimer() - t0 < kWaitNs) {
   }
 }
 
@@ -120,8 +147,8 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
 }
 
 // Shared-memory matrix descriptor: K-major tile, 128-byte swizzle, 8-row
-// groups 1024 bytes apart (SBO), version 1, base offset 0 (tiles are
-// 1024-byte aligned).
+// groups 1024 bytes apart (SBO), descriptor version 1, base offset 0 (tiles
+// are 1024-byte aligned).
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   uint64_t d = 0;
   d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
@@ -166,17 +193,53 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
         "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Knuth's TwoSum: hi + lo += x with the rounding error of hi + x kept in lo.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float v = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, v)), __fsub_rn(x, v));
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+
+constexpr int kStgLd = 17;  // padded row of the per-warp output staging tile (doubles)
+constexpr uint32_t kStgBytes = kEpiWarps * 32 * kStgLd * 8;
 
 template <int BN>
 struct TcCfg {
-  static constexpr int kStages = (BN >= 256) ? 4 : (BN >= 128 ? 6 : 8);
+  static constexpr int kStages = (BN >= 128) ? 5 : (BN >= 64 ? 7 : 8);
   static constexpr uint32_t kABytes = BM * BK * 2;
   static constexpr uint32_t kBBytes = BN * BK * 2;
   static constexpr uint32_t kStageBytes = kABytes + kBBytes;
-  static constexpr uint32_t kSmem = 1024 + kStages * kStageBytes + 256;
-  static constexpr uint32_t kTmemCols = BN < 32 ? 32 : BN;
+  static constexpr uint32_t kSmem = 1024 + kStages * kStageBytes + kStgBytes + 256;
+  // two accumulators [0, 2 BN) + the float-float low words [2 BN, 3 BN)
+  static constexpr uint32_t kTmemCols = BN >= 128 ? 512 : (BN >= 64 ? 256 : 128);
+  static constexpr int kCols = BN / 2;                               // columns per epilogue thread
 };
 
 template <int BN>
@@ -185,29 +248,38 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
                    const GemmTcArgs g) {
   using Cfg = TcCfg<BN>;
   constexpr int S = Cfg::kStages;
+  constexpr int COLS = Cfg::kCols;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
   uint8_t* sA = smem;
   uint8_t* sB = smem + S * Cfg::kABytes;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + S * Cfg::kBBytes);
+  double* stg_all = reinterpret_cast<double*>(sB + S * Cfg::kBBytes);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + S * Cfg::kBBytes + kStgBytes);
   uint64_t* empty = full + S;
-  uint64_t* accb = empty + S;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+  uint64_t* acc_full = empty + S;   // [2]
+  uint64_t* acc_empty = acc_full + 2;  // [2]
+  uint64_t* done = acc_empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
 
   const int warp = threadIdx.x / 32;
   const int lane = threadIdx.x % 32;
-  const int64_t n0 = static_cast<int64_t>(blockIdx.x) * BN;
-  const int64_t m0 = static_cast<int64_t>(blockIdx.y) * BM;
+  const int ntn = static_cast<int>(g.Npad / BN);
+  const int ntiles = ntn * static_cast<int>(g.Mpad / BM);
   const int kblocks = static_cast<int>(g.Kpad / BK);
   const int n_iter = kblocks * g.npairs;
+  const int chunk = g.chunk > 0 ? g.chunk : 4;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accb, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], kEpiWarps);
+    }
+    mbar_init(done, 1);
     fence_barrier_init();
   }
   if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
@@ -220,93 +292,177 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     if (lane == 0) {
       prefetch_tmap(&tmA);
       prefetch_tmap(&tmB);
-      int issued = 0;
-      for (int it = 0; it < n_iter; ++it) {
-        const int s = it % S;
-        const uint32_t ph = (it / S) & 1;
-        if (!mbar_wait(&empty[s], ph ^ 1, g.err)) {
-          record_error(g.err, kDevTimeout);
-          break;
-        }
-        const int kb = it / g.npairs;
-        const int pr = it % g.npairs;
-        mbar_expect_tx(&full[s], Cfg::kStageBytes);
-        tma_load_3d(&tmA, &full[s], sA + s * Cfg::kABytes, kb * BK, static_cast<int>(m0), g.pa[pr]);
-        tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBBytes, kb * BK, static_cast<int>(n0), g.pb[pr]);
-        ++issued;
-      }
-      // drain: every copy this thread issued has landed before the CTA exits
-      const int first = issued > S ? issued - S : 0;
-      for (int it = first; it < issued; ++it) {
-        if (!mbar_wait(&full[it % S], (it / S) & 1, g.err)) {
-          // last resort: bounded again, ignoring the error early-exit
-          const uint64_t t0 = globaltimer();
-          while (!mbar_try_wait(&full[it % S], (it / S) & 1) && globaltimer() - t0 < kWaitNs) {
+      uint32_t gi = 0;  // stage-use counter across tiles
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int n0 = (tile % ntn) * BN;
+        const int m0 = (tile / ntn) * BM;
+        for (int it = 0; it < n_iter; ++it, ++gi) {
+          const int s = gi % S;
+          if (!mbar_wait(&empty[s], ((gi / S) & 1) ^ 1, g.err)) {
+            record_error(g.err, kDevTimeout);
+            ok = false;
+            break;
           }
+          const int kb = it / g.npairs;
+          const int pr = it - kb * g.npairs;
+          mbar_expect_tx(&full[s], Cfg::kStageBytes);
+          tma_load_3d(&tmA, &full[s], sA + s * Cfg::kABytes, kb * BK, m0, g.pa[pr]);
+          tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBBytes, kb * BK, n0, g.pb[pr]);
         }
       }
+      // every copy issued here has landed before the CTA can exit
+      const uint32_t first = gi > static_cast<uint32_t>(S) ? gi - S : 0;
+      for (uint32_t u = first; u < gi; ++u) mbar_wait_teardown(&full[u % S], (u / S) & 1);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(BM, BN);
+      uint32_t gi = 0;  // stage-use counter
+      uint32_t c = 0;   // chunk counter
       bool ok = true;
-      for (int it = 0; it < n_iter; ++it) {
-        const int s = it % S;
-        const uint32_t ph = (it / S) & 1;
-        if (!mbar_wait(&full[s], ph, g.err)) {
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (int it = 0; it < n_iter; ++it, ++gi) {
+          const int pos = it % chunk;
+          const uint32_t b = c & 1;
+          if (pos == 0 && !mbar_wait(&acc_empty[b], ((c >> 1) & 1) ^ 1, g.err)) {
+            record_error(g.err, kDevTimeout);
+            ok = false;
+            break;
+          }
+          const int s = gi % S;
+          if (!mbar_wait(&full[s], (gi / S) & 1, g.err)) {
+            record_error(g.err, kDevTimeout);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(sA + s * Cfg::kABytes);
+          const uint32_t b0 = smem_u32(sB + s * Cfg::kBBytes);
+          const uint32_t d = tmem + b * BN;
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            mma_bf16(d, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc,
+                     (pos > 0 || k > 0) ? 1u : 0u);
+          }
+          mma_commit(&empty[s]);
+          if (pos == chunk - 1 || it == n_iter - 1) {
+            mma_commit(&acc_full[b]);
+            ++c;
+          }
+        }
+      }
+      // TMEM is freed below only after every MMA issued here has completed
+      mma_commit(done);
+      mbar_wait_teardown(done, 0);
+    }
+  } else if (warp >= kEpiWarp0) {
+    // epilogue warps
+    const int q = warp & 3;
+    const int h = (warp - kEpiWarp0) >> 2;
+    const int row = q * 32 + lane;
+    const int col0 = h * COLS;
+    const uint32_t lane_addr = static_cast<uint32_t>(q * 32) << 16;
+    const int nchunks = (n_iter + chunk - 1) / chunk;
+    // TMEM columns [2 BN, 3 BN): float-float high words, [3 BN, 4 BN): low words
+    const uint32_t hi_base = tmem + lane_addr + 2 * BN + col0;
+    const uint32_t lo_base = tmem + lane_addr + 3 * BN + col0;
+    const int fold = g.fold > 0 ? g.fold : 16;
+    uint32_t c = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const int64_t n0 = static_cast<int64_t>(tile % ntn) * BN;
+      const int64_t m0 = static_cast<int64_t>(tile / ntn) * BM;
+      // p: plain FP32 sum of the chunks since the last fold
+      float p[COLS];
+#pragma unroll
+      for (int j = 0; j < COLS; ++j) p[j] = 0.f;
+      bool first_fold = true;
+      for (int cc = 0; cc < nchunks; ++cc, ++c) {
+        const uint32_t b = c & 1;
+        if (!mbar_wait(&acc_full[b], (c >> 1) & 1, g.err)) {
           record_error(g.err, kDevTimeout);
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t a0 = smem_u32(sA + s * Cfg::kABytes);
-        const uint32_t b0 = smem_u32(sB + s * Cfg::kBBytes);
+        const uint32_t base = tmem + lane_addr + b * BN + col0;
 #pragma unroll
-        for (int k = 0; k < BK / 16; ++k) {
-          mma_bf16(tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc,
-                   (it > 0 || k > 0) ? 1u : 0u);
+        for (int j0 = 0; j0 < COLS; j0 += 16) {
+          uint32_t r[16];
+          tmem_ld16(base + j0, r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 16; ++j) p[j0 + j] = __fadd_rn(p[j0 + j], __uint_as_float(r[j]));
         }
-        mma_commit(&empty[s]);
-      }
-      (void)ok;
-      mma_commit(accb);  // tracks completion of every MMA issued above
-      // TMEM is freed below only after every issued MMA has completed
-      const uint64_t t0 = globaltimer();
-      while (!mbar_try_wait(accb, 0) && globaltimer() - t0 < kWaitNs) {
-      }
-    }
-  } else {
-    // epilogue warps 2..5
-    const int q = warp & 3;
-    const int row = q * 32 + lane;
-    const int64_t m = m0 + row;
-    const bool ready = mbar_wait(accb, 0, g.err);
-    tc_fence_after();
-    const bool write = ready && (*reinterpret_cast<const volatile int*>(g.err) == kDevOk);
-    if (!ready) record_error(g.err, kDevTimeout);
-    if (ready) {
-      const int64_t om = (m < g.M) ? g.cm[m] : 0;
-#pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t r[32];
-        tmem_ld32(tmem + (static_cast<uint32_t>(q * 32) << 16) + static_cast<uint32_t>(c0), r);
-        if (write && m < g.M) {
+        // the accumulator buffer is free again
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[b]);
+        if ((cc + 1) % fold == 0 || cc == nchunks - 1) {
+          // fold p into the float-float (hi, lo) pair kept in TMEM
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int64_t n = n0 + c0 + j;
-            if (n < g.N) {
-              double* p = g.C + om + g.cn[n];
-              const double val = g.alpha * static_cast<double>(__uint_as_float(r[j]));
+          for (int j0 = 0; j0 < COLS; j0 += 16) {
+            uint32_t h[16], l[16];
+            if (!first_fold) {
+              tmem_ld16(hi_base + j0, h);
+              tmem_ld16(lo_base + j0, l);
+              tmem_ld_wait();
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              float hv = first_fold ? 0.f : __uint_as_float(h[j]);
+              float lv = first_fold ? 0.f : __uint_as_float(l[j]);
+              two_sum_acc(hv, lv, p[j0 + j]);
+              h[j] = __float_as_uint(hv);
+              l[j] = __float_as_uint(lv);
+              p[j0 + j] = 0.f;
+            }
+            tmem_st16(hi_base + j0, h);
+            tmem_st16(lo_base + j0, l);
+          }
+          tmem_st_wait();
+          first_fold = false;
+        }
+      }
+      if (!ok) break;
+      if (*reinterpret_cast<const volatile int*>(g.err) != kDevOk) continue;
+      // stage 32 rows x 16 columns through shared memory, then write with the
+      // lanes along N (coalesced when C is contiguous in N)
+      double* stg = stg_all + (warp - kEpiWarp0) * 32 * kStgLd;
+      const int cj = lane & 15;
+#pragma unroll
+      for (int j0 = 0; j0 < COLS; j0 += 16) {
+        uint32_t h[16], l[16];
+        tmem_ld16(hi_base + j0, h);
+        tmem_ld16(lo_base + j0, l);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          stg[lane * kStgLd + j] =
+              static_cast<double>(__uint_as_float(h[j])) + static_cast<double>(__uint_as_float(l[j]));
+        __syncwarp();
+        const int64_t n = n0 + col0 + j0 + cj;
+        if (cj < COLS && n < g.N) {
+          const int64_t on = g.cn[n];
+#pragma unroll 4
+          for (int rr = lane >> 4; rr < 32; rr += 2) {
+            const int64_t m = m0 + q * 32 + rr;
+            if (m < g.M) {
+              double* p = g.C + g.cm[m] + on;
+              const double val = g.alpha * stg[rr * kStgLd + cj];
               *p = (g.beta == 0.0) ? val : fma(g.beta, *p, val);
             }
           }
         }
+        __syncwarp();
       }
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
+    __syncwarp();
     tc_fence_after();
     tmem_dealloc(tmem, Cfg::kTmemCols);
   }
@@ -341,6 +497,17 @@ bool make_map(CUtensorMap* map, const void* base, int64_t slices, int64_t rows, 
   return r == CUDA_SUCCESS;
 }
 
+int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
 template <int BN>
 bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
   using Cfg = TcCfg<BN>;
@@ -354,7 +521,8 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
       return false;
     attr_set = true;
   }
-  dim3 grid(static_cast<unsigned>(g.Npad / BN), static_cast<unsigned>(g.Mpad / BM));
+  const int64_t ntiles = (g.Npad / BN) * (g.Mpad / BM);
+  const int grid = static_cast<int>(ntiles < num_sms() ? ntiles : num_sms());
   gemm_tc_kernel<BN><<<grid, kThreadsTc, Cfg::kSmem, st>>>(ma, mb, g);
   return true;
 }
@@ -364,20 +532,20 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
 int gemm_tc_pick_bn(int64_t N) {
   if (N <= 32) return 32;
   if (N <= 64) return 64;
-  if (N <= 128) return 128;
-  return 256;
+  return 128;
 }
 
 bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return true;
-  if (g.Mpad % BM || g.Kpad % BK || g.Npad % g.bn || g.npairs < 1 || g.npairs > kMaxPairs) return false;
+  if (g.Mpad % BM || g.Kpad % BK || g.Kpad < BK || g.Npad % g.bn || g.npairs < 1 ||
+      g.npairs > kMaxPairs)
+    return false;
   if (g.Mpad > (1LL << 31) - 1 || g.Npad > (1LL << 31) - 1 || g.Kpad > (1LL << 31) - 1) return false;
-  if (g.Mpad / BM > 65535) return false;
+  if ((g.Npad / g.bn) * (g.Mpad / BM) > (1LL << 31) - 1) return false;
   switch (g.bn) {
     case 32: return launch_bn<32>(g, st);
     case 64: return launch_bn<64>(g, st);
     case 128: return launch_bn<128>(g, st);
-    case 256: return launch_bn<256>(g, st);
     default: return false;
   }
 }

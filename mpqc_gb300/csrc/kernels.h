@@ -71,7 +71,8 @@ void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st);
 // Split-BF16 tcgen05 GEMM (sm_103a):
 //   C[cm[m] + cn[n]] = beta*C + alpha * sum_{(p,q) in pairs} A_p[m][:] . B_q[n][:]
 // A_p: slice p of A, [Mpad][Kpad] bf16 K-contiguous; B_q likewise [Npad][Kpad].
-// Accumulation in FP32 (TMEM), recombination to FP64 in the epilogue.
+// Each TMEM (FP32) accumulation covers `chunk` k-blocks; chunks are summed in
+// float-float registers and converted to FP64 in the epilogue.
 // ---------------------------------------------------------------------------
 constexpr int kMaxPairs = 9;
 struct GemmTcArgs {
@@ -85,7 +86,9 @@ struct GemmTcArgs {
   const int64_t* cm;
   const int64_t* cn;
   double alpha, beta;
-  int bn;                // N tile (32, 64, 128 or 256)
+  int bn;                // N tile (32, 64 or 128)
+  int chunk;             // k-blocks per TMEM accumulation (0: default 4)
+  int fold;              // chunks summed in FP32 before a float-float fold (0: default 16)
   int* err;              // device error word
 };
 // Returns false if the tensor maps could not be encoded (bad alignment / size).

@@ -1,6 +1,7 @@
 // Test hooks (include/gbcc_testing.h): single-kernel GEMM runs and an FP64
 // throughput probe.  Not used by the solver itself.
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "../../include/gbcc.h"
@@ -94,6 +95,8 @@ extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* 
         for (int b = 0; b < slices; ++b)
           if (a + b < slices) { t.pa[t.npairs] = a; t.pb[t.npairs] = b; ++t.npairs; }
       t.C = dC; t.cm = cm; t.cn = cn; t.alpha = 1.0; t.beta = 0.0; t.bn = bn; t.err = err;
+      if (const char* e = std::getenv("GBCC_TC_CHUNK")) t.chunk = std::atoi(e);
+      if (const char* e = std::getenv("GBCC_TC_FOLD")) t.fold = std::atoi(e);
       if (!launch_gemm_tc(t, st)) throw Error(GBCC_ERR_CUDA, "tcgen05 launch rejected");
       GBCC_CK(cudaEventRecord(e0, st));
       for (int r = 0; r < repeat; ++r) launch_gemm_tc(t, st);

@@ -86,7 +86,7 @@ def test_solve_fp64_golden():
 
 @pytest.mark.parametrize("o,v,naux,seed", [(3, 10, 14, 21), (5, 19, 30, 22), (6, 30, 40, 23)])
 def test_solve_fp64_random(o, v, naux, seed):
-    inp = synth.make_inputs(o, v, naux, seed=seed)
+    inp = synth.make_inputs(o, v, naux, seed=seed, b_scale=0.03)
     ref = R.solve_ccsd(oracle_ints(inp), inp.eps_o, inp.eps_v, target_precision=1e-10, max_iter=60)
     with _solver(inp, target_precision=1e-10, max_iter=60) as s:
         e, t1, t2, rep = s.solve()
@@ -96,7 +96,7 @@ def test_solve_fp64_random(o, v, naux, seed):
 
 
 def test_solve_mixed_with_fp64_refinement():
-    inp = synth.make_inputs(8, 40, 40, seed=31)
+    inp = synth.make_inputs(8, 40, 40, seed=31, b_scale=0.02)
     ref = R.solve_ccsd(oracle_ints(inp), inp.eps_o, inp.eps_v, target_precision=1e-10, max_iter=60)
     with _solver(inp, precision="mixed", target_precision=1e-10, max_iter=60, refine_iters=2) as s:
         e, t1, t2, rep = s.solve()
