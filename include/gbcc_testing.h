@@ -21,6 +21,11 @@ extern "C" {
 int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
                       int slices, int repeat, float* ms);
 
+/* As gbcc_testing_gemm with the K dimension split over `ksplit` groups of
+ * CTAs (partial tiles reduced in a fixed order by a second kernel). */
+int gbcc_testing_gemm_split(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+                            int slices, int ksplit, int repeat, float* ms);
+
 /* Peak probe: FP64 FMA throughput of this GPU in GFLOP/s (a register-resident
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);

@@ -148,6 +148,8 @@ struct GemmPlan {
   double alpha = 1.0, beta = 0.0;
   double* C = nullptr;
   int slices = 0, npairs = 0, bn = 0;
+  int ksplit = 1;         // K split over CTAs (deterministic two-pass reduction)
+  int64_t k_per_split = 0;  // FP64: K elements per split; tensor cores: k-blocks per split
   int pa[kMaxPairs] = {}, pb[kMaxPairs] = {};
   double flops = 0.0;
 };
@@ -225,6 +227,7 @@ Engine::~Engine() {
   dev_free(w64b_);
   dev_free(wbfa_);
   dev_free(wbfb_);
+  dev_free(wpart_);
 }
 
 Tensor& Engine::tensor(const std::string& name, std::initializer_list<int64_t> dims, bool constant) {
@@ -262,7 +265,9 @@ void Engine::reset_plans() {
   for (void* p : owned_) dev_free(p);
   owned_.clear();
   planned_ = false;
-  ws64_a_ = ws64_b_ = wsbf_a_ = wsbf_b_ = 0;
+  ws64_a_ = ws64_b_ = wsbf_a_ = wsbf_b_ = wspart_ = 0;
+  dev_free(wpart_);
+  wpart_ = nullptr;
   dev_free(w64a_);
   dev_free(w64b_);
   dev_free(wbfa_);
@@ -437,11 +442,19 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       t.bn = p.bn;
       t.chunk = chunk_;
       t.err = err_;
+      t.ksplit = p.ksplit;
+      t.kb_per_split = static_cast<int>(p.k_per_split);
+      t.partial = wpart_;
       prof_gemm(s);
       if (!launch_gemm_tc(t, stream_))
         throw Error(GBCC_ERR_CUDA, "tcgen05 GEMM launch rejected (tensor map or size)");
       ++n_tc_;
       ++n_launch_;
+      if (p.ksplit > 1) {
+        launch_splitk_reduce(p.M, p.N, p.ksplit, wpart_, t.Mpad, t.Npad, p.C, p.cm, p.cn, p.alpha, p.beta,
+                             stream_);
+        ++n_launch_;
+      }
     } else {
       const double* panel[2];
       for (int side = 0; side < 2; ++side) {
@@ -470,9 +483,12 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       f.cn = p.cn;
       f.alpha = p.alpha;
       f.beta = p.beta;
+      f.ksplit = p.ksplit;
+      f.k_per_split = p.k_per_split;
+      f.partial = wpart_;
       prof_gemm(s);
       launch_gemm_f64(f, stream_);
-      ++n_launch_;
+      n_launch_ += p.ksplit > 1 ? 2 : 1;
     }
     prof_end(s);
     return;
@@ -604,6 +620,22 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       p.cm = upload(offsets(p.P[0].ext, e, cx)).d;
       p.cn = upload(offsets(p.P[1].ext, e, cx)).d;
     }
+    if (!p.use_tc) {
+      // few 64 x 64 output tiles and a long K: split K over blocks
+      const int64_t tiles = ((p.M + 63) / 64) * ((p.N + 63) / 64);
+      const int64_t sms = num_sms();
+      if (tiles < 2 * sms && K >= 4096) {
+        int64_t ks = std::min<int64_t>((2 * sms + tiles - 1) / tiles, K / 1024);
+        if (ks > 1) {
+          int64_t kps = (K + ks - 1) / ks;
+          kps = (kps + 15) / 16 * 16;
+          ks = (K + kps - 1) / kps;
+          p.ksplit = static_cast<int>(ks);
+          p.k_per_split = kps;
+          wspart_ = std::max(wspart_, static_cast<size_t>(ks * p.M * p.N));
+        }
+      }
+    }
     if (p.use_tc) {
       p.slices = slices;
       p.bn = gemm_tc_pick_bn(p.N);
@@ -637,6 +669,20 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
           wsbf_b_ = std::max(wsbf_b_, need);
         }
       }
+      // fewer output tiles than SMs and a long K: split K over CTAs
+      const int64_t tiles = (p.P[0].rows_pad / kTcBM) * (p.P[1].rows_pad / p.bn);
+      const int64_t kblocks = Kpad / kTcBK;
+      const int64_t sms = num_sms();
+      if (tiles < sms && kblocks >= 16) {
+        int64_t ks = std::min<int64_t>((sms + tiles - 1) / tiles, kblocks / 8);
+        if (ks > 1) {
+          const int64_t kbps = (kblocks + ks - 1) / ks;
+          ks = (kblocks + kbps - 1) / kbps;
+          p.ksplit = static_cast<int>(ks);
+          p.k_per_split = kbps;
+          wspart_ = std::max(wspart_, static_cast<size_t>(ks * p.P[0].rows_pad * p.P[1].rows_pad));
+        }
+      }
     }
   }
 }
@@ -651,7 +697,9 @@ void Engine::finalize(bool prepack_mixed) {
   w64b_ = static_cast<double*>(dev_alloc(ws64_b_ * sizeof(double)));
   wbfa_ = static_cast<__nv_bfloat16*>(dev_alloc(wsbf_a_ * sizeof(__nv_bfloat16)));
   wbfb_ = static_cast<__nv_bfloat16*>(dev_alloc(wsbf_b_ * sizeof(__nv_bfloat16)));
-  bytes_ += (ws64_a_ + ws64_b_) * sizeof(double) + (wsbf_a_ + wsbf_b_) * sizeof(__nv_bfloat16);
+  dev_free(wpart_);
+  wpart_ = static_cast<double*>(dev_alloc(wspart_ * sizeof(double)));
+  bytes_ += (ws64_a_ + ws64_b_ + wspart_) * sizeof(double) + (wsbf_a_ + wsbf_b_) * sizeof(__nv_bfloat16);
   if (prepack_mixed) {
     for (auto& sp : sites_) {
       if (sp->kind != 1) continue;

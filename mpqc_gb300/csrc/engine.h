@@ -169,7 +169,8 @@ class Engine {
   std::unordered_map<std::string, std::unique_ptr<Tensor>> tensors_;
   std::vector<void*> owned_;  // tables and constant-pack buffers
   // shared workspaces (sized during PLAN)
-  size_t ws64_a_ = 0, ws64_b_ = 0, wsbf_a_ = 0, wsbf_b_ = 0;
+  size_t ws64_a_ = 0, ws64_b_ = 0, wsbf_a_ = 0, wsbf_b_ = 0, wspart_ = 0;
+  double* wpart_ = nullptr;  // K-split partial tiles
   double* w64a_ = nullptr;
   double* w64b_ = nullptr;
   __nv_bfloat16* wbfa_ = nullptr;

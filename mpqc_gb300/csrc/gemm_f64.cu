@@ -19,6 +19,9 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmF64Args g) {
   const int tx = tid % 16, ty = tid / 16;
   const int64_t m0 = static_cast<int64_t>(blockIdx.y) * BM;
   const int64_t n0 = static_cast<int64_t>(blockIdx.x) * BN;
+  // K range of this block (blockIdx.z selects the K split)
+  const int64_t kbeg = g.ksplit > 1 ? static_cast<int64_t>(blockIdx.z) * g.k_per_split : 0;
+  const int64_t kend = g.ksplit > 1 ? min(g.K, kbeg + g.k_per_split) : g.K;
 
   double ra[4], rb[4];
   auto load_regs = [&](int64_t k0) {
@@ -27,8 +30,8 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmF64Args g) {
       const int idx = tid + NT * l;
       const int row = idx / BK, kk = idx % BK;
       const int64_t m = m0 + row, n = n0 + row, k = k0 + kk;
-      ra[l] = (m < g.M && k < g.K) ? g.A[m * g.lda + k] : 0.0;
-      rb[l] = (n < g.N && k < g.K) ? g.B[n * g.ldb + k] : 0.0;
+      ra[l] = (m < g.M && k < kend) ? g.A[m * g.lda + k] : 0.0;
+      rb[l] = (n < g.N && k < kend) ? g.B[n * g.ldb + k] : 0.0;
     }
   };
   auto store_smem = [&](int buf) {
@@ -47,13 +50,13 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmF64Args g) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
 
-  const int64_t nk = (g.K + BK - 1) / BK;
-  load_regs(0);
+  const int64_t nk = (kend - kbeg + BK - 1) / BK;
+  load_regs(kbeg);
   store_smem(0);
   __syncthreads();
   for (int64_t kt = 0; kt < nk; ++kt) {
     const int buf = kt & 1;
-    if (kt + 1 < nk) load_regs((kt + 1) * BK);
+    if (kt + 1 < nk) load_regs(kbeg + (kt + 1) * BK);
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       double a[4], b[4];
@@ -70,6 +73,20 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmF64Args g) {
     __syncthreads();
   }
 
+  if (g.ksplit > 1) {
+    double* P = g.partial + static_cast<int64_t>(blockIdx.z) * g.M * g.N;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t m = m0 + ty + 16 * i;
+      if (m >= g.M) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t n = n0 + tx + 16 * j;
+        if (n < g.N) P[m * g.N + n] = acc[i][j];
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int64_t m = m0 + ty + 16 * i;
@@ -90,8 +107,11 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmF64Args g) {
 
 void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return;
-  dim3 grid(static_cast<unsigned>((g.N + BN - 1) / BN), static_cast<unsigned>((g.M + BM - 1) / BM));
+  dim3 grid(static_cast<unsigned>((g.N + BN - 1) / BN), static_cast<unsigned>((g.M + BM - 1) / BM),
+            static_cast<unsigned>(g.ksplit > 1 ? g.ksplit : 1));
   gemm_f64_kernel<<<grid, NT, 0, st>>>(g);
+  if (g.ksplit > 1)
+    launch_splitk_reduce(g.M, g.N, g.ksplit, g.partial, g.M, g.N, g.C, g.cm, g.cn, g.alpha, g.beta, st);
 }
 
 }  // namespace gbcc

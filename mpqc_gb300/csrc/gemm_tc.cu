@@ -265,10 +265,23 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   const int warp = threadIdx.x / 32;
   const int lane = threadIdx.x % 32;
   const int ntn = static_cast<int>(g.Npad / BN);
-  const int ntiles = ntn * static_cast<int>(g.Mpad / BM);
+  const int ntiles_mn = ntn * static_cast<int>(g.Mpad / BM);
+  const int ksplit = g.ksplit > 1 ? g.ksplit : 1;
+  const int ntiles = ntiles_mn * ksplit;
   const int kblocks = static_cast<int>(g.Kpad / BK);
-  const int n_iter = kblocks * g.npairs;
+  const int kb_per_split = ksplit > 1 ? g.kb_per_split : kblocks;
   const int chunk = g.chunk > 0 ? g.chunk : 4;
+  // tile -> (K split, M block, N block); N fastest so CTAs running together
+  // share the A panel in L2
+  auto decode = [&](int tile, int& m0, int& n0, int& kb0, int& n_iter, int& split) {
+    split = tile / ntiles_mn;
+    const int mn = tile - split * ntiles_mn;
+    n0 = (mn % ntn) * BN;
+    m0 = (mn / ntn) * BM;
+    kb0 = split * kb_per_split;
+    const int nkb = kblocks - kb0 < kb_per_split ? kblocks - kb0 : kb_per_split;
+    n_iter = nkb * g.npairs;
+  };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -295,8 +308,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       uint32_t gi = 0;  // stage-use counter across tiles
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int n0 = (tile % ntn) * BN;
-        const int m0 = (tile / ntn) * BM;
+        int m0, n0, kb0, n_iter, split;
+        decode(tile, m0, n0, kb0, n_iter, split);
         for (int it = 0; it < n_iter; ++it, ++gi) {
           const int s = gi % S;
           if (!mbar_wait(&empty[s], ((gi / S) & 1) ^ 1, g.err)) {
@@ -304,8 +317,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
             ok = false;
             break;
           }
-          const int kb = it / g.npairs;
-          const int pr = it - kb * g.npairs;
+          const int kb = kb0 + it / g.npairs;
+          const int pr = it % g.npairs;
           mbar_expect_tx(&full[s], Cfg::kStageBytes);
           tma_load_3d(&tmA, &full[s], sA + s * Cfg::kABytes, kb * BK, m0, g.pa[pr]);
           tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBBytes, kb * BK, n0, g.pb[pr]);
@@ -322,6 +335,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       uint32_t c = 0;   // chunk counter
       bool ok = true;
       for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        int m0, n0, kb0, n_iter, split;
+        decode(tile, m0, n0, kb0, n_iter, split);
         for (int it = 0; it < n_iter; ++it, ++gi) {
           const int pos = it % chunk;
           const uint32_t b = c & 1;
@@ -363,7 +378,6 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     const int row = q * 32 + lane;
     const int col0 = h * COLS;
     const uint32_t lane_addr = static_cast<uint32_t>(q * 32) << 16;
-    const int nchunks = (n_iter + chunk - 1) / chunk;
     // TMEM columns [2 BN, 3 BN): float-float high words, [3 BN, 4 BN): low words
     const uint32_t hi_base = tmem + lane_addr + 2 * BN + col0;
     const uint32_t lo_base = tmem + lane_addr + 3 * BN + col0;
@@ -371,8 +385,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     uint32_t c = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const int64_t n0 = static_cast<int64_t>(tile % ntn) * BN;
-      const int64_t m0 = static_cast<int64_t>(tile / ntn) * BM;
+      int m0i, n0i, kb0, n_iter, split;
+      decode(tile, m0i, n0i, kb0, n_iter, split);
+      const int64_t n0 = n0i, m0 = m0i;
+      const int nchunks = (n_iter + chunk - 1) / chunk;
       // p: plain FP32 sum of the chunks since the last fold
       float p[COLS];
 #pragma unroll
@@ -443,16 +459,33 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
               static_cast<double>(__uint_as_float(h[j])) + static_cast<double>(__uint_as_float(l[j]));
         __syncwarp();
         const int64_t n = n0 + col0 + j0 + cj;
-        if (cj < COLS && n < g.N) {
-          const int64_t on = g.cn[n];
-#pragma unroll 4
+        if (ksplit > 1) {
+          // K-split partial tile: plain stores, reduced by splitk_reduce
+          double* P = g.partial + static_cast<int64_t>(split) * g.Mpad * g.Npad + n;
+#pragma unroll
           for (int rr = lane >> 4; rr < 32; rr += 2) {
             const int64_t m = m0 + q * 32 + rr;
-            if (m < g.M) {
-              double* p = g.C + g.cm[m] + on;
-              const double val = g.alpha * stg[rr * kStgLd + cj];
-              *p = (g.beta == 0.0) ? val : fma(g.beta, *p, val);
-            }
+            P[m * g.Npad] = stg[rr * kStgLd + cj];
+          }
+        } else if (cj < COLS && n < g.N) {
+          const int64_t on = g.cn[n];
+          // 16 rows per lane: issue every read of C before the stores
+          double cv[16];
+          int64_t off[16];
+#pragma unroll
+          for (int r = 0; r < 16; ++r) {
+            const int64_t m = m0 + q * 32 + (lane >> 4) + 2 * r;
+            off[r] = m < g.M ? g.cm[m] + on : -1;
+          }
+          if (g.beta != 0.0) {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) cv[r] = off[r] >= 0 ? g.C[off[r]] : 0.0;
+          }
+#pragma unroll
+          for (int r = 0; r < 16; ++r) {
+            if (off[r] < 0) continue;
+            const double val = g.alpha * stg[((lane >> 4) + 2 * r) * kStgLd + cj];
+            g.C[off[r]] = (g.beta == 0.0) ? val : fma(g.beta, cv[r], val);
           }
         }
         __syncwarp();
@@ -497,16 +530,6 @@ bool make_map(CUtensorMap* map, const void* base, int64_t slices, int64_t rows, 
   return r == CUDA_SUCCESS;
 }
 
-int num_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  return sms;
-}
 
 template <int BN>
 bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
@@ -521,7 +544,7 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
       return false;
     attr_set = true;
   }
-  const int64_t ntiles = (g.Npad / BN) * (g.Mpad / BM);
+  const int64_t ntiles = (g.Npad / BN) * (g.Mpad / BM) * (g.ksplit > 1 ? g.ksplit : 1);
   const int grid = static_cast<int>(ntiles < num_sms() ? ntiles : num_sms());
   gemm_tc_kernel<BN><<<grid, kThreadsTc, Cfg::kSmem, st>>>(ma, mb, g);
   return true;
@@ -541,7 +564,10 @@ bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
       g.npairs > kMaxPairs)
     return false;
   if (g.Mpad > (1LL << 31) - 1 || g.Npad > (1LL << 31) - 1 || g.Kpad > (1LL << 31) - 1) return false;
-  if ((g.Npad / g.bn) * (g.Mpad / BM) > (1LL << 31) - 1) return false;
+  if ((g.Npad / g.bn) * (g.Mpad / BM) * (g.ksplit > 1 ? g.ksplit : 1) > (1LL << 31) - 1) return false;
+  if (g.ksplit > 1 && (!g.partial || g.kb_per_split < 1 ||
+                       static_cast<int64_t>(g.ksplit - 1) * g.kb_per_split >= g.Kpad / BK))
+    return false;
   switch (g.bn) {
     case 32: return launch_bn<32>(g, st);
     case 64: return launch_bn<64>(g, st);

@@ -317,7 +317,45 @@ __global__ void __launch_bounds__(kThreads) extrapolate_t2_tau_kernel(ExtrapArgs
   }
 }
 
+__global__ void __launch_bounds__(kThreads) splitk_reduce_kernel(int64_t M, int64_t N, int ksplit,
+                                                                 const double* __restrict__ partial,
+                                                                 int64_t rows, int64_t ldp, double* C,
+                                                                 const int64_t* __restrict__ cm,
+                                                                 const int64_t* __restrict__ cn,
+                                                                 double alpha, double beta) {
+  const int64_t total = M * N;
+  const int64_t split_stride = rows * ldp;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t m = e / N, n = e - m * N;
+    const double* p = partial + m * ldp + n;
+    double acc = 0.0;
+    for (int s = 0; s < ksplit; ++s) acc += p[s * split_stride];
+    double* c = C + cm[m] + cn[n];
+    *c = (beta == 0.0) ? alpha * acc : fma(beta, *c, alpha * acc);
+  }
+}
+
 }  // namespace
+
+int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+void launch_splitk_reduce(int64_t M, int64_t N, int ksplit, const double* partial, int64_t rows,
+                          int64_t ldp, double* C, const int64_t* cm, const int64_t* cn, double alpha,
+                          double beta, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  splitk_reduce_kernel<<<grid_for(M * N, kThreads), kThreads, 0, st>>>(M, N, ksplit, partial, rows, ldp, C,
+                                                                      cm, cn, alpha, beta);
+}
 
 // ---------------------------------------------------------------------------
 // launchers

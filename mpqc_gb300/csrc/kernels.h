@@ -56,6 +56,9 @@ void launch_gather(const GatherArgs& args, cudaStream_t st);
 // ---------------------------------------------------------------------------
 struct GemmF64Args {
   int64_t M, N, K;
+  int ksplit;            // >1: blockIdx.z covers K range z; partials [ksplit][M][N]
+  int64_t k_per_split;
+  double* partial;
   const double* A;
   int64_t lda;
   const double* B;
@@ -89,8 +92,19 @@ struct GemmTcArgs {
   int bn;                // N tile (32, 64 or 128)
   int chunk;             // k-blocks per TMEM accumulation (0: default 4)
   int fold;              // chunks summed in FP32 before a float-float fold (0: default 16)
+  int ksplit;            // >1: K split over CTAs; partial tiles go to `partial`
+  int kb_per_split;      // k-blocks per split (every split gets at least one)
+  double* partial;       // [ksplit][Mpad][Npad] FP64 partial tiles (ksplit > 1)
   int* err;              // device error word
 };
+// Deterministic K-split reduction: C[cm[m] + cn[n]] = beta*C + alpha * sum_s
+// partial[s][m][n] (splits summed in order), partial rows of length ldp and
+// split stride rows*ldp.
+void launch_splitk_reduce(int64_t M, int64_t N, int ksplit, const double* partial, int64_t rows,
+                          int64_t ldp, double* C, const int64_t* cm, const int64_t* cn, double alpha,
+                          double beta, cudaStream_t st);
+int num_sms();
+
 // Returns false if the tensor maps could not be encoded (bad alignment / size).
 bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st);
 int gemm_tc_pick_bn(int64_t N);

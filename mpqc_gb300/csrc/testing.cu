@@ -29,8 +29,13 @@ __global__ void fp64_fma_probe(double* out, int iters) {
 
 extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
                                  double* Cout, int slices, int repeat, float* ms) {
+  return gbcc_testing_gemm_split(M, N, K, A, B, Cout, slices, 1, repeat, ms);
+}
+
+extern "C" int gbcc_testing_gemm_split(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
+                                       double* Cout, int slices, int ksplit, int repeat, float* ms) {
   using namespace gbcc;
-  if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1)
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1 || ksplit < 1)
     return GBCC_ERR_INVALID_ARG;
   std::vector<void*> owned;
   auto alloc = [&](size_t bytes) {
@@ -66,6 +71,12 @@ extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* 
       g.M = M; g.N = N; g.K = K;
       g.A = dA; g.lda = K; g.B = dB; g.ldb = K;
       g.C = dC; g.cm = cm; g.cn = cn; g.alpha = 1.0; g.beta = 0.0;
+      if (ksplit > 1) {
+        g.ksplit = ksplit;
+        g.k_per_split = (K + ksplit - 1) / ksplit;
+        g.ksplit = static_cast<int>((K + g.k_per_split - 1) / g.k_per_split);
+        g.partial = static_cast<double*>(alloc(g.ksplit * M * N * sizeof(double)));
+      }
       launch_gemm_f64(g, st);
       GBCC_CK(cudaEventRecord(e0, st));
       for (int r = 0; r < repeat; ++r) launch_gemm_f64(g, st);
@@ -97,9 +108,20 @@ extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* 
       t.C = dC; t.cm = cm; t.cn = cn; t.alpha = 1.0; t.beta = 0.0; t.bn = bn; t.err = err;
       if (const char* e = std::getenv("GBCC_TC_CHUNK")) t.chunk = std::atoi(e);
       if (const char* e = std::getenv("GBCC_TC_FOLD")) t.fold = std::atoi(e);
-      if (!launch_gemm_tc(t, st)) throw Error(GBCC_ERR_CUDA, "tcgen05 launch rejected");
+      if (ksplit > 1) {
+        const int64_t kblocks = Kpad / kTcBK;
+        t.kb_per_split = static_cast<int>((kblocks + ksplit - 1) / ksplit);
+        t.ksplit = static_cast<int>((kblocks + t.kb_per_split - 1) / t.kb_per_split);
+        t.partial = static_cast<double*>(alloc(t.ksplit * Mpad * Npad * sizeof(double)));
+      }
+      auto run = [&]() {
+        if (!launch_gemm_tc(t, st)) throw Error(GBCC_ERR_CUDA, "tcgen05 launch rejected");
+        if (t.ksplit > 1)
+          launch_splitk_reduce(M, N, t.ksplit, t.partial, Mpad, Npad, dC, cm, cn, 1.0, 0.0, st);
+      };
+      run();
       GBCC_CK(cudaEventRecord(e0, st));
-      for (int r = 0; r < repeat; ++r) launch_gemm_tc(t, st);
+      for (int r = 0; r < repeat; ++r) run();
       GBCC_CK(cudaEventRecord(e1, st));
     }
     GBCC_CK(cudaEventSynchronize(e1));

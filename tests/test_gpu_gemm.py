@@ -61,3 +61,24 @@ def test_fp64_probe_runs(tlib):
     g = C.c_double()
     assert tlib.gbcc_testing_fp64_peak(C.byref(g)) == 0
     assert g.value > 10.0
+
+
+@pytest.mark.parametrize("slices", [0, 3])
+@pytest.mark.parametrize("M,N,K,ksplit", [(32, 32, 20000, 37), (320, 32, 9000, 9), (5, 7, 4096, 64),
+                                          (200, 130, 3000, 3)])
+def test_gemm_split_k(tlib, M, N, K, ksplit, slices):
+    rng = np.random.default_rng(K + ksplit)
+    A = rng.normal(size=(M, K))
+    B = rng.normal(size=(N, K))
+    ref = A @ B.T
+    out = np.empty((M, N))
+    ms = C.c_float()
+    st = tlib.gbcc_testing_gemm_split(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, slices, ksplit, 1,
+                                      C.byref(ms))
+    assert st == 0
+    tol = TOL[slices] + (8 * 2.0**-24 * np.sqrt(K) if slices else 0.0)
+    assert np.max(np.abs(out - ref)) <= tol * np.max(np.abs(ref))
+    out2 = np.empty((M, N))
+    tlib.gbcc_testing_gemm_split(M, N, K, A.ctypes.data, B.ctypes.data, out2.ctypes.data, slices, ksplit, 1,
+                                 C.byref(ms))
+    assert np.array_equal(out, out2)
