@@ -24,7 +24,8 @@ PREC_MIXED = 1
 EXPORTS = (
     "gbcc_abi_version", "gbcc_status_string", "gbcc_config_default", "gbcc_create",
     "gbcc_set_inputs", "gbcc_device_inputs", "gbcc_commit_inputs", "gbcc_residual",
-    "gbcc_residual_ex", "gbcc_energy", "gbcc_solve", "gbcc_destroy", "gbcc_last_error",
+    "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
+    "gbcc_last_error",
 )
 # test hooks of include/gbcc_testing.h
 TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_split", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
@@ -114,6 +115,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_residual_ex.argtypes = [vp, i32, vp, vp, vp, vp]
     lib.gbcc_energy.restype = C.c_int
     lib.gbcc_energy.argtypes = [vp, vp, vp, vp, vp, dp, dp]
+    lib.gbcc_energy_noalloc.restype = C.c_int
+    lib.gbcc_energy_noalloc.argtypes = [C.c_int64, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.gbcc_solve.restype = C.c_int
     lib.gbcc_solve.argtypes = [vp, vp, vp, dp, C.POINTER(Report)]
     lib.gbcc_destroy.restype = C.c_int

@@ -200,6 +200,9 @@ void commit_inputs(gbcc_handle* h) {
 
 }  // namespace
 
+// Thread-local message read by gbcc_last_error(NULL) (handle-free entry points).
+void gbcc_set_thread_error(const std::string& msg) { g_create_error = msg; }
+
 extern "C" {
 
 int gbcc_abi_version(void) { return GBCC_ABI_VERSION; }

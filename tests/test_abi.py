@@ -105,3 +105,11 @@ def test_array_checks():
     with pytest.raises(InputError):
         _ptr(np.zeros((3, 4))[:, ::2])
     assert _ptr(np.zeros(3)) != 0
+
+
+def test_energy_noalloc_rejects_sizes_beyond_its_scratch(lib):
+    from mpqc_gb300._lib import GBCC_ERR_INVALID_ARG
+    st = lib.gbcc_energy_noalloc(4, 513, None, None, None, None, None, None, None, None)
+    assert st == GBCC_ERR_INVALID_ARG
+    assert "v <= 512" in lib.gbcc_last_error(None).decode()
+    assert lib.gbcc_energy_noalloc(0, 8, None, None, None, None, None, None, None, None) == GBCC_ERR_INVALID_ARG
