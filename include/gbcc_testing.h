@@ -21,10 +21,14 @@ extern "C" {
 int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
                       int slices, int repeat, float* ms);
 
-/* As gbcc_testing_gemm with the K dimension split over `ksplit` groups of
- * CTAs (partial tiles reduced in a fixed order by a second kernel). */
-int gbcc_testing_gemm_split(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
-                            int slices, int ksplit, int repeat, float* ms);
+/* As gbcc_testing_gemm with the tensor-core kernel's knobs exposed: the K
+ * dimension split over `ksplit` groups of CTAs (partial tiles reduced in a
+ * fixed order by a second kernel), the N tile `bn` (0: automatic; 256 sums
+ * chunks in FP32 registers), CTA pairs (`cta2`, tcgen05 cta_group::2), the
+ * k-blocks per TMEM accumulation (`chunk`, 0: default) and the chunks per
+ * float-float fold (`fold`, 0: default).  slices == 0 runs the FP64 kernel. */
+int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+                         int slices, int ksplit, int bn, int cta2, int chunk, int fold, int repeat, float* ms);
 
 /* Peak probe: FP64 FMA throughput of this GPU in GFLOP/s (a register-resident
  * DFMA loop over all SMs). */

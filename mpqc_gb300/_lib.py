@@ -28,7 +28,7 @@ EXPORTS = (
     "gbcc_last_error",
 )
 # test hooks of include/gbcc_testing.h
-TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_split", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
+TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims")
 
@@ -91,9 +91,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_testing_gemm.restype = C.c_int
     lib.gbcc_testing_gemm.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp, C.c_int, C.c_int,
                                       C.POINTER(C.c_float)]
-    lib.gbcc_testing_gemm_split.restype = C.c_int
-    lib.gbcc_testing_gemm_split.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp, C.c_int, C.c_int,
-                                            C.c_int, C.POINTER(C.c_float)]
+    lib.gbcc_testing_gemm_ex.restype = C.c_int
+    lib.gbcc_testing_gemm_ex.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp] + [C.c_int] * 7 + \
+        [C.POINTER(C.c_float)]
     lib.gbcc_testing_fp64_peak.restype = C.c_int
     lib.gbcc_testing_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     ip = C.POINTER(C.c_int)

@@ -149,6 +149,7 @@ struct GemmPlan {
   double* C = nullptr;
   int slices = 0, npairs = 0, bn = 0;
   int ksplit = 1;         // K split over CTAs (deterministic two-pass reduction)
+  bool m_major = false;   // C unit-stride along M
   int64_t k_per_split = 0;  // FP64: K elements per split; tensor cores: k-blocks per split
   int pa[kMaxPairs] = {}, pb[kMaxPairs] = {};
   double flops = 0.0;
@@ -445,6 +446,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       t.ksplit = p.ksplit;
       t.kb_per_split = static_cast<int>(p.k_per_split);
       t.partial = wpart_;
+      t.m_major = p.m_major ? 1 : 0;
       prof_gemm(s);
       if (!launch_gemm_tc(t, stream_))
         throw Error(GBCC_ERR_CUDA, "tcgen05 GEMM launch rejected (tensor map or size)");
@@ -617,8 +619,13 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     p.alpha = alpha * coef_direct;
     {
       Ix cx = c;
-      p.cm = upload(offsets(p.P[0].ext, e, cx)).d;
-      p.cn = upload(offsets(p.P[1].ext, e, cx)).d;
+      const std::vector<int64_t> hm = offsets(p.P[0].ext, e, cx), hn = offsets(p.P[1].ext, e, cx);
+      // epilogue lane direction: along M when C is unit-stride in M but not in N
+      const bool m_unit = hm.size() > 1 && hm[1] - hm[0] == 1;
+      const bool n_unit = hn.size() > 1 && hn[1] - hn[0] == 1;
+      p.m_major = m_unit && !n_unit;
+      p.cm = upload(hm).d;
+      p.cn = upload(hn).d;
     }
     if (!p.use_tc) {
       // few 64 x 64 output tiles and a long K: split K over blocks
@@ -638,7 +645,8 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     }
     if (p.use_tc) {
       p.slices = slices;
-      p.bn = gemm_tc_pick_bn(p.N);
+      // the ladder and ring contractions take the faster 256-wide tiles
+      p.bn = gemm_tc_pick_bn(p.N, cls == kClassLadder || cls == kClassRing);
       p.npairs = 0;
       for (int a = 0; a < slices; ++a)
         for (int b = 0; b < slices; ++b)

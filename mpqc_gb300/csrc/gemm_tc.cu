@@ -19,6 +19,11 @@
 // additions, independent of K.  TMEM holds two accumulators, so the MMAs of
 // the next chunk run while the epilogue drains the previous one.
 //
+// With BN = 256 the two accumulators fill TMEM, so the chunks of a tile sum in
+// FP32 registers only (error that of one chunk plus one FP32 addition per
+// chunk); BN = 256 is about 1.5x faster, since an N = 128 MMA needs more shared-
+// memory operand traffic per FLOP than the tensor core can be fed.
+//
 // Persistent kernel: one CTA per SM walks the 128 x BN output tiles
 // (N-tile index fastest, so CTAs running together share the A panel in L2).
 //   warp 0     : TMA producer (one thread), STAGES-deep smem ring
@@ -45,9 +50,6 @@ namespace {
 
 constexpr int BM = kTcBM;   // 128
 constexpr int BK = kTcBK;   // 64 bf16 = 128 bytes = one swizzle row
-constexpr int kEpiWarps = 8;
-constexpr int kEpiWarp0 = 4;  // epilogue warps are 4..11 (warps 2,3 idle)
-constexpr int kThreadsTc = 32 * (kEpiWarp0 + kEpiWarps);
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -216,6 +218,71 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16
 
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
+// ---- CTA-pair (cta_group::2) helpers
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// shared::cluster address of the same shared variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_to_rank(const void* p, uint32_t rank) {
+  uint32_t out;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(smem_u32(p)), "r"(rank));
+  return out;
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc2(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc2(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// TMA load into this CTA's shared memory, completion counted on the mbarrier
+// at cluster address `bar` (the pair leader's barrier).
+__device__ __forceinline__ void tma_load_3d_pair(const CUtensorMap* map, uint32_t bar, void* dst, int c0, int c1,
+                                                 int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrive on the mbarrier at the same shared offset in every CTA of `mask`
+// once the MMAs issued so far have completed.
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // Knuth's TwoSum: hi + lo += x with the rounding error of hi + x kept in lo.
@@ -228,25 +295,44 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }
 
 constexpr int kStgLd = 17;  // padded row of the per-warp output staging tile (doubles)
-constexpr uint32_t kStgBytes = kEpiWarps * 32 * kStgLd * 8;
 
-template <int BN>
+template <int BN, bool CTA2>
 struct TcCfg {
-  static constexpr int kStages = (BN >= 128) ? 5 : (BN >= 64 ? 7 : 8);
+  // a CTA pair splits B along N: each CTA stages BN/2 rows of it
+  static constexpr int kBRows = CTA2 ? BN / 2 : BN;
   static constexpr uint32_t kABytes = BM * BK * 2;
-  static constexpr uint32_t kBBytes = BN * BK * 2;
+  static constexpr uint32_t kBBytes = kBRows * BK * 2;
+  static constexpr int kStages = (kABytes + kBBytes) >= 49152 ? 3
+                                 : (kABytes + kBBytes) >= 32768 ? 5
+                                 : ((kABytes + kBBytes) >= 24576 ? 7 : 8);
   static constexpr uint32_t kStageBytes = kABytes + kBBytes;
+  // warps 0 (TMA), 1 (MMA), 2-3 idle, 4-11 epilogue: three warps per
+  // scheduler leave 168 registers a thread
+  static constexpr int kEpiWarps = 8;
+  static constexpr int kEpiWarp0 = 4;
+  static constexpr int kThreads = 32 * (kEpiWarp0 + kEpiWarps);
+  static constexpr uint32_t kStgBytes = kEpiWarps * 32 * kStgLd * 8;
   static constexpr uint32_t kSmem = 1024 + kStages * kStageBytes + kStgBytes + 256;
-  // two accumulators [0, 2 BN) + the float-float low words [2 BN, 3 BN)
+  // BN <= 128: two accumulators [0, 2 BN) + float-float words [2 BN, 4 BN);
+  // BN = 256: the two accumulators fill TMEM and the chunks of a tile sum in
+  // FP32 registers (no float-float fold)
+  static constexpr bool kFold = BN <= 128;
   static constexpr uint32_t kTmemCols = BN >= 128 ? 512 : (BN >= 64 ? 256 : 128);
-  static constexpr int kCols = BN / 2;                               // columns per epilogue thread
+  static constexpr int kCols = BN / (kEpiWarps / 4);                // columns per epilogue thread
 };
 
-template <int BN>
-__global__ void __launch_bounds__(kThreadsTc, 1)
+template <int BN, bool CTA2>
+__global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const GemmTcArgs g) {
-  using Cfg = TcCfg<BN>;
+  using Cfg = TcCfg<BN, CTA2>;
+  // CTA pair: rank 0 (leader) issues the MMAs for the 256-row tile; rank r
+  // owns rows [128 r, 128 r + 128) of it and B rows [r BN/2, (r+1) BN/2)
+  constexpr int BMP = CTA2 ? 2 * BM : BM;
+  const uint32_t rank = CTA2 ? cluster_rank() : 0;
+  const bool leader = rank == 0;
+  const int unit = CTA2 ? static_cast<int>(blockIdx.x / 2) : static_cast<int>(blockIdx.x);
+  const int nunits = CTA2 ? static_cast<int>(gridDim.x / 2) : static_cast<int>(gridDim.x);
   constexpr int S = Cfg::kStages;
   constexpr int COLS = Cfg::kCols;
   extern __shared__ uint8_t smem_raw[];
@@ -255,7 +341,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   uint8_t* sA = smem;
   uint8_t* sB = smem + S * Cfg::kABytes;
   double* stg_all = reinterpret_cast<double*>(sB + S * Cfg::kBBytes);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + S * Cfg::kBBytes + kStgBytes);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + S * Cfg::kBBytes + Cfg::kStgBytes);
+  constexpr int kEpiWarps = Cfg::kEpiWarps;
+  constexpr int kEpiWarp0 = Cfg::kEpiWarp0;
   uint64_t* empty = full + S;
   uint64_t* acc_full = empty + S;   // [2]
   uint64_t* acc_empty = acc_full + 2;  // [2]
@@ -265,7 +353,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   const int warp = threadIdx.x / 32;
   const int lane = threadIdx.x % 32;
   const int ntn = static_cast<int>(g.Npad / BN);
-  const int ntiles_mn = ntn * static_cast<int>(g.Mpad / BM);
+  const int ntiles_mn = ntn * static_cast<int>(g.Mpad / BMP);
   const int ksplit = g.ksplit > 1 ? g.ksplit : 1;
   const int ntiles = ntiles_mn * ksplit;
   const int kblocks = static_cast<int>(g.Kpad / BK);
@@ -277,7 +365,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     split = tile / ntiles_mn;
     const int mn = tile - split * ntiles_mn;
     n0 = (mn % ntn) * BN;
-    m0 = (mn / ntn) * BM;
+    m0 = (mn / ntn) * BMP + static_cast<int>(rank) * BM;
     kb0 = split * kb_per_split;
     const int nkb = kblocks - kb0 < kb_per_split ? kblocks - kb0 : kb_per_split;
     n_iter = nkb * g.npairs;
@@ -290,14 +378,18 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], kEpiWarps);
+      mbar_init(&acc_empty[b], kEpiWarps * (CTA2 ? 2 : 1));
     }
     mbar_init(done, 1);
     fence_barrier_init();
   }
-  if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
+  if (warp == 1) {
+    if constexpr (CTA2) tmem_alloc2(tmem_slot, Cfg::kTmemCols);
+    else tmem_alloc(tmem_slot, Cfg::kTmemCols);
+  }
   tc_fence_before();
   __syncthreads();
+  if constexpr (CTA2) cluster_sync();  // both CTAs' barriers exist before any remote arrive
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
@@ -307,68 +399,105 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       prefetch_tmap(&tmB);
       uint32_t gi = 0;  // stage-use counter across tiles
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      // stage-ring position kept incrementally (no divisions in the loop)
+      int s = 0;
+      uint32_t ph = 0;
+      const uint32_t full0 = CTA2 ? map_to_rank(&full[0], 0) : 0;
+      for (int tile = unit; tile < ntiles && ok; tile += nunits) {
         int m0, n0, kb0, n_iter, split;
         decode(tile, m0, n0, kb0, n_iter, split);
+        const int nb0 = n0 + static_cast<int>(rank) * Cfg::kBRows;
+        int kb = kb0, pr = 0;
         for (int it = 0; it < n_iter; ++it, ++gi) {
-          const int s = gi % S;
-          if (!mbar_wait(&empty[s], ((gi / S) & 1) ^ 1, g.err)) {
+          if (!mbar_wait(&empty[s], ph ^ 1, g.err)) {
             record_error(g.err, kDevTimeout);
             ok = false;
             break;
           }
-          const int kb = kb0 + it / g.npairs;
-          const int pr = it % g.npairs;
-          mbar_expect_tx(&full[s], Cfg::kStageBytes);
-          tma_load_3d(&tmA, &full[s], sA + s * Cfg::kABytes, kb * BK, m0, g.pa[pr]);
-          tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBBytes, kb * BK, n0, g.pb[pr]);
+          if constexpr (CTA2) {
+            // the leader's full barrier counts the bytes of both CTAs
+            const uint32_t bar = full0 + static_cast<uint32_t>(s) * 8u;
+            if (leader) mbar_expect_tx(&full[s], 2 * Cfg::kStageBytes);
+            tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kABytes, kb * BK, m0, g.pa[pr]);
+            tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBBytes, kb * BK, nb0, g.pb[pr]);
+          } else {
+            mbar_expect_tx(&full[s], Cfg::kStageBytes);
+            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kABytes, kb * BK, m0, g.pa[pr]);
+            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBBytes, kb * BK, nb0, g.pb[pr]);
+          }
+          if (++pr == g.npairs) {
+            pr = 0;
+            ++kb;
+          }
+          if (++s == S) {
+            s = 0;
+            ph ^= 1;
+          }
         }
       }
-      // every copy issued here has landed before the CTA can exit
+      // every copy issued here has landed before the CTA can exit: the
+      // leader's full barriers count them; the partner sees them consumed
       const uint32_t first = gi > static_cast<uint32_t>(S) ? gi - S : 0;
-      for (uint32_t u = first; u < gi; ++u) mbar_wait_teardown(&full[u % S], (u / S) & 1);
+      for (uint32_t u = first; u < gi; ++u) {
+        if (leader) mbar_wait_teardown(&full[u % S], (u / S) & 1);
+        else mbar_wait_teardown(&empty[u % S], (u / S) & 1);
+      }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16(BM, BN);
+    if (lane == 0 && leader) {
+      constexpr uint32_t idesc = idesc_bf16(BMP, BN);
       uint32_t gi = 0;  // stage-use counter
       uint32_t c = 0;   // chunk counter
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      // shared-memory descriptors: built once, advanced by adding encoded
+      // byte offsets (address >> 4) for the stage and the 16-element K step
+      const uint64_t adesc0 = sdesc_sw128(smem_u32(sA));
+      const uint64_t bdesc0 = sdesc_sw128(smem_u32(sB));
+      int s = 0;
+      uint32_t ph = 0;
+      for (int tile = unit; tile < ntiles && ok; tile += nunits) {
         int m0, n0, kb0, n_iter, split;
         decode(tile, m0, n0, kb0, n_iter, split);
+        int pos = 0;
         for (int it = 0; it < n_iter; ++it, ++gi) {
-          const int pos = it % chunk;
           const uint32_t b = c & 1;
           if (pos == 0 && !mbar_wait(&acc_empty[b], ((c >> 1) & 1) ^ 1, g.err)) {
             record_error(g.err, kDevTimeout);
             ok = false;
             break;
           }
-          const int s = gi % S;
-          if (!mbar_wait(&full[s], (gi / S) & 1, g.err)) {
+          if (!mbar_wait(&full[s], ph, g.err)) {
             record_error(g.err, kDevTimeout);
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t a0 = smem_u32(sA + s * Cfg::kABytes);
-          const uint32_t b0 = smem_u32(sB + s * Cfg::kBBytes);
+          const uint64_t ad = adesc0 + ((static_cast<uint64_t>(s) * Cfg::kABytes) >> 4);
+          const uint64_t bd = bdesc0 + ((static_cast<uint64_t>(s) * Cfg::kBBytes) >> 4);
           const uint32_t d = tmem + b * BN;
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k) {
-            mma_bf16(d, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc,
-                     (pos > 0 || k > 0) ? 1u : 0u);
+            const uint32_t acc = (pos > 0 || k > 0) ? 1u : 0u;
+            if constexpr (CTA2) mma_bf16_pair(d, ad + 2 * k, bd + 2 * k, idesc, acc);
+            else mma_bf16(d, ad + 2 * k, bd + 2 * k, idesc, acc);
           }
-          mma_commit(&empty[s]);
-          if (pos == chunk - 1 || it == n_iter - 1) {
-            mma_commit(&acc_full[b]);
+          if constexpr (CTA2) mma_commit_pair(&empty[s], 0x3);
+          else mma_commit(&empty[s]);
+          if (++s == S) {
+            s = 0;
+            ph ^= 1;
+          }
+          if (++pos == chunk || it == n_iter - 1) {
+            if constexpr (CTA2) mma_commit_pair(&acc_full[b], 0x3);
+            else mma_commit(&acc_full[b]);
             ++c;
+            pos = 0;
           }
         }
       }
       // TMEM is freed below only after every MMA issued here has completed
-      mma_commit(done);
+      if constexpr (CTA2) mma_commit_pair(done, 0x1);
+      else mma_commit(done);
       mbar_wait_teardown(done, 0);
     }
   } else if (warp >= kEpiWarp0) {
@@ -384,7 +513,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
     const int fold = g.fold > 0 ? g.fold : 16;
     uint32_t c = 0;
     bool ok = true;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const uint32_t acc_empty_leader0 = CTA2 ? map_to_rank(&acc_empty[0], 0) : 0;
+    const uint32_t acc_empty_leader1 = CTA2 ? map_to_rank(&acc_empty[1], 0) : 0;
+    for (int tile = unit; tile < ntiles && ok; tile += nunits) {
       int m0i, n0i, kb0, n_iter, split;
       decode(tile, m0i, n0i, kb0, n_iter, split);
       const int64_t n0 = n0i, m0 = m0i;
@@ -414,8 +545,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
         // the accumulator buffer is free again
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&acc_empty[b]);
-        if ((cc + 1) % fold == 0 || cc == nchunks - 1) {
+        if (lane == 0) {
+          if constexpr (CTA2) mbar_arrive_cluster(b ? acc_empty_leader1 : acc_empty_leader0);
+          else mbar_arrive(&acc_empty[b]);
+        }
+        if (Cfg::kFold && ((cc + 1) % fold == 0 || cc == nchunks - 1)) {
           // fold p into the float-float (hi, lo) pair kept in TMEM
 #pragma unroll
           for (int j0 = 0; j0 < COLS; j0 += 16) {
@@ -443,6 +577,47 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
       }
       if (!ok) break;
       if (*reinterpret_cast<const volatile int*>(g.err) != kDevOk) continue;
+      if (ksplit == 1 && g.m_major) {
+        // C contiguous in M: every lane owns one row, so the lanes of a warp
+        // write 32 consecutive rows of one column
+        const int64_t m = m0 + row;
+#pragma unroll
+        for (int j0 = 0; j0 < COLS; j0 += 16) {
+          uint32_t h[16], l[16];
+          if constexpr (Cfg::kFold) {
+            tmem_ld16(hi_base + j0, h);
+            tmem_ld16(lo_base + j0, l);
+            tmem_ld_wait();
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              h[j] = __float_as_uint(p[j0 + j]);
+              l[j] = 0u;
+            }
+          }
+          if (m < g.M) {
+            const int64_t om = g.cm[m];
+            double cv[16];
+            if (g.beta != 0.0) {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const int64_t n = n0 + col0 + j0 + j;
+                cv[j] = n < g.N ? g.C[om + g.cn[n]] : 0.0;
+              }
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int64_t n = n0 + col0 + j0 + j;
+              if (n < g.N) {
+                const double val = g.alpha * (static_cast<double>(__uint_as_float(h[j])) +
+                                              static_cast<double>(__uint_as_float(l[j])));
+                g.C[om + g.cn[n]] = (g.beta == 0.0) ? val : fma(g.beta, cv[j], val);
+              }
+            }
+          }
+        }
+        continue;
+      }
       // stage 32 rows x 16 columns through shared memory, then write with the
       // lanes along N (coalesced when C is contiguous in N)
       double* stg = stg_all + (warp - kEpiWarp0) * 32 * kStgLd;
@@ -450,9 +625,17 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
 #pragma unroll
       for (int j0 = 0; j0 < COLS; j0 += 16) {
         uint32_t h[16], l[16];
-        tmem_ld16(hi_base + j0, h);
-        tmem_ld16(lo_base + j0, l);
-        tmem_ld_wait();
+        if constexpr (Cfg::kFold) {
+          tmem_ld16(hi_base + j0, h);
+          tmem_ld16(lo_base + j0, l);
+          tmem_ld_wait();
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            h[j] = __float_as_uint(p[j0 + j]);
+            l[j] = 0u;
+          }
+        }
 #pragma unroll
         for (int j = 0; j < 16; ++j)
           stg[lane * kStgLd + j] =
@@ -494,10 +677,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1)
   }
   tc_fence_before();
   __syncthreads();
+  if constexpr (CTA2) {
+    __syncwarp();
+    cluster_sync();  // no remote arrive or MMA into this CTA is pending
+  }
   if (warp == 1) {
     __syncwarp();
     tc_fence_after();
-    tmem_dealloc(tmem, Cfg::kTmemCols);
+    if constexpr (CTA2) tmem_dealloc2(tmem, Cfg::kTmemCols);
+    else tmem_dealloc(tmem, Cfg::kTmemCols);
   }
 }
 
@@ -531,30 +719,57 @@ bool make_map(CUtensorMap* map, const void* base, int64_t slices, int64_t rows, 
 }
 
 
-template <int BN>
+template <int BN, bool CTA2>
 bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
-  using Cfg = TcCfg<BN>;
+  using Cfg = TcCfg<BN, CTA2>;
   CUtensorMap ma, mb;
   if (!make_map(&ma, g.A, g.a_slices, g.Mpad, g.Kpad, BM)) return false;
-  if (!make_map(&mb, g.B, g.b_slices, g.Npad, g.Kpad, BN)) return false;
+  if (!make_map(&mb, g.B, g.b_slices, g.Npad, g.Kpad, Cfg::kBRows)) return false;
   static bool attr_set = false;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(gemm_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(gemm_tc_kernel<BN, CTA2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              Cfg::kSmem) != cudaSuccess)
       return false;
     attr_set = true;
   }
-  const int64_t ntiles = (g.Npad / BN) * (g.Mpad / BM) * (g.ksplit > 1 ? g.ksplit : 1);
-  const int grid = static_cast<int>(ntiles < num_sms() ? ntiles : num_sms());
-  gemm_tc_kernel<BN><<<grid, kThreadsTc, Cfg::kSmem, st>>>(ma, mb, g);
-  return true;
+  const int64_t units = (g.Npad / BN) * (g.Mpad / (CTA2 ? 2 * BM : BM)) * (g.ksplit > 1 ? g.ksplit : 1);
+  if (!CTA2) {
+    const int grid = static_cast<int>(units < num_sms() ? units : num_sms());
+    gemm_tc_kernel<BN, false><<<grid, Cfg::kThreads, Cfg::kSmem, st>>>(ma, mb, g);
+    return true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(Cfg::kThreads);
+  cfg.dynamicSmemBytes = Cfg::kSmem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  static int max_pairs = 0;
+  if (!max_pairs) {
+    cfg.gridDim = dim3(2 * (num_sms() / 2));
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, gemm_tc_kernel<BN, true>, &cfg) != cudaSuccess || n < 1) {
+      cudaGetLastError();
+      n = num_sms() / 2;
+    }
+    max_pairs = n;
+  }
+  const int64_t pairs = units < max_pairs ? units : max_pairs;
+  cfg.gridDim = dim3(static_cast<unsigned>(2 * pairs));
+  return cudaLaunchKernelEx(&cfg, gemm_tc_kernel<BN, true>, ma, mb, g) == cudaSuccess;
 }
 
 }  // namespace
 
-int gemm_tc_pick_bn(int64_t N) {
+int gemm_tc_pick_bn(int64_t N, bool allow256) {
   if (N <= 32) return 32;
   if (N <= 64) return 64;
+  if (allow256 && N >= 256) return 256;
   return 128;
 }
 
@@ -568,10 +783,19 @@ bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
   if (g.ksplit > 1 && (!g.partial || g.kb_per_split < 1 ||
                        static_cast<int64_t>(g.ksplit - 1) * g.kb_per_split >= g.Kpad / BK))
     return false;
+  if (g.cta2) {
+    if (g.Mpad % (2 * BM)) return false;
+    switch (g.bn) {
+      case 64: return launch_bn<64, true>(g, st);
+      case 128: return launch_bn<128, true>(g, st);
+      default: return false;
+    }
+  }
   switch (g.bn) {
-    case 32: return launch_bn<32>(g, st);
-    case 64: return launch_bn<64>(g, st);
-    case 128: return launch_bn<128>(g, st);
+    case 32: return launch_bn<32, false>(g, st);
+    case 64: return launch_bn<64, false>(g, st);
+    case 128: return launch_bn<128, false>(g, st);
+    case 256: return launch_bn<256, false>(g, st);
     default: return false;
   }
 }

@@ -89,12 +89,14 @@ struct GemmTcArgs {
   const int64_t* cm;
   const int64_t* cn;
   double alpha, beta;
-  int bn;                // N tile (32, 64 or 128)
+  int bn;                // N tile (32, 64, 128 or 256)
   int chunk;             // k-blocks per TMEM accumulation (0: default 4)
   int fold;              // chunks summed in FP32 before a float-float fold (0: default 16)
   int ksplit;            // >1: K split over CTAs; partial tiles go to `partial`
   int kb_per_split;      // k-blocks per split (every split gets at least one)
   double* partial;       // [ksplit][Mpad][Npad] FP64 partial tiles (ksplit > 1)
+  int m_major;           // C is contiguous along M: epilogue lanes run along M
+  int cta2;              // CTA pairs (tcgen05 cta_group::2, 256-row tiles); Mpad % 256 == 0, bn >= 64
   int* err;              // device error word
 };
 // Deterministic K-split reduction: C[cm[m] + cn[n]] = beta*C + alpha * sum_s
@@ -107,7 +109,9 @@ int num_sms();
 
 // Returns false if the tensor maps could not be encoded (bad alignment / size).
 bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st);
-int gemm_tc_pick_bn(int64_t N);
+// N tile for a GEMM of N columns; allow256: 256-wide tiles (faster, FP32
+// register accumulation of the chunks) for N >= 256
+int gemm_tc_pick_bn(int64_t N, bool allow256);
 constexpr int kTcBM = 128;
 constexpr int kTcBK = 64;
 

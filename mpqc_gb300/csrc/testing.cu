@@ -1,7 +1,6 @@
 // Test hooks (include/gbcc_testing.h): single-kernel GEMM runs and an FP64
 // throughput probe.  Not used by the solver itself.
 #include <cstdio>
-#include <cstdlib>
 #include <vector>
 
 #include "../../include/gbcc.h"
@@ -29,14 +28,16 @@ __global__ void fp64_fma_probe(double* out, int iters) {
 
 extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
                                  double* Cout, int slices, int repeat, float* ms) {
-  return gbcc_testing_gemm_split(M, N, K, A, B, Cout, slices, 1, repeat, ms);
+  return gbcc_testing_gemm_ex(M, N, K, A, B, Cout, slices, 1, 0, 0, 0, 0, repeat, ms);
 }
 
-extern "C" int gbcc_testing_gemm_split(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
-                                       double* Cout, int slices, int ksplit, int repeat, float* ms) {
+extern "C" int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
+                                    double* Cout, int slices, int ksplit, int bn_req, int cta2, int chunk,
+                                    int fold, int repeat, float* ms) {
   using namespace gbcc;
   if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1 || ksplit < 1)
     return GBCC_ERR_INVALID_ARG;
+  if (bn_req != 0 && bn_req != 32 && bn_req != 64 && bn_req != 128 && bn_req != 256) return GBCC_ERR_INVALID_ARG;
   std::vector<void*> owned;
   auto alloc = [&](size_t bytes) {
     void* p = dev_alloc(bytes);
@@ -82,8 +83,8 @@ extern "C" int gbcc_testing_gemm_split(int64_t M, int64_t N, int64_t K, const do
       for (int r = 0; r < repeat; ++r) launch_gemm_f64(g, st);
       GBCC_CK(cudaEventRecord(e1, st));
     } else {
-      const int bn = gemm_tc_pick_bn(N);
-      const int64_t Mpad = rup(M, kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
+      const int bn = bn_req ? bn_req : (cta2 ? (N <= 64 ? 64 : 128) : gemm_tc_pick_bn(N, false));
+      const int64_t Mpad = rup(M, cta2 ? 2 * kTcBM : kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
       auto* sa = static_cast<__nv_bfloat16*>(alloc(slices * Mpad * Kpad * sizeof(__nv_bfloat16)));
       auto* sb = static_cast<__nv_bfloat16*>(alloc(slices * Npad * Kpad * sizeof(__nv_bfloat16)));
       auto pack = [&](const double* src, int64_t rows, int64_t rows_pad, __nv_bfloat16* dst) {
@@ -106,8 +107,9 @@ extern "C" int gbcc_testing_gemm_split(int64_t M, int64_t N, int64_t K, const do
         for (int b = 0; b < slices; ++b)
           if (a + b < slices) { t.pa[t.npairs] = a; t.pb[t.npairs] = b; ++t.npairs; }
       t.C = dC; t.cm = cm; t.cn = cn; t.alpha = 1.0; t.beta = 0.0; t.bn = bn; t.err = err;
-      if (const char* e = std::getenv("GBCC_TC_CHUNK")) t.chunk = std::atoi(e);
-      if (const char* e = std::getenv("GBCC_TC_FOLD")) t.fold = std::atoi(e);
+      t.cta2 = cta2 ? 1 : 0;
+      t.chunk = chunk;
+      t.fold = fold;
       if (ksplit > 1) {
         const int64_t kblocks = Kpad / kTcBK;
         t.kb_per_split = static_cast<int>((kblocks + ksplit - 1) / ksplit);

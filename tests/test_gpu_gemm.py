@@ -73,12 +73,34 @@ def test_gemm_split_k(tlib, M, N, K, ksplit, slices):
     ref = A @ B.T
     out = np.empty((M, N))
     ms = C.c_float()
-    st = tlib.gbcc_testing_gemm_split(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, slices, ksplit, 1,
-                                      C.byref(ms))
+    st = tlib.gbcc_testing_gemm_ex(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, slices, ksplit,
+                                   0, 0, 0, 0, 1, C.byref(ms))
     assert st == 0
     tol = TOL[slices] + (8 * 2.0**-24 * np.sqrt(K) if slices else 0.0)
     assert np.max(np.abs(out - ref)) <= tol * np.max(np.abs(ref))
     out2 = np.empty((M, N))
-    tlib.gbcc_testing_gemm_split(M, N, K, A.ctypes.data, B.ctypes.data, out2.ctypes.data, slices, ksplit, 1,
-                                 C.byref(ms))
+    tlib.gbcc_testing_gemm_ex(M, N, K, A.ctypes.data, B.ctypes.data, out2.ctypes.data, slices, ksplit,
+                              0, 0, 0, 0, 1, C.byref(ms))
     assert np.array_equal(out, out2)
+
+
+# kernel variants: (bn, cta2, chunk, fold); bn 256 sums chunks in FP32 registers
+VARIANTS = [(256, 0, 4, 0), (256, 0, 8, 0), (128, 1, 4, 16), (64, 1, 4, 16), (128, 0, 1, 1), (64, 0, 16, 64)]
+
+
+@pytest.mark.parametrize("bn,cta2,chunk,fold", VARIANTS)
+@pytest.mark.parametrize("M,N,K,ksplit", [(256, 256, 64, 1), (300, 520, 1000, 1), (700, 300, 2000, 3),
+                                          (128, 256, 6000, 5)])
+def test_gemm_kernel_variants(tlib, M, N, K, ksplit, bn, cta2, chunk, fold):
+    rng = np.random.default_rng(M + N + K + bn)
+    A = rng.normal(size=(M, K))
+    B = rng.normal(size=(N, K))
+    ref = A @ B.T
+    out = np.empty((M, N))
+    ms = C.c_float()
+    st = tlib.gbcc_testing_gemm_ex(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, 3, ksplit, bn, cta2,
+                                   chunk, fold, 1, C.byref(ms))
+    assert st == 0
+    # FP32 accumulation of the chunks (bn 256) grows like sqrt(number of chunks)
+    tol = TOL[3] + 8 * 2.0**-24 * np.sqrt(K)
+    assert np.max(np.abs(out - ref)) <= tol * np.max(np.abs(ref))
