@@ -255,6 +255,23 @@ def ours(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    if args.residual_only:
+        # profiling driver: warmup + steps mixed residuals and nothing else;
+        # reports which tensor-core GEMM launch of a residual is the ladder
+        for _ in range(args.warmup + args.steps):
+            s.residual(t1, t2, r1, r2, precision="mixed")
+        torch.cuda.synchronize()
+        prof = s.profile_residual(precision="mixed")
+        tc = [p for p in prof if p["pairs"] > 0]
+        ordinal = next(i for i, p in enumerate(tc) if p["cls"] == 0)
+        launches = s.last_launches()
+        s.close()
+        if rank == 0:
+            print(json.dumps({"residual_only": True, "o": o, "v": v, "naux": naux,
+                              "tc_launches_per_residual": len(tc), "ladder_tc_ordinal": ordinal,
+                              "launches_per_residual": launches}), flush=True)
+        return 0
+
     # ---- mixed precision, device-resident inputs
     for _ in range(args.warmup):
         s.residual(t1, t2, r1, r2, precision="mixed")
@@ -372,6 +389,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--residual-only", action="store_true",
+                    help="profiling driver: run warmup+steps mixed residuals only")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
