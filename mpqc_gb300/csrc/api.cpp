@@ -188,6 +188,7 @@ void commit_inputs(gbcc_handle* h) {
   h->aux->end();
   h->eng->reset_plans();
   h->prepacked = false;
+  h->eng->set_frozen({S.t1, S.t2, S.tau});
   h->eng->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
   gbcc::residual_program(*h->eng, S);
   h->eng->end();

@@ -111,6 +111,14 @@ std::string set_and(const std::string& a, const std::string& b) {
   return out;
 }
 
+// Gather direction: read along R (and transpose in shared memory) when the
+// first term is unit-stride along R but not along C.
+int pick_transpose(const std::vector<int64_t>& ra, const std::vector<int64_t>& ca) {
+  const bool r_unit = ra.size() > 1 && ra[1] - ra[0] == 1;
+  const bool c_unit = ca.size() > 1 && ca[1] - ca[0] == 1;
+  return (r_unit && !c_unit && ra.size() >= 32) ? 1 : 0;
+}
+
 bool same_set(const std::string& a, const std::string& b) {
   std::string x = a, y = b;
   std::sort(x.begin(), x.end());
@@ -136,6 +144,11 @@ struct OperandPlan {
   int64_t rows_pad = 0, Kpad = 0;
   __nv_bfloat16* packed = nullptr;  // dedicated split buffer (constants)
   size_t pack_elems = 0;
+  // reuse of one split pack by several contractions within a residual
+  std::string sig;        // non-empty: sources are not written during a residual
+  bool cache_first = false;  // packs into cache_buf
+  bool cache_reuse = false;  // reads cache_buf packed by an earlier contraction
+  __nv_bfloat16* cache_buf = nullptr;
 };
 
 struct GemmPlan {
@@ -262,6 +275,7 @@ Tensor* Engine::find(const std::string& name) {
 }
 
 void Engine::reset_plans() {
+  pack_uses_.clear();
   sites_.clear();
   for (void* p : owned_) dev_free(p);
   owned_.clear();
@@ -366,8 +380,10 @@ void Engine::assign(const Ix& c, double beta, const std::vector<Factor>& terms) 
     GatherTerm& T = g.t[t];
     T.coef = terms[t].coef;
     T.a = terms[t].a.t->d;
-    T.ra = upload(offsets(rlab, e, terms[t].a)).d;
-    T.ca = upload(offsets(clab, e, terms[t].a)).d;
+    const std::vector<int64_t> hra = offsets(rlab, e, terms[t].a), hca = offsets(clab, e, terms[t].a);
+    if (t == 0) g.transpose = pick_transpose(hra, hca);
+    T.ra = upload(hra).d;
+    T.ca = upload(hca).d;
     if (terms[t].b.t) {
       T.b = terms[t].b.t->d;
       T.rb = upload(offsets(rlab, e, terms[t].b)).d;
@@ -412,8 +428,10 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         if (op.constant) {
           if (!op.packed) throw Error(GBCC_ERR_STATE, "engine: constant operand not packed");
           panel[side] = op.packed;
+        } else if (op.cache_reuse) {
+          panel[side] = op.cache_buf;
         } else {
-          panel[side] = side == 0 ? wbfa_ : wbfb_;
+          panel[side] = op.cache_first ? op.cache_buf : (side == 0 ? wbfa_ : wbfb_);
           GatherArgs g = op.gather;
           g.outs = panel[side];
           launch_gather(g, stream_);
@@ -601,8 +619,10 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       for (size_t t = 0; t < op.terms.size(); ++t) {
         g.t[t].coef = op.terms[t].coef;
         g.t[t].a = op.terms[t].x.t->d;
-        g.t[t].ra = upload(offsets(op.ext, e, op.terms[t].x)).d;
-        g.t[t].ca = upload(offsets(op.kord, e, op.terms[t].x)).d;
+        const std::vector<int64_t> hra = offsets(op.ext, e, op.terms[t].x), hca = offsets(op.kord, e, op.terms[t].x);
+        if (t == 0) g.transpose = pick_transpose(hra, hca);
+        g.t[t].ra = upload(hra).d;
+        g.t[t].ca = upload(hca).d;
       }
       g.R = op.rows;
       g.C = op.K;
@@ -669,6 +689,20 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         g.nslices = slices;
         g.slice_stride = op.rows_pad * Kpad;
         const size_t need = static_cast<size_t>(slices) * op.rows_pad * Kpad;
+        if (!op.constant) {
+          bool frozen = true;
+          std::string sig;
+          for (const auto& l : op.terms) {
+            frozen = frozen && frozen_.count(l.x.t) > 0;
+            sig += l.x.t->name + "(" + l.x.lab + ")*" + std::to_string(l.coef) + ";";
+          }
+          if (frozen) {
+            op.sig = sig + op.ext + "|" + op.kord + "|" + std::to_string(slices) + "|" +
+                     std::to_string(op.rows_pad) + "|" + std::to_string(Kpad);
+            op.pack_elems = need;
+            pack_uses_[op.sig].push_back(&op);
+          }
+        }
         if (op.constant) {
           op.pack_elems = need;  // allocated and packed by finalize(true)
         } else if (side == 0) {
@@ -708,6 +742,21 @@ void Engine::finalize(bool prepack_mixed) {
   dev_free(wpart_);
   wpart_ = static_cast<double*>(dev_alloc(wspart_ * sizeof(double)));
   bytes_ += (ws64_a_ + ws64_b_ + wspart_) * sizeof(double) + (wsbf_a_ + wsbf_b_) * sizeof(__nv_bfloat16);
+  // packs shared by several contractions of a residual get their own buffer
+  for (auto& kv : pack_uses_) {
+    if (kv.second.size() < 2) continue;
+    OperandPlan* first = kv.second.front();
+    if (!first->cache_buf) {
+      first->cache_buf = static_cast<__nv_bfloat16*>(dev_alloc(first->pack_elems * sizeof(__nv_bfloat16)));
+      owned_.push_back(first->cache_buf);
+      bytes_ += first->pack_elems * sizeof(__nv_bfloat16);
+    }
+    first->cache_first = true;
+    for (size_t i = 1; i < kv.second.size(); ++i) {
+      kv.second[i]->cache_reuse = true;
+      kv.second[i]->cache_buf = first->cache_buf;
+    }
+  }
   if (prepack_mixed) {
     for (auto& sp : sites_) {
       if (sp->kind != 1) continue;

@@ -24,6 +24,7 @@
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/gbcc.h"
@@ -124,6 +125,9 @@ class Engine {
   void set_chunk(int k) { chunk_ = k; }
   // Record CUDA events around every operation of EXEC passes.
   void set_profile(bool on) { profile_ = on; }
+  // Tensors a residual program reads but never writes (its amplitude inputs);
+  // packs of them can be shared between contractions.
+  void set_frozen(std::initializer_list<const Tensor*> ts) { frozen_ = std::unordered_set<const Tensor*>(ts); }
   std::vector<SiteStat> site_stats(int precision);
 
   // Persistent device tensor owned by the engine (allocated on first request).
@@ -178,6 +182,8 @@ class Engine {
   int* err_ = nullptr;
   int chunk_ = 4;  // k-blocks per TMEM accumulation in the tensor-core GEMM
   bool profile_ = false;
+  std::unordered_set<const Tensor*> frozen_;
+  std::unordered_map<std::string, std::vector<struct OperandPlan*>> pack_uses_;
   double flops_ = 0.0;
   size_t bytes_ = 0;
   int n_tc_ = 0;

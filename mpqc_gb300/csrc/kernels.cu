@@ -61,6 +61,52 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs g) {
   }
 }
 
+// Same contract as gather_kernel for sources contiguous along R: a 32 x 32
+// tile is read with the lanes along R (coalesced), transposed through shared
+// memory and written with the lanes along C (coalesced).  Block 32 x 8.
+__global__ void __launch_bounds__(256) gather_t_kernel(GatherArgs g) {
+  __shared__ double tile[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int64_t nrt = (g.Rpad + 31) / 32, nct = (g.Cpad + 31) / 32;
+  for (int64_t t = blockIdx.x; t < nrt * nct; t += gridDim.x) {
+    const int64_t r0 = (t / nct) * 32, c0 = (t % nct) * 32;
+    // read: lanes along r
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t r = r0 + tx, c = c0 + ty + 8 * k;
+      double val = 0.0;
+      if (r < g.R && c < g.C) {
+#pragma unroll
+        for (int q = 0; q < kMaxTerms; ++q) {
+          if (q < g.nterms) {
+            const GatherTerm& T = g.t[q];
+            double x = T.a[T.ra[r] + T.ca[c]];
+            if (T.b) x *= T.b[T.rb[r] + T.cb[c]];
+            val = fma(T.coef, x, val);
+          }
+        }
+      }
+      tile[ty + 8 * k][tx] = val;
+    }
+    __syncthreads();
+    // write: lanes along c
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t r = r0 + ty + 8 * k, c = c0 + tx;
+      if (r < g.Rpad && c < g.Cpad) {
+        const double val = tile[tx][ty + 8 * k];
+        if (g.out) {
+          double* p = g.out + r * g.ldo + c;
+          *p = (g.beta == 0.0) ? val : fma(g.beta, *p, val);
+        } else {
+          split_store(val, g.outs, g.nslices, g.slice_stride, r * g.ldo + c);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -362,6 +408,12 @@ void launch_splitk_reduce(int64_t M, int64_t N, int ksplit, const double* partia
 
 void launch_gather(const GatherArgs& g, cudaStream_t st) {
   if (g.Rpad <= 0 || g.Cpad <= 0) return;
+  if (g.transpose) {
+    const int64_t tiles = ((g.Rpad + 31) / 32) * ((g.Cpad + 31) / 32);
+    const int64_t grid = std::min<int64_t>(tiles, 152LL * 16);
+    gather_t_kernel<<<static_cast<unsigned>(grid), dim3(32, 8), 0, st>>>(g);
+    return;
+  }
   int bx = 1;
   while (bx < g.Cpad && bx < kThreads) bx <<= 1;
   if (bx < 32) bx = 32;

@@ -45,6 +45,9 @@ struct GatherArgs {
   __nv_bfloat16* outs;
   int nslices;
   int64_t slice_stride;
+  // 1: the sources are contiguous along R, not C -- read 32 x 32 tiles along R
+  // and transpose them through shared memory (set by the planner)
+  int transpose;
 };
 
 void launch_gather(const GatherArgs& args, cudaStream_t st);
