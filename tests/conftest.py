@@ -47,3 +47,25 @@ def gbcc_lib():
     build.build()
     from mpqc_gb300 import _lib
     return _lib.load()
+
+
+INTEGRAL_NAMES = ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc", "Gabcd")
+
+
+def freeze_first_occupied(blocks, eps_o, n=1):
+    """Blocks of the same orbitals with the lowest ``n`` occupied orbitals frozen."""
+    s = slice(n, None)
+    fc = dict(Fia=blocks["Fia"][s], Fij=blocks["Fij"][s, s], Fab=blocks["Fab"],
+              Gijab=blocks["Gijab"][s, s], Gijkl=blocks["Gijkl"][s, s, s, s],
+              Giajb=blocks["Giajb"][s, :, s], Gijka=blocks["Gijka"][s, s, s],
+              Giabc=blocks["Giabc"][s], Gabcd=blocks["Gabcd"])
+    return {k: np.ascontiguousarray(v) for k, v in fc.items()}, np.ascontiguousarray(eps_o[s])
+
+
+def load_molecule(name):
+    """Water MO blocks (MPQC annotation order), orbital energies and the whole
+    fixture (oracle amplitudes and energies, the reference's recorded energies)."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    g = {k: z[k] for k in z.files}
+    blocks = {k: np.ascontiguousarray(g[k]) for k in INTEGRAL_NAMES}
+    return blocks, g["eps_o"], g["eps_v"], g

@@ -82,8 +82,10 @@ def test_gepp_matches_lapack():
     for n in (1, 2, 5, 9):
         A = rng.normal(size=(n, n)) + n * np.eye(n)
         b = rng.normal(size=n)
-        assert np.allclose(R.gepp_solve(A, b), np.linalg.solve(A, b), rtol=1e-12, atol=1e-12)
-    assert R.gepp_solve(np.zeros((3, 3)), np.ones(3)) is None
+        x, det = R.gepp_solve(A, b)
+        assert np.allclose(x, np.linalg.solve(A, b), rtol=1e-12, atol=1e-12)
+        assert np.isclose(det, abs(np.linalg.det(A)), rtol=1e-10)
+    assert R.gepp_solve(np.zeros((3, 3)), np.ones(3)) == (None, 0.0)
 
 
 def test_diis_solves_linear_fixed_point():
