@@ -119,11 +119,11 @@ class _DevArray:
                                          "data": (int(ptr), False), "version": 3, "strides": None}
 
 
-def build_inputs(torch, solver, o, v, naux, seed, dev):
+def build_inputs(torch, solver, o, v, naux, seed, dev, b_scale=0.05):
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
     n = o + v
-    B = torch.randn((naux, n, n), generator=g, device=dev, dtype=torch.float64) * 0.05
+    B = torch.randn((naux, n, n), generator=g, device=dev, dtype=torch.float64) * b_scale
     B = (B + B.transpose(1, 2)) * (0.5 ** 0.5)
     eps_o = torch.sort(torch.rand(o, generator=g, device=dev, dtype=torch.float64) * 1.2 - 1.5).values
     eps_v = torch.sort(torch.rand(v, generator=g, device=dev, dtype=torch.float64) * 2.9 + 0.1).values
@@ -245,8 +245,13 @@ def ours(args):
     log(f"[bench] rank {rank}: building inputs o={o} v={v} naux={naux} on {torch.cuda.get_device_name(dev)}")
     t_setup = time.perf_counter()
     s = Solver(o, v, precision="mixed", slices=(args.slices,) * 3, device=local)
-    t1, t2 = build_inputs(torch, s, o, v, naux, args.seed, dev)
+    t1, t2 = build_inputs(torch, s, o, v, naux, args.seed, dev,
+                          b_scale=0.05 if args.b_scale is None else args.b_scale)
     log(f"[bench] inputs + split packing ready in {time.perf_counter() - t_setup:.1f} s")
+    # slice counts per term class from the error measured at this workload's
+    # amplitudes (fewest slices within 1e-5 of the 3-slice residual)
+    slices_used, slice_err = s.calibrate_slices(t1, t2)
+    log(f"[bench] slices (ladder, ring, other) = {slices_used}, rel. change vs 3 slices = {slice_err}")
     r1 = torch.empty_like(t1)
     r2 = torch.empty_like(t2)
 
@@ -361,7 +366,10 @@ def ours(args):
         "data": "synthetic",
         "config": {"workload": "synthetic CCSD doubles residual, one R1+R2 evaluation",
                    "o": o, "v": v, "naux": naux, "parallelism": f"replicas{ws}",
-                   "precision": f"split-BF16 x{args.slices} slices, float-float chunk accumulation",
+                   "precision": "split-BF16 slices per class (ladder, ring, other) = "
+                                f"{slices_used}, FP32/float-float chunk accumulation",
+                   "slices": list(slices_used),
+                   "slice_rel_change_vs_3": list(slice_err),
                    "flops_per_step": F, "l2": "inputs larger than L2 (no flush)"},
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io, "ms_per_step": e2e_ms},
@@ -376,6 +384,60 @@ def ours(args):
     return 0
 
 
+def solve_report(args):
+    """Whole Jacobi+DIIS solves from t = 0 on one synthetic input: mixed precision
+    (split-BF16 bulk contractions, then plain-FP64 refinement iterations) and plain
+    FP64, with s/iter of each and the mixed result's |dE_corr| and max|dT2|
+    against the FP64 one."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    from mpqc_gb300 import build as gb
+    gb.build()
+    from mpqc_gb300 import Solver
+    o, v, naux = args.o, args.v, args.naux
+    # random DF factors give a pair correlation energy of about 0.45 v^2 naux b^4;
+    # this scale puts it near 1.5e-3 Eh (real molecules: ~1e-3 Eh per pair)
+    bs = (3.0e-3 / (v * v * naux)) ** 0.25 if args.b_scale is None else args.b_scale
+    F = flop_count(o, v)
+    runs, amps = {}, {}
+    for prec in ("mixed",) if args.no_solve_fp64 else ("mixed", "fp64"):
+        s = Solver(o, v, precision=prec, slices=(args.slices,) * 3, target_precision=args.solve_precision,
+                   max_iter=args.max_iter, refine_iters=2)
+        build_inputs(torch, s, o, v, naux, args.seed, dev, b_scale=bs)
+        sl_used, sl_err = s.slice_policy()
+        t0 = time.perf_counter()
+        e, t1, t2, rep = s.solve()
+        wall = time.perf_counter() - t0
+        s.close()
+        sm, sf = rep.seconds_residual_mixed, rep.seconds_residual_fp64
+        runs[prec] = {"e_corr": e, "converged": rep.converged, "iters": rep.iters,
+                      "mixed_iters": rep.mixed_iters, "fp64_iters": rep.fp64_iters,
+                      "seconds_total": wall,
+                      "s_per_iter_mixed": sm or None, "s_per_iter_fp64": sf or None,
+                      "tflops_mixed": F / sm / 1e12 if sm else None,
+                      "tflops_fp64": F / sf / 1e12 if sf else None}
+        if prec == "mixed":
+            runs[prec]["slices"] = list(sl_used)
+            runs[prec]["slice_rel_change_vs_3"] = list(sl_err)
+        amps[prec] = (t1, t2)
+        log(f"[solve] {prec}: E={e:.12f} iters={rep.iters} ({rep.mixed_iters} mixed) "
+            f"converged={rep.converged} {wall:.1f} s")
+    line = {"solve": True, "o": o, "v": v, "naux": naux, "b_scale": bs, "seed": args.seed,
+            "flops_per_iter": F, "target_precision": args.solve_precision, "runs": runs,
+            "data": "synthetic DF-factored integrals, B ~ N(0, b_scale), t = 0 start"}
+    if "fp64" in runs:
+        m, f = runs["mixed"], runs["fp64"]
+        line["abs_dE_mixed_vs_fp64"] = abs(m["e_corr"] - f["e_corr"])
+        line["max_abs_dT2_mixed_vs_fp64"] = float(np.max(np.abs(amps["mixed"][1] - amps["fp64"][1])))
+        line["max_abs_dT1_mixed_vs_fp64"] = float(np.max(np.abs(amps["mixed"][0] - amps["fp64"][0])))
+        if m["s_per_iter_mixed"] and f["s_per_iter_fp64"]:
+            line["per_iteration_speedup"] = f["s_per_iter_fp64"] / m["s_per_iter_mixed"]
+        line["solve_speedup"] = f["seconds_total"] / m["seconds_total"]
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -385,15 +447,26 @@ def main():
     ap.add_argument("--o", type=int, default=32)
     ap.add_argument("--v", type=int, default=320)
     ap.add_argument("--naux", type=int, default=1200)
-    ap.add_argument("--slices", type=int, default=3)
+    ap.add_argument("--slices", type=int, default=0,
+                    help="BF16 slices per operand for every class; 0 (default): chosen per class "
+                         "from the measured residual error")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--residual-only", action="store_true",
                     help="profiling driver: run warmup+steps mixed residuals only")
+    ap.add_argument("--solve", action="store_true",
+                    help="whole mixed and plain-FP64 solves from t = 0; prints one JSON line")
+    ap.add_argument("--b-scale", type=float, default=None,
+                    help="std of the DF factor B (default 0.05; with --solve (3e-3 / (v^2 naux))^(1/4))")
+    ap.add_argument("--solve-precision", type=float, default=1e-8)
+    ap.add_argument("--max-iter", type=int, default=40)
+    ap.add_argument("--no-solve-fp64", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.solve:
+        return solve_report(args)
     return ours(args)
 
 

@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define GBCC_ABI_VERSION 1
+#define GBCC_ABI_VERSION 2
 
 typedef enum gbcc_status {
   GBCC_OK = 0,
@@ -62,11 +62,13 @@ typedef struct gbcc_config {
   int64_t o;                   /* active occupied orbitals                                     */
   int64_t v;                   /* virtual orbitals                                             */
   int32_t precision;           /* gbcc_precision                                               */
-  int32_t slices_ladder;       /* BF16 slices per operand, particle-particle ladder (1..3)     */
+  int32_t slices_ladder;       /* BF16 slices per operand, particle-particle ladder (1..3;     */
+                               /* 0, the default: chosen from the measured error, see below) */
   int32_t slices_ring;         /* ... o^3 v^3 ring terms and the ladder's T1 part (1..3)       */
   int32_t slices_other;        /* ... every remaining contraction (1..3)                       */
   int32_t refine_iters;        /* plain-FP64 iterations after the mixed phase                  */
-  double mixed_switch_precision; /* mixed phase ends once converged to this precision          */
+  double mixed_switch_precision; /* mixed phase ends once converged to this precision;         */
+                               /* 0 (default): target_precision                              */
   int32_t max_iter;            /* "max_iter", default 30 (ccsd.h:104)                          */
   double target_precision;     /* Energy precision, default 1e-9 (energy.h:45)                 */
   int32_t diis_start;          /* "diis_start", default 1      (cc/solvers.h:93)               */
@@ -76,6 +78,10 @@ typedef struct gbcc_config {
   int32_t diis_group_nstart;   /* "diis_group_nstart", default 1                               */
   int32_t verbose;             /* print the iteration table (ccsd.h:28-46)                     */
   int32_t device;              /* CUDA device ordinal                                          */
+  int32_t use_graphs;          /* 1 (default): each residual evaluation replays a CUDA graph    */
+                               /* captured on first use per precision; 0: direct launches     */
+  double slice_tolerance;      /* automatic slices: largest max|dr|/max|r| (r1 and r2) a class */
+                               /* may add against 3 slices at the probe amplitudes; 1e-5     */
 } gbcc_config;
 
 typedef struct gbcc_inputs {
@@ -175,6 +181,22 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
 
 /* Release the handle and all its device memory.  NULL is accepted. */
 gbcc_status gbcc_destroy(gbcc_handle* h);
+
+/* Slice counts in use per contraction class {ladder, ring, other} once inputs
+ * are set, and for classes configured as 0 the measured max|dr|/max|r| of the
+ * chosen count against 3 slices (-1: fixed by the configuration).  In mixed
+ * mode gbcc_set_inputs / gbcc_commit_inputs choose them: at probe amplitudes
+ * (two Jacobi steps from t = 0) each automatic class takes the fewest slices
+ * (3, 2 or 1) whose residual change stays within slice_tolerance.  No
+ * reference counterpart (MPQC computes in FP64 only). */
+gbcc_status gbcc_slice_policy(gbcc_handle* h, int32_t slices[3], double rel_change[3]);
+
+/* Re-choose the automatic slice counts (mixed handles) at the caller's
+ * amplitudes t1[v][o], t2[v][v][o][o] (host or device) instead of the probe
+ * amplitudes gbcc_set_inputs used, e.g. before evaluating residuals at given
+ * amplitudes with gbcc_residual.  Same rule as above; leaves t = 0 in the
+ * handle.  No reference counterpart. */
+gbcc_status gbcc_calibrate_slices(gbcc_handle* h, const double* t1_ai, const double* t2_abij);
 
 /* Message of the last failing call on this handle ("" if none); with a NULL
  * handle, the message of the last failed gbcc_create on this thread. */

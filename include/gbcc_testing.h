@@ -30,6 +30,10 @@ int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const do
 int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
                          int slices, int ksplit, int bn, int cta2, int chunk, int fold, int repeat, float* ms);
 
+/* The BF16 split the packing kernels apply: x[0..n) (host) -> out[s*n + i]
+ * (host), the bit patterns of slices s = 0..nslices-1 (nslices 1..3). */
+int gbcc_testing_split(const double* x, int64_t n, int nslices, uint16_t* out);
+
 /* Peak probe: FP64 FMA throughput of this GPU in GFLOP/s (a register-resident
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);

@@ -25,10 +25,10 @@ EXPORTS = (
     "gbcc_abi_version", "gbcc_status_string", "gbcc_config_default", "gbcc_create",
     "gbcc_set_inputs", "gbcc_device_inputs", "gbcc_commit_inputs", "gbcc_residual",
     "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
-    "gbcc_last_error",
+    "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error",
 )
 # test hooks of include/gbcc_testing.h
-TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
+TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_split", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims")
 
@@ -42,7 +42,8 @@ class Config(C.Structure):
         ("max_iter", C.c_int32), ("target_precision", C.c_double),
         ("diis_start", C.c_int32), ("n_diis", C.c_int32), ("diis_damp", C.c_double),
         ("diis_ngroup", C.c_int32), ("diis_group_nstart", C.c_int32),
-        ("verbose", C.c_int32), ("device", C.c_int32),
+        ("verbose", C.c_int32), ("device", C.c_int32), ("use_graphs", C.c_int32),
+        ("slice_tolerance", C.c_double),
     ]
 
 
@@ -94,6 +95,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_testing_gemm_ex.restype = C.c_int
     lib.gbcc_testing_gemm_ex.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp] + [C.c_int] * 7 + \
         [C.POINTER(C.c_float)]
+    lib.gbcc_testing_split.restype = C.c_int
+    lib.gbcc_testing_split.argtypes = [vp, C.c_int64, C.c_int, vp]
     lib.gbcc_testing_fp64_peak.restype = C.c_int
     lib.gbcc_testing_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     ip = C.POINTER(C.c_int)
@@ -121,6 +124,10 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_solve.argtypes = [vp, vp, vp, dp, C.POINTER(Report)]
     lib.gbcc_destroy.restype = C.c_int
     lib.gbcc_destroy.argtypes = [vp]
+    lib.gbcc_calibrate_slices.restype = C.c_int
+    lib.gbcc_calibrate_slices.argtypes = [vp, vp, vp]
+    lib.gbcc_slice_policy.restype = C.c_int
+    lib.gbcc_slice_policy.argtypes = [vp, vp, vp]
     lib.gbcc_last_error.restype = C.c_char_p
     lib.gbcc_last_error.argtypes = [vp]
     del i64

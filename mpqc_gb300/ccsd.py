@@ -73,10 +73,10 @@ class Solver:
     """One ``gbcc_handle``: device-resident integrals, residual engine and
     Jacobi+DIIS loop for fixed (o, v)."""
 
-    def __init__(self, o, v, precision="fp64", slices=(3, 3, 3), refine_iters=2,
-                 mixed_switch_precision=1e-7, max_iter=30, target_precision=1e-9,
+    def __init__(self, o, v, precision="fp64", slices=(0, 0, 0), refine_iters=2,
+                 mixed_switch_precision=0.0, max_iter=30, target_precision=1e-9,
                  diis_start=1, n_diis=8, diis_damp=0.0, diis_ngroup=1, diis_group_nstart=1,
-                 verbose=False, device=0):
+                 verbose=False, device=0, use_graphs=True, slice_tolerance=1e-5):
         self.lib = L.load()
         cfg = L.Config()
         self.lib.gbcc_config_default(C.byref(cfg))
@@ -92,6 +92,8 @@ class Solver:
         cfg.diis_ngroup, cfg.diis_group_nstart = int(diis_ngroup), int(diis_group_nstart)
         cfg.verbose = int(bool(verbose))
         cfg.device = int(device)
+        cfg.use_graphs = int(bool(use_graphs))
+        cfg.slice_tolerance = float(slice_tolerance)
         self.cfg = cfg
         self.o, self.v = int(o), int(v)
         h = C.c_void_p()
@@ -180,6 +182,20 @@ class Solver:
         _check(self.lib, self.h, self.lib.gbcc_residual_ex(self.h, prec, _ptr(t1), _ptr(t2), _ptr(r1), _ptr(r2)))
         return r1, r2
 
+    def calibrate_slices(self, t1, t2):
+        """Re-choose the automatic slice counts at these amplitudes (numpy or
+        torch CUDA arrays); returns slice_policy()."""
+        _check(self.lib, self.h, self.lib.gbcc_calibrate_slices(self.h, _ptr(t1), _ptr(t2)))
+        return self.slice_policy()
+
+    def slice_policy(self):
+        """((ladder, ring, other) slice counts in use, measured relative residual
+        change of each automatically chosen count against 3 slices or None)."""
+        sl = (C.c_int32 * 3)()
+        err = (C.c_double * 3)()
+        _check(self.lib, self.h, self.lib.gbcc_slice_policy(self.h, sl, err))
+        return tuple(sl), tuple(None if e < 0 else e for e in err)
+
     def energy(self, t1, t2, r1, r2):
         e, err = C.c_double(), C.c_double()
         _check(self.lib, self.h, self.lib.gbcc_energy(self.h, _ptr(t1), _ptr(t2), _ptr(r1), _ptr(r2),
@@ -220,8 +236,8 @@ class CCSD:
     ``diis_start`` (1), ``n_diis`` (8), ``diis_damp`` (0.0), ``diis_ngroup`` (1),
     ``diis_group_nstart`` (1), ``precision`` (the Energy property precision,
     1e-9).  Additional keys of this implementation: ``gbcc_precision``
-    ("fp64" | "mixed"), ``slices`` ([ladder, ring, other], default [3,3,3]),
-    ``refine_iters`` (2), ``mixed_switch_precision`` (1e-7), ``device`` (0).
+    ("fp64" | "mixed"), ``slices`` ([ladder, ring, other], default [0,0,0]: chosen from the measured error),
+    ``refine_iters`` (2), ``mixed_switch_precision`` (0: the target precision), ``device`` (0).
     """
 
     def __init__(self, kv: dict):
@@ -252,9 +268,9 @@ class CCSD:
         o, v = np.asarray(eps_o).size if isinstance(eps_o, np.ndarray) else eps_o.numel(), \
             np.asarray(eps_v).size if isinstance(eps_v, np.ndarray) else eps_v.numel()
         kv = self.kv
-        with Solver(o, v, precision=kv.get("gbcc_precision", "fp64"), slices=kv.get("slices", (3, 3, 3)),
+        with Solver(o, v, precision=kv.get("gbcc_precision", "fp64"), slices=kv.get("slices", (0, 0, 0)),
                     refine_iters=kv.get("refine_iters", 2),
-                    mixed_switch_precision=kv.get("mixed_switch_precision", 1e-7),
+                    mixed_switch_precision=kv.get("mixed_switch_precision", 0.0),
                     max_iter=self.max_iter, target_precision=self.precision,
                     diis_start=kv.get("diis_start", 1), n_diis=kv.get("n_diis", 8),
                     diis_damp=kv.get("diis_damp", 0.0), diis_ngroup=kv.get("diis_ngroup", 1),

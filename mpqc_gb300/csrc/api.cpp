@@ -8,6 +8,7 @@
 #include <array>
 #include <chrono>
 #include <cmath>
+#include <limits>
 #include <utility>
 #include <cstdio>
 #include <cstring>
@@ -46,6 +47,15 @@ struct gbcc_handle {
   cudaEvent_t slots[8] = {};
   std::vector<double> prof_gemm_ms;
   std::vector<std::array<int64_t, 3>> prof_dims;
+  // residual program captured as a CUDA graph, one per precision (FP64, mixed)
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_launches[2] = {0, 0};
+  bool profiling = false;
+  bool calibrating = false;
+  // slice counts in use per class (ladder, ring, other) and, for classes the
+  // calibration chose, the measured relative residual change; -1 when not measured
+  int slices_used[3] = {3, 3, 3};
+  double slice_err[3] = {-1.0, -1.0, -1.0};
 };
 
 namespace {
@@ -104,26 +114,70 @@ bool check_config(const gbcc_config* c, std::string& why) {
   if (c->o > 4096 || c->v > 8192) { why = "o or v out of range"; return false; }
   if (c->precision != GBCC_PREC_FP64 && c->precision != GBCC_PREC_MIXED) { why = "bad precision"; return false; }
   for (int s : {c->slices_ladder, c->slices_ring, c->slices_other})
-    if (s < 1 || s > 3) { why = "slices must be 1..3"; return false; }
+    if (s < 0 || s > 3) { why = "slices must be 0 (automatic) or 1..3"; return false; }
+  if (!(c->slice_tolerance > 0.0)) { why = "slice_tolerance must be > 0"; return false; }
   if (c->n_diis < 1 || c->n_diis > 16) { why = "n_diis must be 1..16"; return false; }
   if (c->diis_ngroup < 1 || c->diis_start < 0 || c->diis_group_nstart < 0) { why = "bad DIIS parameters"; return false; }
   if (!(c->diis_damp >= 0.0)) { why = "diis_damp must be >= 0"; return false; }
   if (c->max_iter < 1) { why = "max_iter must be >= 1"; return false; }
   if (!(c->target_precision > 0.0)) { why = "target_precision must be > 0"; return false; }
   if (c->refine_iters < 0) { why = "refine_iters must be >= 0"; return false; }
+  if (!(c->mixed_switch_precision >= 0.0)) { why = "mixed_switch_precision must be >= 0"; return false; }
   return true;
 }
 
-void run_residual(gbcc_handle* h, int precision) {
+void drop_graphs(gbcc_handle* h) {
+  for (auto& g : h->graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  h->graph_launches[0] = h->graph_launches[1] = 0;
+}
+
+// r1, r2 of the device-resident t1, t2, tau.  The first evaluation in each
+// precision is captured into a CUDA graph (every launch of the EXEC pass has
+// fixed pointers, sizes and tensor maps once the plan is finalised); later
+// evaluations replay it.  Returns the number of kernels it enqueued.
+int enqueue_residual_program(gbcc_handle* h, int precision) {
   if (precision == GBCC_PREC_MIXED && !h->prepacked) {
     h->eng->finalize(true);
     h->prepacked = true;
   }
+  auto direct = [&]() {
+    h->eng->begin(gbcc::Mode::kExec, precision);
+    gbcc::residual_program(*h->eng, h->S);
+    h->eng->end();
+    return h->eng->kernel_launches();
+  };
+  if (!h->cfg.use_graphs || h->profiling || h->calibrating) return direct();
+  const int gi = precision == GBCC_PREC_MIXED ? 1 : 0;
+  if (!h->graph[gi]) {
+    cudaGraph_t g = nullptr;
+    GBCC_CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int n = 0;
+    try {
+      n = direct();
+    } catch (...) {
+      cudaStreamEndCapture(h->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      throw;
+    }
+    GBCC_CK(cudaStreamEndCapture(h->stream, &g));
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) throw Error(GBCC_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    h->graph[gi] = ge;
+    h->graph_launches[gi] = n;
+  }
+  GBCC_CK(cudaGraphLaunch(h->graph[gi], h->stream));
+  return h->graph_launches[gi];
+}
+
+void run_residual(gbcc_handle* h, int precision) {
   gbcc::launch_make_tau(h->cfg.o, h->cfg.v, h->S.t1->d, h->S.t2->d, h->S.tau->d, h->stream);
-  h->eng->begin(gbcc::Mode::kExec, precision);
-  gbcc::residual_program(*h->eng, h->S);
-  h->eng->end();
-  h->last_launches = 1 + h->eng->kernel_launches();
+  h->last_launches = 1 + enqueue_residual_program(h, precision);
 }
 
 // E and error of the current t/tau/r (device-resident); returns {E, error}
@@ -174,6 +228,101 @@ void validate_eps(const double* eps_o, const double* eps_v, int64_t o, int64_t v
                     "orbital energies non-finite or degenerate across the gap (zero Jacobi denominator)");
 }
 
+// max|a - ref| / max|ref| over n device doubles
+double rel_change(gbcc_handle* h, int64_t n, const double* a, const double* ref) {
+  auto* out = reinterpret_cast<unsigned long long*>(h->d_out + 8);
+  GBCC_CK(cudaMemsetAsync(out, 0, 2 * sizeof(double), h->stream));
+  gbcc::launch_maxabs_diff(n, a, ref, out, h->stream);
+  GBCC_CK(cudaMemcpyAsync(h->h_out + 8, h->d_out + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  sync_check(h);
+  const double md = h->h_out[8], mb = h->h_out[9];
+  if (mb == 0.0) return md == 0.0 ? 0.0 : std::numeric_limits<double>::infinity();
+  return md / mb;
+}
+
+void plan_residual(gbcc_handle* h) {
+  drop_graphs(h);
+  h->eng->reset_plans();
+  h->prepacked = false;
+  h->eng->set_slices(h->slices_used[0], h->slices_used[1], h->slices_used[2]);
+  h->eng->set_frozen({h->S.t1, h->S.t2, h->S.tau});
+  h->eng->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
+  gbcc::residual_program(*h->eng, h->S);
+  h->eng->end();
+  const bool mixed = h->cfg.precision == GBCC_PREC_MIXED;
+  h->eng->finalize(mixed);
+  h->prepacked = mixed;
+}
+
+// Slice counts for the classes configured as 0 (automatic), chosen from their
+// measured error.  The residual at the calibration amplitudes with every
+// automatic class at 3 slices is the reference; each automatic class in turn
+// is evaluated with 2, then 1 slices (the other classes at 3) and keeps the
+// smallest count whose max|dr| / max|r|, over r1 and r2, is at most
+// slice_tolerance.  The amplitudes are the caller's (t1_in, t2_in: host or
+// device) or, when those are NULL, probe amplitudes: two Jacobi steps from
+// t = 0 (MP2 amplitudes, then one residual further, so t1 is nonzero).
+// The residual plan is rebuilt for the chosen counts; t1 = t2 = tau = 0 after.
+void calibrate_slices(gbcc_handle* h, const double* t1_in, const double* t2_in) {
+  gbcc::CcsdTensors& S = h->S;
+  const int req[3] = {h->cfg.slices_ladder, h->cfg.slices_ring, h->cfg.slices_other};
+  const int64_t o = h->cfg.o, v = h->cfg.v, n1 = n1_of(h), n2 = n2_of(h);
+  cudaStream_t st = h->stream;
+  for (int k = 0; k < 3; ++k) {
+    h->slices_used[k] = req[k] == 0 ? 3 : req[k];
+    h->slice_err[k] = -1.0;
+  }
+  plan_residual(h);
+  struct Guard {
+    gbcc_handle* h;
+    double* ref = nullptr;
+    ~Guard() {
+      h->calibrating = false;
+      h->eng->set_slice_limit(0, 0, 0);
+      gbcc::dev_free(ref);
+    }
+  } guard{h};
+  h->calibrating = true;
+  if (t1_in && t2_in) {
+    GBCC_CK(cudaMemcpyAsync(S.t1->d, t1_in, n1 * sizeof(double), cudaMemcpyDefault, st));
+    GBCC_CK(cudaMemcpyAsync(S.t2->d, t2_in, n2 * sizeof(double), cudaMemcpyDefault, st));
+  } else {
+    GBCC_CK(cudaMemsetAsync(S.t1->d, 0, n1 * sizeof(double), st));
+    GBCC_CK(cudaMemsetAsync(S.t2->d, 0, n2 * sizeof(double), st));
+    gbcc::launch_jacobi_inplace(o, v, S.eps_o->d, S.eps_v->d, S.f_ai->d, S.g_abij->d, S.t1->d, S.t2->d, st);
+    gbcc::launch_make_tau(o, v, S.t1->d, S.t2->d, S.tau->d, st);
+    enqueue_residual_program(h, GBCC_PREC_MIXED);
+    gbcc::launch_jacobi_inplace(o, v, S.eps_o->d, S.eps_v->d, S.r1->d, S.r2->d, S.t1->d, S.t2->d, st);
+  }
+  gbcc::launch_make_tau(o, v, S.t1->d, S.t2->d, S.tau->d, st);
+  enqueue_residual_program(h, GBCC_PREC_MIXED);
+  guard.ref = static_cast<double*>(gbcc::dev_alloc((n1 + n2) * sizeof(double)));
+  GBCC_CK(cudaMemcpyAsync(guard.ref, S.r1->d, n1 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  GBCC_CK(cudaMemcpyAsync(guard.ref + n1, S.r2->d, n2 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  for (int k = 0; k < 3; ++k) {
+    if (req[k] != 0) continue;
+    h->slice_err[k] = 0.0;
+    for (int s = 2; s >= 1; --s) {
+      int lim[3] = {0, 0, 0};
+      lim[k] = s;
+      h->eng->set_slice_limit(lim[0], lim[1], lim[2]);
+      enqueue_residual_program(h, GBCC_PREC_MIXED);
+      const double e = std::max(rel_change(h, n1, S.r1->d, guard.ref), rel_change(h, n2, S.r2->d, guard.ref + n1));
+      if (!(e <= h->cfg.slice_tolerance)) break;
+      h->slices_used[k] = s;
+      h->slice_err[k] = e;
+    }
+  }
+  h->eng->set_slice_limit(0, 0, 0);
+  GBCC_CK(cudaMemsetAsync(S.t1->d, 0, n1 * sizeof(double), st));
+  GBCC_CK(cudaMemsetAsync(S.t2->d, 0, n2 * sizeof(double), st));
+  GBCC_CK(cudaMemsetAsync(S.tau->d, 0, n2 * sizeof(double), st));
+  sync_check(h);
+  h->calibrating = false;
+  if (h->slices_used[0] != 3 || h->slices_used[1] != 3 || h->slices_used[2] != 3) plan_residual(h);
+  sync_check(h);
+}
+
 // Derived constants, the residual plan for both precisions and (mixed
 // handles) the split copies of the constant operands.
 void commit_inputs(gbcc_handle* h) {
@@ -186,16 +335,17 @@ void commit_inputs(gbcc_handle* h) {
   h->aux->begin(gbcc::Mode::kExec, GBCC_PREC_FP64);
   gbcc::setup_program(*h->aux, S);
   h->aux->end();
-  h->eng->reset_plans();
-  h->prepacked = false;
-  h->eng->set_frozen({S.t1, S.t2, S.tau});
-  h->eng->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
-  gbcc::residual_program(*h->eng, S);
-  h->eng->end();
-  const bool mixed = h->cfg.precision == GBCC_PREC_MIXED;
-  h->eng->finalize(mixed);
-  h->prepacked = mixed;
-  sync_check(h);
+  const int req[3] = {h->cfg.slices_ladder, h->cfg.slices_ring, h->cfg.slices_other};
+  if (h->cfg.precision == GBCC_PREC_MIXED && (req[0] == 0 || req[1] == 0 || req[2] == 0)) {
+    calibrate_slices(h, nullptr, nullptr);
+  } else {
+    for (int k = 0; k < 3; ++k) {
+      h->slices_used[k] = req[k] == 0 ? 3 : req[k];
+      h->slice_err[k] = -1.0;
+    }
+    plan_residual(h);
+    sync_check(h);
+  }
   h->inputs_set = true;
 }
 
@@ -226,11 +376,11 @@ void gbcc_config_default(gbcc_config* c) {
   if (!c) return;
   std::memset(c, 0, sizeof(*c));
   c->precision = GBCC_PREC_FP64;
-  c->slices_ladder = 3;
-  c->slices_ring = 3;
-  c->slices_other = 3;
+  c->slices_ladder = 0;
+  c->slices_ring = 0;
+  c->slices_other = 0;
   c->refine_iters = 2;
-  c->mixed_switch_precision = 1e-7;
+  c->mixed_switch_precision = 0.0;
   c->max_iter = 30;
   c->target_precision = 1e-9;
   c->diis_start = 1;
@@ -240,6 +390,8 @@ void gbcc_config_default(gbcc_config* c) {
   c->diis_group_nstart = 1;
   c->verbose = 0;
   c->device = 0;
+  c->use_graphs = 1;
+  c->slice_tolerance = 1e-5;
 }
 
 gbcc_status gbcc_create(gbcc_handle** out, const gbcc_config* cfg) {
@@ -413,6 +565,9 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
     int fp64_resid = 0, mixed_resid = 0;
     double t_mixed = 0.0, t_fp64 = 0.0;
     double E1 = 0.0, E0 = 0.0, dE = 0.0, error = 1.0;
+    double best_error = std::numeric_limits<double>::infinity();
+    double best_dE = std::numeric_limits<double>::infinity();
+    int stalled = 0;
     int iter = 0;
     bool converged = false;
     int diis_iter = 0, nvec = 0, head = -1;
@@ -430,8 +585,26 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
       if (c.verbose && iter > 0) print_iter(iter, dE, error, E1, secs);
       bool conv = iter > 0 && error <= c.target_precision && dE <= 0.1 * c.target_precision;
       if (mixed_phase) {
-        if (iter > 0 && error <= c.mixed_switch_precision && dE <= 0.1 * c.mixed_switch_precision)
-          mixed_phase = false;
+        // The split-precision phase ends once it has converged on its own residual
+        // (switch precision, default the target) or once it stops making progress:
+        // near its fixed point the split map has a rounding floor below which
+        // neither dE nor the error shrinks (DIIS otherwise sets a new minimum of
+        // both every iteration or two).  The FP64 iterations then absorb the
+        // split error.
+        const double sw = c.mixed_switch_precision > 0.0 ? c.mixed_switch_precision : c.target_precision;
+        if (iter > 0) {
+          bool progress = false;
+          if (error < 0.5 * best_error) {
+            best_error = error;
+            progress = true;
+          }
+          if (dE < 0.5 * best_dE) {
+            best_dE = dE;
+            progress = true;
+          }
+          stalled = progress ? 0 : stalled + 1;
+          if ((error <= sw && dE <= 0.1 * sw) || stalled >= 4) mixed_phase = false;
+        }
         conv = false;
       } else if (used_mixed && fp64_resid < c.refine_iters) {
         conv = false;
@@ -478,13 +651,7 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
       // residual of the new amplitudes
       const int prec = mixed_phase ? GBCC_PREC_MIXED : GBCC_PREC_FP64;
       GBCC_CK(cudaEventRecord(h->ev0, h->stream));
-      if (prec == GBCC_PREC_MIXED && !h->prepacked) {
-        h->eng->finalize(true);
-        h->prepacked = true;
-      }
-      h->eng->begin(gbcc::Mode::kExec, prec);
-      gbcc::residual_program(*h->eng, S);
-      h->eng->end();
+      h->last_launches = enqueue_residual_program(h, prec);
       GBCC_CK(cudaEventRecord(h->ev1, h->stream));
       sync_check(h);
       float ms = 0.f;
@@ -523,6 +690,7 @@ gbcc_status gbcc_destroy(gbcc_handle* h) {
   if (!h) return GBCC_OK;
   cudaSetDevice(h->cfg.device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
   h->eng.reset();
   h->aux.reset();
   for (void* p : {(void*)h->x1, (void*)h->x2, (void*)h->e1, (void*)h->e2, (void*)h->Bmat, (void*)h->coef,
@@ -535,6 +703,28 @@ gbcc_status gbcc_destroy(gbcc_handle* h) {
     if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+  return GBCC_OK;
+}
+
+gbcc_status gbcc_calibrate_slices(gbcc_handle* h, const double* t1_ai, const double* t2_abij) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "gbcc_calibrate_slices: inputs not set");
+    if (h->cfg.precision != GBCC_PREC_MIXED) throw Error(GBCC_ERR_STATE, "gbcc_calibrate_slices: not a mixed-precision handle");
+    if (!t1_ai || !t2_abij) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_calibrate_slices: NULL amplitudes");
+    h->inputs_set = false;
+    calibrate_slices(h, t1_ai, t2_abij);
+    h->inputs_set = true;
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_slice_policy(gbcc_handle* h, int32_t slices[3], double rel_change[3]) {
+  if (!h || !slices) return GBCC_ERR_INVALID_ARG;
+  if (!h->inputs_set) return fail(h, GBCC_ERR_STATE, "gbcc_slice_policy: inputs not set");
+  for (int k = 0; k < 3; ++k) {
+    slices[k] = h->slices_used[k];
+    if (rel_change) rel_change[k] = h->slice_err[k];
+  }
   return GBCC_OK;
 }
 
@@ -551,14 +741,17 @@ int gbcc_testing_profile_residual(gbcc_handle* h, int precision, int max_sites, 
     if (precision != GBCC_PREC_FP64 && precision != GBCC_PREC_MIXED)
       throw Error(GBCC_ERR_INVALID_ARG, "profile: bad precision");
     h->eng->set_profile(true);
+    h->profiling = true;
     try {
       run_residual(h, precision);
       sync_check(h);
     } catch (...) {
       h->eng->set_profile(false);
+      h->profiling = false;
       throw;
     }
     h->eng->set_profile(false);
+    h->profiling = false;
     const auto st = h->eng->site_stats(precision);
     h->prof_gemm_ms.clear();
     h->prof_dims.clear();

@@ -169,7 +169,7 @@ struct GemmPlan {
 };
 
 struct Site {
-  int kind = 0;  // 0 assign, 1 contract
+  int kind = 0;  // 0 assign, 1 contract, 2 custom kernels
   TermClass cls = kClassOther;
   GatherArgs gather{};
   GemmPlan plan[2];
@@ -413,6 +413,19 @@ bool storage_is_panel(const Ix& x, const std::string& ext) {
 
 }  // namespace
 
+void Engine::custom(const std::function<void(cudaStream_t)>& fn, int launches) {
+  Site& s = site();
+  if (mode_ == Mode::kExec) {
+    if (s.kind != 2) throw Error(GBCC_ERR_STATE, "engine: site kind mismatch");
+    prof_begin(s);
+    fn(stream_);
+    n_launch_ += launches;
+    prof_end(s);
+    return;
+  }
+  s.kind = 2;
+}
+
 void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<Lin>& A,
                       const std::vector<Lin>& B, TermClass cls) {
   Site& s = site();
@@ -448,10 +461,16 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       t.a_slices = p.slices;
       t.B = panel[1];
       t.b_slices = p.slices;
-      t.npairs = p.npairs;
+      // a slice limit below the packed count keeps the pairs p + q < limit: the
+      // split is sequential, so these are exactly the products of a
+      // limit-slice split (used to measure the error of fewer slices)
+      const int lim = slice_limit_[cls];
+      t.npairs = 0;
       for (int q = 0; q < p.npairs; ++q) {
-        t.pa[q] = p.pa[q];
-        t.pb[q] = p.pb[q];
+        if (lim > 0 && p.pa[q] + p.pb[q] >= lim) continue;
+        t.pa[t.npairs] = p.pa[q];
+        t.pb[t.npairs] = p.pb[q];
+        ++t.npairs;
       }
       t.C = p.C;
       t.cm = p.cm;
@@ -616,8 +635,12 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       GatherArgs& g = op.gather;
       std::memset(&g, 0, sizeof(g));
       g.nterms = static_cast<int>(op.terms.size());
+      // a single term packs as a plain copy; its coefficient scales alpha
+      const bool single = op.terms.size() == 1;
+      if (single) coef_direct *= op.terms[0].coef;
+      g.plain = single ? 1 : 0;
       for (size_t t = 0; t < op.terms.size(); ++t) {
-        g.t[t].coef = op.terms[t].coef;
+        g.t[t].coef = single ? 1.0 : op.terms[t].coef;
         g.t[t].a = op.terms[t].x.t->d;
         const std::vector<int64_t> hra = offsets(op.ext, e, op.terms[t].x), hca = offsets(op.kord, e, op.terms[t].x);
         if (t == 0) g.transpose = pick_transpose(hra, hca);
@@ -648,11 +671,13 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       p.cn = upload(hn).d;
     }
     if (!p.use_tc) {
-      // few 64 x 64 output tiles and a long K: split K over blocks
+      // fewer 64 x 64 output tiles than two per SM: split K over blocks (one SM
+      // runs FP64 at ~1/150 of the GPU's already low FP64 rate, so even a
+      // 1 MFLOP contraction is slow on a single block)
       const int64_t tiles = ((p.M + 63) / 64) * ((p.N + 63) / 64);
       const int64_t sms = num_sms();
-      if (tiles < 2 * sms && K >= 4096) {
-        int64_t ks = std::min<int64_t>((2 * sms + tiles - 1) / tiles, K / 1024);
+      if (tiles < 2 * sms && K >= 32) {
+        int64_t ks = std::min<int64_t>((2 * sms + tiles - 1) / tiles, K / 16);
         if (ks > 1) {
           int64_t kps = (K + ks - 1) / ks;
           kps = (kps + 15) / 16 * 16;
@@ -694,7 +719,9 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
           std::string sig;
           for (const auto& l : op.terms) {
             frozen = frozen && frozen_.count(l.x.t) > 0;
-            sig += l.x.t->name + "(" + l.x.lab + ")*" + std::to_string(l.coef) + ";";
+            // a single term is packed unscaled (plain copy)
+            const double coef = op.terms.size() == 1 ? 1.0 : l.coef;
+            sig += l.x.t->name + "(" + l.x.lab + ")*" + std::to_string(coef) + ";";
           }
           if (frozen) {
             op.sig = sig + op.ext + "|" + op.kord + "|" + std::to_string(slices) + "|" +

@@ -22,6 +22,7 @@
 
 #include <memory>
 #include <stdexcept>
+#include <functional>
 #include <string>
 #include <unordered_map>
 #include <unordered_set>
@@ -122,6 +123,13 @@ class Engine {
     slices_[2] = other;
   }
   void set_error_word(int* err) { err_ = err; }
+  // at EXEC, use only the slice products of a split with this many slices
+  // (0: all packed slices) for the contractions of each class
+  void set_slice_limit(int ladder, int ring, int other) {
+    slice_limit_[0] = ladder;
+    slice_limit_[1] = ring;
+    slice_limit_[2] = other;
+  }
   void set_chunk(int k) { chunk_ = k; }
   // Record CUDA events around every operation of EXEC passes.
   void set_profile(bool on) { profile_ = on; }
@@ -148,6 +156,9 @@ class Engine {
   // C = beta*C + alpha * sum_K (sum_s a_s A_s)(sum_t b_t B_t)
   void contract(const Ix& c, double beta, double alpha, const std::vector<Lin>& A,
                 const std::vector<Lin>& B, TermClass cls);
+  // a fixed kernel sequence of the program, enqueued in program order at EXEC;
+  // `launches` is the number of kernels it enqueues
+  void custom(const std::function<void(cudaStream_t)>& fn, int launches);
 
   // Statistics of the last EXEC pass (FLOPs of the contractions as planned).
   double flops() const { return flops_; }
@@ -167,6 +178,7 @@ class Engine {
   Mode mode_ = Mode::kPlan;
   int prec_ = GBCC_PREC_FP64;
   int slices_[3] = {3, 3, 3};
+  int slice_limit_[3] = {0, 0, 0};
   size_t cursor_ = 0;
   bool planned_ = false;
   std::vector<std::unique_ptr<Site>> sites_;

@@ -19,15 +19,85 @@ inline unsigned grid_for(int64_t n, int threads, int64_t cap = 152 * 32) {
   return static_cast<unsigned>(b);
 }
 
-// Split a value into nslices BF16 pieces x = s0 + s1 + ... (each the
-// round-to-nearest BF16 of what the previous slices left over).
+// BF16 bits of a finite float, rounded to nearest even (integer operations only)
+__device__ __forceinline__ unsigned bf16_rne(float f) {
+  const unsigned b = __float_as_uint(f);
+  return (b + 0x7FFFu + ((b >> 16) & 1u)) >> 16;
+}
+
+// Split of an FP64 value into nslices (<= 3) BF16 slices, x ~ s1 + s2 + s3.
+// The value is first taken apart without FP64 arithmetic (GB300 runs FP64
+// and its conversions at ~2 per clock per SM): hi = x truncated to 24
+// significant bits, exact, from the bit pattern; lo = the remaining 29
+// mantissa bits, one integer-to-float conversion (relative error 2^-24 of lo,
+// i.e. 2^-47 of x).  Each slice is then the remainder rounded to BF16 (nearest
+// even), remainders in FP32: s1 = bf16(hi), r = (hi - s1) + lo, s2 = bf16(r),
+// r -= s2, s3 = bf16(r); hi - s1 and r - s2 are exact, so
+// |x - s1 - s2 - s3| <= 2^-24 |x| (plus 2^-33 |x| from absorbing lo).
+// |x| >= 2^128 gives infinity, |x| < 2^-126 signed zeros, nan stays nan.
+// The numpy emulation in the tests follows these steps bit for bit.
+__device__ __forceinline__ void split_bits(double x, unsigned short* out, int nslices) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned sign = static_cast<unsigned>(u >> 63);
+  const int E = static_cast<int>((u >> 52) & 0x7FFull);
+  out[0] = out[1] = out[2] = 0;
+  const int e32 = E - 896;  // biased FP32 exponent of x
+  if (E == 0x7FF) {
+    out[0] = static_cast<unsigned short>((sign << 15) | ((u & 0xFFFFFFFFFFFFFull) ? 0x7FC0u : 0x7F80u));
+    return;
+  }
+  if (e32 >= 255) {
+    out[0] = static_cast<unsigned short>((sign << 15) | 0x7F80u);
+    return;
+  }
+  if (e32 <= 0) {  // zero, FP64 subnormals and magnitudes below FP32's normal range
+    out[0] = static_cast<unsigned short>(sign << 15);
+    return;
+  }
+  const float hi = __uint_as_float((sign << 31) | (static_cast<unsigned>(e32) << 23) |
+                                   (static_cast<unsigned>(u >> 29) & 0x7FFFFFu));
+  const unsigned lo_int = static_cast<unsigned>(u) & 0x1FFFFFFFu;  // value lo_int * 2^(E - 1075)
+  const int es = E - 948;                                           // biased FP32 exponent of 2^(E - 1075)
+  float lo = 0.f;
+  if (lo_int != 0u) {
+    // 2^(E - 1075) is below FP32's normal range for |x| < 2^-74: scale in two steps
+    lo = es >= 1 ? __uint2float_rn(lo_int) * __uint_as_float(static_cast<unsigned>(es) << 23)
+                 : (__uint2float_rn(lo_int) * 0x1p-64f) * __uint_as_float(static_cast<unsigned>(es + 64) << 23);
+    if (sign) lo = -lo;
+  }
+  const unsigned b1 = bf16_rne(hi);
+  out[0] = static_cast<unsigned short>(b1);
+  if (nslices < 2) return;
+  float r = __fadd_rn(__fsub_rn(hi, __uint_as_float(b1 << 16)), lo);
+  const unsigned b2 = bf16_rne(r);
+  out[1] = static_cast<unsigned short>(b2);
+  if (nslices < 3) return;
+  r = __fsub_rn(r, __uint_as_float(b2 << 16));
+  out[2] = static_cast<unsigned short>(bf16_rne(r));
+}
+
 __device__ __forceinline__ void split_store(double x, __nv_bfloat16* out, int nslices,
                                             int64_t slice_stride, int64_t idx) {
-  for (int s = 0; s < nslices; ++s) {
-    __nv_bfloat16 h = __double2bfloat16(x);
-    out[s * slice_stride + idx] = h;
-    x -= static_cast<double>(__bfloat162float(h));
+  unsigned short b[3];
+  split_bits(x, b, nslices);
+  for (int s = 0; s < nslices; ++s) out[s * slice_stride + idx] = __ushort_as_bfloat16(b[s]);
+}
+
+// value of one packed element: a single unscaled term is a plain load (its
+// coefficient was folded into the GEMM's alpha), otherwise an FP64 sum
+__device__ __forceinline__ double gather_value(const GatherArgs& g, int64_t r, int64_t c) {
+  if (g.plain) return g.t[0].a[g.t[0].ra[r] + g.t[0].ca[c]];
+  double val = 0.0;
+#pragma unroll
+  for (int t = 0; t < kMaxTerms; ++t) {
+    if (t < g.nterms) {
+      const GatherTerm& T = g.t[t];
+      double x = T.a[T.ra[r] + T.ca[c]];
+      if (T.b) x *= T.b[T.rb[r] + T.cb[c]];
+      val = fma(T.coef, x, val);
+    }
   }
+  return val;
 }
 
 __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs g) {
@@ -39,23 +109,57 @@ __global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs g) {
   for (int64_t r = r0; r < g.Rpad; r += rstep) {
     const bool rin = r < g.R;
     for (int64_t c = c0; c < g.Cpad; c += cstep) {
-      double val = 0.0;
-      if (rin && c < g.C) {
-#pragma unroll
-        for (int t = 0; t < kMaxTerms; ++t) {
-          if (t < g.nterms) {
-            const GatherTerm& T = g.t[t];
-            double x = T.a[T.ra[r] + T.ca[c]];
-            if (T.b) x *= T.b[T.rb[r] + T.cb[c]];
-            val = fma(T.coef, x, val);
-          }
-        }
-      }
+      const double val = (rin && c < g.C) ? gather_value(g, r, c) : 0.0;
       if (g.out) {
         double* p = g.out + r * g.ldo + c;
         *p = (g.beta == 0.0) ? val : fma(g.beta, *p, val);
       } else {
         split_store(val, g.outs, g.nslices, g.slice_stride, r * g.ldo + c);
+      }
+    }
+  }
+}
+
+// Plain single-term packs into BF16 slices (the common case), 4 consecutive
+// K elements per thread: the row offset is loaded once per row, the K offsets
+// as 16-byte vectors, and every slice gets one 8-byte store per thread.  The
+// launcher checks Cpad, ldo and slice_stride are multiples of 4 (K is padded
+// to 64) so the stores are 8-byte aligned.
+__global__ void __launch_bounds__(kThreads) gather_split4_kernel(GatherArgs g) {
+  const int64_t nq = g.Cpad / 4;
+  const int64_t q0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t qstep = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const int64_t r0 = static_cast<int64_t>(blockIdx.y) * blockDim.y + threadIdx.y;
+  const int64_t rstep = static_cast<int64_t>(gridDim.y) * blockDim.y;
+  const double* __restrict__ a = g.t[0].a;
+  const int64_t* __restrict__ ca = g.t[0].ca;
+  const int ns = g.nslices;
+  for (int64_t r = r0; r < g.Rpad; r += rstep) {
+    const bool rin = r < g.R;
+    const int64_t rb = rin ? g.t[0].ra[r] : 0;
+    unsigned short* orow = reinterpret_cast<unsigned short*>(g.outs) + r * g.ldo;
+    for (int64_t q = q0; q < nq; q += qstep) {
+      const int64_t c = 4 * q;
+      double x[4];
+      if (rin && c + 3 < g.C) {
+        const longlong2 o01 = *reinterpret_cast<const longlong2*>(ca + c);
+        const longlong2 o23 = *reinterpret_cast<const longlong2*>(ca + c + 2);
+        x[0] = a[rb + o01.x];
+        x[1] = a[rb + o01.y];
+        x[2] = a[rb + o23.x];
+        x[3] = a[rb + o23.y];
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) x[j] = (rin && c + j < g.C) ? a[rb + ca[c + j]] : 0.0;
+      }
+      unsigned short b[4][3];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) split_bits(x[j], b[j], ns);
+      for (int s = 0; s < ns; ++s) {
+        uint2 w;
+        w.x = static_cast<unsigned>(b[0][s]) | (static_cast<unsigned>(b[1][s]) << 16);
+        w.y = static_cast<unsigned>(b[2][s]) | (static_cast<unsigned>(b[3][s]) << 16);
+        *reinterpret_cast<uint2*>(orow + s * g.slice_stride + c) = w;
       }
     }
   }
@@ -74,19 +178,7 @@ __global__ void __launch_bounds__(256) gather_t_kernel(GatherArgs g) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int64_t r = r0 + tx, c = c0 + ty + 8 * k;
-      double val = 0.0;
-      if (r < g.R && c < g.C) {
-#pragma unroll
-        for (int q = 0; q < kMaxTerms; ++q) {
-          if (q < g.nterms) {
-            const GatherTerm& T = g.t[q];
-            double x = T.a[T.ra[r] + T.ca[c]];
-            if (T.b) x *= T.b[T.rb[r] + T.cb[c]];
-            val = fma(T.coef, x, val);
-          }
-        }
-      }
-      tile[ty + 8 * k][tx] = val;
+      tile[ty + 8 * k][tx] = (r < g.R && c < g.C) ? gather_value(g, r, c) : 0.0;
     }
     __syncthreads();
     // write: lanes along c
@@ -187,6 +279,158 @@ __global__ void __launch_bounds__(kThreads) make_tau_kernel(int64_t o, int64_t v
 }
 
 // ---------------------------------------------------------------------------
+// Particle-particle ladder over pair-(anti)symmetric combinations.
+//
+// B(a,b,i,j) = sum_cd G(a,b,c,d) tau(c,d,i,j) splits, with G+ = G_abcd + G_abdc
+// (G_abcc on the diagonal), G- = G_abcd - G_abdc, tau+ = (tau_cdij + tau_dcij)/2
+// (tau_ccij on the diagonal), tau- = (tau_cdij - tau_dcij)/2, into
+//   B = sum_{c<=d} G+ tau+ + sum_{c<d} G- tau-.
+// <ab|cd> = <ba|dc> makes G+ symmetric and G- antisymmetric under a<->b, and
+// pair-symmetric amplitudes (tau(c,d,i,j) = tau(d,c,j,i)) make tau+ symmetric,
+// tau- antisymmetric under i<->j, so the two products are needed for a <= b,
+// i <= j (a < b, i < j) only: a quarter of the FLOPs of the plain contraction.
+// Pair indices, row-major over the upper triangle:
+//   sym(a,b)  = a n - a(a-1)/2 + (b - a)      a <= b < n
+//   anti(a,b) = a (n-1) - a(a-1)/2 + (b-a-1)  a < b < n
+
+__device__ __forceinline__ int64_t pair_sym(int64_t a, int64_t b, int64_t n) {
+  return a * n - a * (a - 1) / 2 + (b - a);
+}
+__device__ __forceinline__ int64_t pair_anti(int64_t a, int64_t b, int64_t n) {
+  return a * (n - 1) - a * (a - 1) / 2 + (b - a - 1);
+}
+
+// One block per (a, b): Gp[sym(a,b)][sym(c,d)], Gm[anti(a,b)][anti(c,d)].  Also
+// used for o v^3 blocks (rows = any leading index pair, cols = c <= d) when
+// ab_pairs is false: then row r = a*v + b of G maps to row r of the outputs.
+__global__ void __launch_bounds__(kThreads) build_gpm_kernel(int64_t rows_v, int64_t v, bool ab_pairs,
+                                                             const double* __restrict__ G, double* __restrict__ Gp,
+                                                             double* __restrict__ Gm) {
+  const int64_t np = v * (v + 1) / 2, nm = v * (v - 1) / 2;
+  for (int64_t row = blockIdx.x; row < rows_v * v; row += gridDim.x) {
+    const int64_t a = row / v, b = row % v;
+    int64_t rp = row, rm = row;
+    if (ab_pairs) {
+      if (a > b) continue;
+      rp = pair_sym(a, b, v);
+      rm = a < b ? pair_anti(a, b, v) : -1;
+    }
+    const double* g = G + row * v * v;
+    double* gp = Gp + rp * np;
+    double* gm = rm >= 0 ? Gm + rm * nm : nullptr;
+    for (int64_t c = 0; c < v; ++c) {
+      for (int64_t d = c + threadIdx.x; d < v; d += blockDim.x) {
+        const double x = g[c * v + d], y = g[d * v + c];
+        gp[pair_sym(c, d, v)] = c < d ? x + y : x;
+        if (gm && c < d) gm[pair_anti(c, d, v)] = x - y;
+      }
+    }
+  }
+}
+
+// One block per (c <= d): taup[sym(c,d)][sym(i,j)], taum[anti(c,d)][anti(i,j)].
+__global__ void __launch_bounds__(kThreads) tau_pm_kernel(int64_t o, int64_t v, const double* __restrict__ tau,
+                                                          double* __restrict__ taup, double* __restrict__ taum) {
+  const int64_t o2 = o * o, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
+  for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
+    const int64_t c = p / v, d = p % v;
+    if (c > d) continue;
+    const double* x = tau + (c * v + d) * o2;
+    const double* y = tau + (d * v + c) * o2;
+    double* tp = taup + pair_sym(c, d, v) * sp;
+    double* tm = c < d ? taum + pair_anti(c, d, v) * sm : nullptr;
+    for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
+      const int64_t i = ij / o, j = ij % o;
+      if (i > j) continue;
+      if (c == d) {
+        tp[pair_sym(i, j, o)] = x[ij];
+      } else {
+        tp[pair_sym(i, j, o)] = 0.5 * (x[ij] + y[ij]);
+        if (i < j) tm[pair_anti(i, j, o)] = 0.5 * (x[ij] - y[ij]);
+      }
+    }
+  }
+}
+
+// out(a,b,i,j) (+)= Bp[sym(ab)][sym(ij)] + s_ab s_ij Bm[anti(ab)][anti(ij)], s = +1 for an
+// ordered pair, -1 for a swapped one, 0 on the diagonal.  With ab_pairs false the
+// row index r = a*v + b addresses Bp / Bm directly (no symmetry in the row pair).
+__global__ void __launch_bounds__(kThreads) pair_unpack_kernel(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs,
+                                                               const double* __restrict__ Bp,
+                                                               const double* __restrict__ Bm, double beta,
+                                                               double* __restrict__ out) {
+  const int64_t o2 = o * o, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
+  for (int64_t row = blockIdx.x; row < rows_v * v; row += gridDim.x) {
+    const int64_t a = row / v, b = row % v;
+    int64_t rp = row, rm = row;
+    double sab = 1.0;
+    if (ab_pairs) {
+      const int64_t lo = a < b ? a : b, hi = a < b ? b : a;
+      rp = pair_sym(lo, hi, v);
+      rm = lo < hi ? pair_anti(lo, hi, v) : -1;
+      sab = a < b ? 1.0 : -1.0;
+    }
+    const double* bp = Bp + rp * sp;
+    const double* bm = (Bm && rm >= 0) ? Bm + rm * sm : nullptr;
+    double* op = out + row * o2;
+    for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
+      const int64_t i = ij / o, j = ij % o;
+      const int64_t li = i < j ? i : j, hj = i < j ? j : i;
+      double val = bp[pair_sym(li, hj, o)];
+      if (bm && li < hj) val += (i < j ? sab : -sab) * bm[pair_anti(li, hj, o)];
+      op[ij] = beta == 0.0 ? val : op[ij] + val;
+    }
+  }
+}
+
+// t += r / D in place (the Jacobi step of lcao/cc/solvers.h:165-258 without
+// DIIS), used to build probe amplitudes for the slice calibration
+__global__ void __launch_bounds__(kThreads) jacobi_inplace_kernel(int64_t o, int64_t v, const double* eps_o,
+                                                                  const double* eps_v, const double* r1,
+                                                                  const double* r2, double* t1, double* t2) {
+  const int64_t o2 = o * o;
+  for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
+    const int64_t a = p / v, b = p % v;
+    const double eab = eps_v[a] + eps_v[b];
+    for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
+      const int64_t i = ij / o, j = ij % o;
+      t2[p * o2 + ij] += r2[p * o2 + ij] / (eps_o[i] + eps_o[j] - eab);
+    }
+  }
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < v * o;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    t1[e] += r1[e] / (eps_o[e % o] - eps_v[e / o]);
+}
+
+// out[0] = max |a - b|, out[1] = max |b| (out zeroed by the caller): block
+// maxima combined with atomicMax on the bit patterns, which order like the
+// values for non-negative doubles
+__global__ void __launch_bounds__(kThreads) maxabs_diff_kernel(int64_t n, const double* a, const double* b,
+                                                               unsigned long long* out) {
+  __shared__ double sd[kThreads], sb[kThreads];
+  double md = 0.0, mb = 0.0;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    md = fmax(md, fabs(a[e] - b[e]));
+    mb = fmax(mb, fabs(b[e]));
+  }
+  sd[threadIdx.x] = md;
+  sb[threadIdx.x] = mb;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sd[threadIdx.x] = fmax(sd[threadIdx.x], sd[threadIdx.x + w]);
+      sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(sd[0])));
+    atomicMax(out + 1, static_cast<unsigned long long>(__double_as_longlong(sb[0])));
+  }
+}
+
+// ---------------------------------------------------------------------------
 // DIIS
 
 constexpr int kDiisMax = 16;
@@ -240,18 +484,23 @@ __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) 
   }
 }
 
-// Gaussian elimination with partial pivoting; returns false on a pivot below
-// tol * max|A|.  Same operation order as the FP64 oracle's gepp_solve.
-__device__ bool gepp(double* A, double* b, double* x, int n) {
-  double scale = 0.0;
-  for (int i = 0; i < n * n; ++i) scale = fmax(scale, fabs(A[i]));
+// |det| of the normalised bordered DIIS matrix below which the oldest stored
+// vector is dropped (TiledArray's TA::DIIS test, threshold fixed by the water
+// 6-31G iteration trace MPQC records in its validation outputs).
+constexpr double kDiisDetMin = 1.0e-15;
+
+// Gaussian elimination with partial pivoting on a row-major n x n system;
+// returns |det A| (product of the pivots), 0 with x unset if a pivot is zero.
+__device__ double gepp(double* A, double* b, double* x, int n) {
+  double det = 1.0;
   for (int col = 0; col < n; ++col) {
     int p = col;
     double best = fabs(A[col * n + col]);
     for (int r = col + 1; r < n; ++r) {
       if (fabs(A[r * n + col]) > best) { best = fabs(A[r * n + col]); p = r; }
     }
-    if (best <= 1e-14 * scale) return false;
+    if (best == 0.0) return 0.0;
+    det *= best;
     if (p != col) {
       for (int c = 0; c < n; ++c) { double t = A[col * n + c]; A[col * n + c] = A[p * n + c]; A[p * n + c] = t; }
       double t = b[col]; b[col] = b[p]; b[p] = t;
@@ -267,7 +516,7 @@ __device__ bool gepp(double* A, double* b, double* x, int n) {
     for (int c = r + 1; c < n; ++c) s -= A[r * n + c] * x[c];
     x[r] = s / A[r * n + r];
   }
-  return true;
+  return det;
 }
 
 __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
@@ -293,16 +542,15 @@ __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
     *d.nskip_out = -1;
     return;
   }
-  const double b00 = d.Bmat[d.slots[0] * nd + d.slots[0]];
-  const double bnn = d.Bmat[d.slots[n - 1] * nd + d.slots[n - 1]];
-  double norm = 1.0;
-  if (fabs(b00) > 1e-10 && fabs(bnn) > 1e-10) norm = 1.0 / fabs(b00);
   double A[(kDiisMax + 1) * (kDiisMax + 1)];
   double rhs[kDiisMax + 1];
   double sol[kDiisMax + 1];
   for (int nskip = 0; nskip < n; ++nskip) {
     const int m = n - nskip;
     const int w = m + 1;
+    // normalise by the oldest kept vector's <e, e>
+    const double b0 = fabs(d.Bmat[d.slots[nskip] * nd + d.slots[nskip]]);
+    const double norm = b0 > 0.0 ? 1.0 / b0 : 1.0;
     for (int r = 0; r < w; ++r) {
       rhs[r] = (r == 0) ? -1.0 : 0.0;
       for (int c = 0; c < w; ++c) {
@@ -314,7 +562,8 @@ __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
         A[r * w + c] = val;
       }
     }
-    if (gepp(A, rhs, sol, w)) {
+    const double det = gepp(A, rhs, sol, w);
+    if (det > 0.0 && (det >= kDiisDetMin || nskip == n - 1)) {
       for (int q = 0; q < m; ++q) d.coef[d.slots[nskip + q]] = sol[q + 1];
       *d.nskip_out = nskip;
       return;
@@ -382,7 +631,22 @@ __global__ void __launch_bounds__(kThreads) splitk_reduce_kernel(int64_t M, int6
   }
 }
 
+__global__ void split_test_kernel(const double* x, int64_t n, int nslices, unsigned short* out) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    unsigned short b[3];
+    split_bits(x[i], b, nslices);
+    for (int s = 0; s < nslices; ++s) out[s * n + i] = b[s];
+  }
+}
+
 }  // namespace
+
+void launch_split_test(const double* x, int64_t n, int nslices, unsigned short* out, cudaStream_t st) {
+  if (n <= 0) return;
+  split_test_kernel<<<static_cast<unsigned>(std::min<int64_t>((n + 255) / 256, 4096)), 256, 0, st>>>(
+      x, n, nslices, out);
+}
 
 int num_sms() {
   static int sms = 0;
@@ -414,6 +678,17 @@ void launch_gather(const GatherArgs& g, cudaStream_t st) {
     gather_t_kernel<<<static_cast<unsigned>(grid), dim3(32, 8), 0, st>>>(g);
     return;
   }
+  if (g.outs && g.plain && g.Cpad % 4 == 0 && g.ldo % 4 == 0 && g.slice_stride % 4 == 0 &&
+      reinterpret_cast<uintptr_t>(g.outs) % 8 == 0 && reinterpret_cast<uintptr_t>(g.t[0].ca) % 16 == 0) {
+    const int64_t nq = g.Cpad / 4;
+    int bx = 32;
+    while (bx < nq && bx < kThreads) bx <<= 1;
+    const int by = kThreads / bx;
+    const int64_t gx = std::min<int64_t>((nq + bx - 1) / bx, 152LL * 64);
+    const int64_t gy = std::min<int64_t>({(g.Rpad + by - 1) / by, std::max<int64_t>(1, 152LL * 64 / gx), 65535LL});
+    gather_split4_kernel<<<dim3(static_cast<unsigned>(gx), static_cast<unsigned>(gy)), dim3(bx, by), 0, st>>>(g);
+    return;
+  }
   int bx = 1;
   while (bx < g.Cpad && bx < kThreads) bx <<= 1;
   if (bx < 32) bx = 32;
@@ -442,6 +717,30 @@ void launch_energy_terms(int64_t o, int64_t v, const double* r1, const double* r
 void launch_make_tau(int64_t o, int64_t v, const double* t1, const double* t2, double* tau,
                      cudaStream_t st) {
   make_tau_kernel<<<grid_for(v * v, 1), kThreads, 0, st>>>(o, v, t1, t2, tau);
+}
+
+void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G, double* Gp, double* Gm,
+                      cudaStream_t st) {
+  build_gpm_kernel<<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, ab_pairs, G, Gp, Gm);
+}
+
+void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double* taum, cudaStream_t st) {
+  tau_pm_kernel<<<grid_for(v * v, 1), kThreads, 0, st>>>(o, v, tau, taup, taum);
+}
+
+void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, const double* Bp, const double* Bm,
+                        double beta, double* out, cudaStream_t st) {
+  pair_unpack_kernel<<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, o, ab_pairs, Bp, Bm, beta, out);
+}
+
+void launch_jacobi_inplace(int64_t o, int64_t v, const double* eps_o, const double* eps_v, const double* r1,
+                           const double* r2, double* t1, double* t2, cudaStream_t st) {
+  jacobi_inplace_kernel<<<grid_for(v * v, 1), kThreads, 0, st>>>(o, v, eps_o, eps_v, r1, r2, t1, t2);
+}
+
+void launch_maxabs_diff(int64_t n, const double* a, const double* b, unsigned long long* out, cudaStream_t st) {
+  if (n <= 0) return;
+  maxabs_diff_kernel<<<grid_for(n, kThreads, 1216), kThreads, 0, st>>>(n, a, b, out);
 }
 
 void launch_diis_step(const DiisArgs& d, cudaStream_t st) {

@@ -48,9 +48,14 @@ struct GatherArgs {
   // 1: the sources are contiguous along R, not C -- read 32 x 32 tiles along R
   // and transpose them through shared memory (set by the planner)
   int transpose;
+  // 1: one term, no second factor, coefficient 1 -- a plain load (set by the planner)
+  int plain;
 };
 
 void launch_gather(const GatherArgs& args, cudaStream_t st);
+
+// FP64 -> nslices BF16 bit patterns (out[s*n + i]) with the packing kernels' split
+void launch_split_test(const double* x, int64_t n, int nslices, unsigned short* out, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // FP64 GEMM with scattered epilogue:
@@ -131,6 +136,22 @@ void launch_energy_terms(int64_t o, int64_t v, const double* r1, const double* r
                          const double* tau, double* partial, double* out, cudaStream_t st);
 
 // tau(a,b,i,j) = t2(a,b,i,j) + t1(a,i) t1(b,j)
+// Pair-(anti)symmetric ladder (see kernels.cu): G+/G- over (a <= b or any row
+// pair) x (c <= d) from G[rows_v][v][v][v]; tau+/tau- over (c <= d) x (i <= j);
+// out(row, i, j) = beta out + B+ +- B- unpacked from the pair products.
+void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G, double* Gp, double* Gm,
+                      cudaStream_t st);
+void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double* taum, cudaStream_t st);
+void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, const double* Bp, const double* Bm,
+                        double beta, double* out, cudaStream_t st);
+
+// t1 += r1 / D1, t2 += r2 / D2 in place
+void launch_jacobi_inplace(int64_t o, int64_t v, const double* eps_o, const double* eps_v, const double* r1,
+                           const double* r2, double* t1, double* t2, cudaStream_t st);
+
+// out[0] = bits of max|a - b|, out[1] = bits of max|b|; out must be zeroed first
+void launch_maxabs_diff(int64_t n, const double* a, const double* b, unsigned long long* out, cudaStream_t st);
+
 void launch_make_tau(int64_t o, int64_t v, const double* t1, const double* t2, double* tau,
                      cudaStream_t st);
 

@@ -145,6 +145,25 @@ extern "C" int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const doubl
   return status;
 }
 
+extern "C" int gbcc_testing_split(const double* x, int64_t n, int nslices, uint16_t* out) {
+  using namespace gbcc;
+  if (!x || !out || n < 0 || nslices < 1 || nslices > 3) return GBCC_ERR_INVALID_ARG;
+  if (n == 0) return GBCC_OK;
+  try {
+    double* dx = static_cast<double*>(dev_alloc(n * sizeof(double)));
+    unsigned short* dout = static_cast<unsigned short*>(dev_alloc(n * nslices * sizeof(unsigned short)));
+    GBCC_CK(cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice));
+    launch_split_test(dx, n, nslices, dout, nullptr);
+    GBCC_CK(cudaGetLastError());
+    GBCC_CK(cudaMemcpy(out, dout, n * nslices * sizeof(unsigned short), cudaMemcpyDeviceToHost));
+    dev_free(dx);
+    dev_free(dout);
+    return GBCC_OK;
+  } catch (const Error& e) {
+    return e.status;
+  }
+}
+
 extern "C" int gbcc_testing_fp64_peak(double* gflops) {
   using namespace gbcc;
   if (!gflops) return GBCC_ERR_INVALID_ARG;

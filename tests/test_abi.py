@@ -31,7 +31,7 @@ def test_header_and_binding_agree():
 def test_library_exports_every_declared_symbol(lib):
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.gbcc_abi_version() == 1
+    assert lib.gbcc_abi_version() == 2
 
 
 def test_defaults_follow_the_reference(lib):
@@ -41,11 +41,13 @@ def test_defaults_follow_the_reference(lib):
     # ccsd.h:104 max_iter 30; cc/solvers.h:93-95 DIIS; energy.h:45 precision 1e-9
     assert c.max_iter == 30 and c.n_diis == 8 and c.diis_start == 1
     assert c.diis_damp == 0.0 and c.diis_ngroup == 1 and c.diis_group_nstart == 1
-    assert c.target_precision == 1e-9 and c.precision == 0
+    assert c.target_precision == 1e-9 and c.precision == 0 and c.use_graphs == 1
+    assert (c.slices_ladder, c.slices_ring, c.slices_other) == (0, 0, 0) and c.slice_tolerance == 1e-5
+    assert c.mixed_switch_precision == 0.0
 
 
 @pytest.mark.parametrize("field,value", [("o", 0), ("v", -1), ("n_diis", 0), ("n_diis", 17),
-                                         ("slices_ladder", 4), ("precision", 7), ("max_iter", 0),
+                                         ("slices_ladder", 4), ("slices_ring", -1), ("slice_tolerance", 0.0), ("precision", 7), ("max_iter", 0),
                                          ("target_precision", 0.0), ("diis_damp", -1.0)])
 def test_create_rejects_bad_config(lib, field, value):
     from mpqc_gb300._lib import Config, GBCC_ERR_INVALID_ARG

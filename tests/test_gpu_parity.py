@@ -137,3 +137,65 @@ def test_max_iter_reports_not_converged():
     with _solver(inp, max_iter=2) as s:
         e, t1, t2, rep = s.solve()
     assert not rep.converged and rep.iters == 2 and np.isfinite(e)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_replay_matches_direct_launches(precision):
+    """The captured residual graph reads the amplitudes of each call: replaying it
+    on new t1/t2 gives bitwise the results of direct launches."""
+    inp = synth.make_inputs(6, 30, 20, seed=41, t1_scale=1e-2)
+    t1b, t2b = inp.t1 * 0.5, inp.t2 * 1.3
+    with _solver(inp, precision=precision) as g, _solver(inp, precision=precision, use_graphs=False) as d:
+        ga, gb, gc = g.residual(inp.t1, inp.t2), g.residual(t1b, t2b), g.residual(inp.t1, inp.t2)
+        da, db = d.residual(inp.t1, inp.t2), d.residual(t1b, t2b)
+    for x, y in ((ga, da), (gb, db), (gc, da)):
+        assert np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1])
+    assert not np.array_equal(ga[1], gb[1])
+
+
+def test_graph_solve_matches_direct_solve():
+    inp = synth.make_inputs(5, 24, 20, seed=43, b_scale=0.03)
+    with _solver(inp, precision="mixed", target_precision=1e-10, max_iter=60) as g:
+        eg, t1g, t2g, rg = g.solve()
+    with _solver(inp, precision="mixed", target_precision=1e-10, max_iter=60, use_graphs=False) as d:
+        ed, t1d, t2d, rd = d.solve()
+    assert rg.iters == rd.iters and eg == ed and np.array_equal(t2g, t2d)
+
+
+def test_automatic_slices_follow_measured_error():
+    """Slice counts 0 are chosen at set_inputs from the measured residual change
+    against 3 slices; the residual stays within the tolerance of the 3-slice one."""
+    inp = synth.make_inputs(8, 40, 30, seed=51, t1_scale=1e-2, b_scale=0.03)
+    r1_ref, r2_ref = R.residual(inp.t1, inp.t2, oracle_ints(inp))
+    with _solver(inp, precision="mixed", slices=(0, 0, 0)) as s:
+        sl, err = s.slice_policy()
+        r1, r2 = s.residual(inp.t1, inp.t2)
+    with _solver(inp, precision="mixed", slices=(3, 3, 3)) as s3:
+        q1, q2 = s3.residual(inp.t1, inp.t2)
+        assert s3.slice_policy() == ((3, 3, 3), (None, None, None))
+    assert all(x in (1, 2, 3) for x in sl) and min(sl) < 3
+    assert all(e is not None and 0.0 <= e <= 1e-5 for e in err)
+    # the probe measures at other amplitudes: allow a margin over the tolerance
+    assert rel_err(r2, q2) < 1e-4 and rel_err(r1, q1) < 1e-4
+    assert rel_err(r2, r2_ref) < 1e-4
+    with _solver(inp, precision="mixed", slices=(0, 0, 0), slice_tolerance=1e-14) as s:
+        assert s.slice_policy()[0] == (3, 3, 3)
+    # measured at the amplitudes of the evaluation itself: each class within the
+    # tolerance of 3 slices, so the residual within the sum of the three
+    with _solver(inp, precision="mixed", slices=(0, 0, 0)) as s:
+        sl2, err2 = s.calibrate_slices(inp.t1, inp.t2)
+        c1, c2 = s.residual(inp.t1, inp.t2)
+    assert all(e is not None and 0.0 <= e <= 1e-5 for e in err2)
+    assert rel_err(c2, q2) <= 3e-5 and rel_err(c1, q1) <= 3e-5
+    with _solver(inp, precision="mixed", slices=(3, 0, 1)) as s:
+        sl, err = s.slice_policy()
+        assert sl[0] == 3 and sl[2] == 1 and err[0] is None and err[2] is None and err[1] is not None
+
+
+def test_mixed_solve_with_automatic_slices():
+    inp = synth.make_inputs(8, 40, 40, seed=31, b_scale=0.02)
+    ref = R.solve_ccsd(oracle_ints(inp), inp.eps_o, inp.eps_v, target_precision=1e-10, max_iter=60)
+    with _solver(inp, precision="mixed", slices=(0, 0, 0), target_precision=1e-10, max_iter=60) as s:
+        e, t1, t2, rep = s.solve()
+    assert rep.converged and rep.fp64_iters >= 2
+    assert abs(e - ref.e_corr) < 1e-6 and np.max(np.abs(t2 - ref.t2)) < 1e-6
