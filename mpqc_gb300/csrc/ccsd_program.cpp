@@ -53,12 +53,29 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v) {
   tmp = &E.tensor("tmp", {v, v, o, o});
   W = &E.tensor("W", {o, o, o, o});
   tmp2 = &E.tensor("tmp2", {o, v, o, o});
+  const int64_t np = v * (v + 1) / 2, nm = v * (v - 1) / 2, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
+  Gp = &E.tensor("Gp", {np, np}, true);
+  Gm = &E.tensor("Gm", {nm, nm}, true);
+  Gip = &E.tensor("Gip", {o * v, np}, true);
+  Gim = &E.tensor("Gim", {o * v, nm}, true);
+  taup = &E.tensor("taup", {np, sp});
+  taum = &E.tensor("taum", {nm, sm});
+  Bp = &E.tensor("Bp", {np, sp});
+  Bm = &E.tensor("Bm", {nm, sm});
+  Xp = &E.tensor("Xp", {o * v, sp});
+  Xm = &E.tensor("Xm", {o * v, sm});
 }
 
-// f_ai(a,i) = Fia(i,a), g_abij(a,b,i,j) = Gijab(i,j,a,b)  (ccsd.h:325-330)
+// f_ai(a,i) = Fia(i,a), g_abij(a,b,i,j) = Gijab(i,j,a,b)  (ccsd.h:325-330);
+// G+/G- of Gabcd and Giabc for the pair-symmetric ladder (kernels.cu)
 void setup_program(Engine& E, const CcsdTensors& S) {
   E.assign(ix(*S.f_ai, "ai"), 0.0, {f1(1.0, ix(*S.Fia, "ia"))});
   E.assign(ix(*S.g_abij, "abij"), 0.0, {f1(1.0, ix(*S.Gijab, "ijab"))});
+  const int64_t v = S.t1->dim[0], o = S.t1->dim[1];
+  const double *Gabcd = S.Gabcd->d, *Giabc = S.Giabc->d;
+  double *Gp = S.Gp->d, *Gm = S.Gm->d, *Gip = S.Gip->d, *Gim = S.Gim->d;
+  E.custom([=](cudaStream_t st) { launch_build_gpm(v, v, true, Gabcd, Gp, Gm, st); }, 1);
+  E.custom([=](cudaStream_t st) { launch_build_gpm(o, v, false, Giabc, Gip, Gim, st); }, 1);
 }
 
 void residual_program(Engine& E, const CcsdTensors& S) {
@@ -153,9 +170,24 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijka, "lkjc")}}, {{1.0, ix(t1, "ci")}}, O);
   E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijab, "klcd")}}, {{1.0, ix(tau, "cdij")}}, O);
   E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(W, "klij")}}, {{1.0, ix(tau, "abkl")}}, O);
-  // particle-particle ladder (:272-280)
-  E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(tau, "cdij")}}, {{1.0, ix(Gabcd, "abcd")}}, L);
-  E.contract(ix(*S.tmp2, "kaij"), 0.0, 1.0, {{1.0, ix(Giabc, "kacd")}}, {{1.0, ix(tau, "cdij")}}, R);
+  // particle-particle ladder (:272-280): r2 += tau(c,d,i,j) Gabcd(a,b,c,d) and
+  // tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j), both as sums over c <= d of the
+  // pair-(anti)symmetric combinations (kernels.cu), unpacked into r2 / tmp2
+  {
+    const int64_t v = t1.dim[0], o = t1.dim[1];
+    const bool minus = v > 1 && o > 1;  // otherwise the antisymmetric parts are empty
+    const double* tau_d = tau.d;
+    double *taup = S.taup->d, *taum = S.taum->d, *Bp = S.Bp->d, *Bm = S.Bm->d, *Xp = S.Xp->d, *Xm = S.Xm->d;
+    double *r2d = r2.d, *tmp2 = S.tmp2->d;
+    E.custom([=](cudaStream_t st) { launch_tau_pm(o, v, tau_d, taup, taum, st); }, 1);
+    E.contract(ix(*S.Bp, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
+    if (minus) E.contract(ix(*S.Bm, "XZ"), 0.0, 1.0, {{1.0, ix(*S.Gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);
+    E.custom([=](cudaStream_t st) { launch_pair_unpack(v, v, o, true, Bp, minus ? Bm : nullptr, 1.0, r2d, st); }, 1);
+    E.contract(ix(*S.Xp, "RS"), 0.0, 1.0, {{1.0, ix(*S.Gip, "RQ")}}, {{1.0, ix(*S.taup, "QS")}}, R);
+    if (minus) E.contract(ix(*S.Xm, "RZ"), 0.0, 1.0, {{1.0, ix(*S.Gim, "RY")}}, {{1.0, ix(*S.taum, "YZ")}}, R);
+    E.custom([=](cudaStream_t st) { launch_pair_unpack(o, v, o, false, Xp, minus ? Xm : nullptr, 0.0, tmp2, st); },
+             1);
+  }
   E.contract(ix(r2, "abij"), 1.0, -1.0, {{1.0, ix(*S.tmp2, "kaji")}}, {{1.0, ix(t1, "bk")}}, O);
   E.contract(ix(r2, "abij"), 1.0, -1.0, {{1.0, ix(*S.tmp2, "kbij")}}, {{1.0, ix(t1, "ak")}}, O);
 }

@@ -1,7 +1,11 @@
 // Elementwise, gather/pack, reduction and DIIS kernels of the CCSD engine.
 //
-// Everything here is FP64 and HBM-bound: the amplitude-sized arrays
-// (o^2 v^2 doubles) are streamed once per kernel with coalesced accesses.
+// The amplitude-sized arrays (o^2 v^2 doubles) are streamed once per kernel
+// with coalesced accesses, so HBM bandwidth is the bound these kernels aim at.
+// GB300 executes FP64 arithmetic and FP64 conversions at ~2 per clock per SM
+// (1/64 of FP32), so per-element FP64 work is kept to a few operations: the
+// BF16 split works on bit patterns and FP32 remainders, and single-term packs
+// are plain copies (their coefficient scales the GEMM instead).
 #include "kernels.h"
 
 #include <algorithm>
