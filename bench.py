@@ -291,7 +291,9 @@ def ours(args):
         if rank == 0:
             print(json.dumps({"residual_only": True, "o": o, "v": v, "naux": naux,
                               "tc_launches_per_residual": len(tc), "ladder_tc_ordinal": ordinal,
-                              "launches_per_residual": launches}), flush=True)
+                              "launches_per_residual": launches,
+                              "tc_sites_mnk_class": [[p["M"], p["N"], p["K"], p["cls"]] for p in tc]}),
+                  flush=True)
         return 0
 
     # ---- mixed precision, device-resident inputs

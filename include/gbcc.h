@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define GBCC_ABI_VERSION 2
+#define GBCC_ABI_VERSION 3
 
 typedef enum gbcc_status {
   GBCC_OK = 0,
@@ -82,6 +82,8 @@ typedef struct gbcc_config {
                                /* captured on first use per precision; 0: direct launches     */
   double slice_tolerance;      /* automatic slices: largest max|dr|/max|r| (r1 and r2) a class */
                                /* may add against 3 slices at the probe amplitudes; 1e-5     */
+  int32_t autotune;            /* 1 (default): mixed handles time each tensor-core contraction's */
+                               /* candidate tile widths and K splits once and keep the fastest */
 } gbcc_config;
 
 typedef struct gbcc_inputs {

@@ -23,7 +23,7 @@ int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const do
 
 /* As gbcc_testing_gemm with the tensor-core kernel's knobs exposed: the K
  * dimension split over `ksplit` groups of CTAs (partial tiles reduced in a
- * fixed order by a second kernel), the N tile `bn` (0: automatic; 256 sums
+ * fixed order by a second kernel), the N tile `bn` (0: automatic; 192 and 256 sum
  * chunks in FP32 registers), CTA pairs (`cta2`, tcgen05 cta_group::2), the
  * k-blocks per TMEM accumulation (`chunk`, 0: default) and the chunks per
  * float-float fold (`fold`, 0: default).  slices == 0 runs the FP64 kernel. */
@@ -62,6 +62,11 @@ int gbcc_testing_elapsed(struct gbcc_handle* h, int slot0, int slot1, float* ms)
  * (0 for elementwise operations); same indexing as
  * gbcc_testing_profile_residual. */
 int gbcc_testing_profile_gemm_ms(struct gbcc_handle* h, int max_sites, double* ms);
+
+/* Per operation of the last profiled residual: N tile width of a tensor-core
+ * contraction (-1: the short-K CUDA-core kernel, 0: FP64 / elementwise) and
+ * its K split, as pairs tiles[2 i], tiles[2 i + 1]. */
+int gbcc_testing_profile_tiles(gbcc_handle* h, int max_sites, int32_t* tiles);
 
 /* GEMM shape (M, N, K) of each operation of the last profiled residual,
  * three int64 per operation (elementwise operations: rows, columns, 0). */

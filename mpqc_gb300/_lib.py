@@ -30,7 +30,8 @@ EXPORTS = (
 # test hooks of include/gbcc_testing.h
 TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_split", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
-                   "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims")
+                   "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims",
+                   "gbcc_testing_profile_tiles")
 
 
 class Config(C.Structure):
@@ -43,7 +44,7 @@ class Config(C.Structure):
         ("diis_start", C.c_int32), ("n_diis", C.c_int32), ("diis_damp", C.c_double),
         ("diis_ngroup", C.c_int32), ("diis_group_nstart", C.c_int32),
         ("verbose", C.c_int32), ("device", C.c_int32), ("use_graphs", C.c_int32),
-        ("slice_tolerance", C.c_double),
+        ("slice_tolerance", C.c_double), ("autotune", C.c_int32),
     ]
 
 
@@ -112,6 +113,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_testing_profile_gemm_ms.argtypes = [vp, C.c_int, dp]
     lib.gbcc_testing_profile_dims.restype = C.c_int
     lib.gbcc_testing_profile_dims.argtypes = [vp, C.c_int, C.POINTER(C.c_int64)]
+    lib.gbcc_testing_profile_tiles.restype = C.c_int
+    lib.gbcc_testing_profile_tiles.argtypes = [vp, C.c_int, C.POINTER(C.c_int32)]
     lib.gbcc_residual.restype = C.c_int
     lib.gbcc_residual.argtypes = [vp, vp, vp, vp, vp]
     lib.gbcc_residual_ex.restype = C.c_int

@@ -76,7 +76,7 @@ class Solver:
     def __init__(self, o, v, precision="fp64", slices=(0, 0, 0), refine_iters=2,
                  mixed_switch_precision=0.0, max_iter=30, target_precision=1e-9,
                  diis_start=1, n_diis=8, diis_damp=0.0, diis_ngroup=1, diis_group_nstart=1,
-                 verbose=False, device=0, use_graphs=True, slice_tolerance=1e-5):
+                 verbose=False, device=0, use_graphs=True, slice_tolerance=1e-5, autotune=True):
         self.lib = L.load()
         cfg = L.Config()
         self.lib.gbcc_config_default(C.byref(cfg))
@@ -94,6 +94,7 @@ class Solver:
         cfg.device = int(device)
         cfg.use_graphs = int(bool(use_graphs))
         cfg.slice_tolerance = float(slice_tolerance)
+        cfg.autotune = int(bool(autotune))
         self.cfg = cfg
         self.o, self.v = int(o), int(v)
         h = C.c_void_p()
@@ -155,8 +156,10 @@ class Solver:
         self.lib.gbcc_testing_profile_gemm_ms(self.h, max_sites, gm)
         mnk = (C.c_int64 * (3 * max_sites))()
         self.lib.gbcc_testing_profile_dims(self.h, max_sites, mnk)
+        tl = (C.c_int32 * (2 * max_sites))()
+        self.lib.gbcc_testing_profile_tiles(self.h, max_sites, tl)
         return [dict(ms=ms[i], gemm_ms=gm[i], flops=fl[i], pairs=pr[i], cls=cl[i],
-                     M=mnk[3 * i], N=mnk[3 * i + 1], K=mnk[3 * i + 2])
+                     M=mnk[3 * i], N=mnk[3 * i + 1], K=mnk[3 * i + 2], bn=tl[2 * i], ksplit=tl[2 * i + 1])
                 for i in range(min(n.value, max_sites))]
 
     def record(self, slot):

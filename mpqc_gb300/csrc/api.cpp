@@ -47,6 +47,7 @@ struct gbcc_handle {
   cudaEvent_t slots[8] = {};
   std::vector<double> prof_gemm_ms;
   std::vector<std::array<int64_t, 3>> prof_dims;
+  std::vector<std::array<int32_t, 2>> prof_tiles;
   // residual program captured as a CUDA graph, one per precision (FP64, mixed)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_launches[2] = {0, 0};
@@ -240,6 +241,14 @@ double rel_change(gbcc_handle* h, int64_t n, const double* a, const double* ref)
   return md / mb;
 }
 
+// Tile widths and K splits of the mixed plan from timing (config autotune)
+void tune_plan(gbcc_handle* h) {
+  if (h->cfg.precision != GBCC_PREC_MIXED || !h->cfg.autotune) return;
+  drop_graphs(h);
+  h->eng->autotune(3);
+  sync_check(h);
+}
+
 void plan_residual(gbcc_handle* h) {
   drop_graphs(h);
   h->eng->reset_plans();
@@ -321,6 +330,7 @@ void calibrate_slices(gbcc_handle* h, const double* t1_in, const double* t2_in) 
   h->calibrating = false;
   if (h->slices_used[0] != 3 || h->slices_used[1] != 3 || h->slices_used[2] != 3) plan_residual(h);
   sync_check(h);
+  tune_plan(h);
 }
 
 // Derived constants, the residual plan for both precisions and (mixed
@@ -345,6 +355,7 @@ void commit_inputs(gbcc_handle* h) {
     }
     plan_residual(h);
     sync_check(h);
+    tune_plan(h);
   }
   h->inputs_set = true;
 }
@@ -392,6 +403,7 @@ void gbcc_config_default(gbcc_config* c) {
   c->device = 0;
   c->use_graphs = 1;
   c->slice_tolerance = 1e-5;
+  c->autotune = 1;
 }
 
 gbcc_status gbcc_create(gbcc_handle** out, const gbcc_config* cfg) {
@@ -755,9 +767,11 @@ int gbcc_testing_profile_residual(gbcc_handle* h, int precision, int max_sites, 
     const auto st = h->eng->site_stats(precision);
     h->prof_gemm_ms.clear();
     h->prof_dims.clear();
+    h->prof_tiles.clear();
     for (const auto& x : st) {
       h->prof_gemm_ms.push_back(x.gemm_ms);
       h->prof_dims.push_back({x.M, x.N, x.K});
+      h->prof_tiles.push_back({x.bn, x.ksplit});
     }
     if (nsites) *nsites = static_cast<int>(st.size());
     for (int i = 0; i < max_sites && i < static_cast<int>(st.size()); ++i) {
@@ -773,6 +787,15 @@ int gbcc_testing_profile_residual(gbcc_handle* h, int precision, int max_sites, 
 int gbcc_testing_profile_gemm_ms(gbcc_handle* h, int max_sites, double* ms) {
   if (!h || !ms) return GBCC_ERR_INVALID_ARG;
   for (int i = 0; i < max_sites && i < static_cast<int>(h->prof_gemm_ms.size()); ++i) ms[i] = h->prof_gemm_ms[i];
+  return GBCC_OK;
+}
+
+int gbcc_testing_profile_tiles(gbcc_handle* h, int max_sites, int32_t* tiles) {
+  if (!h || !tiles) return GBCC_ERR_INVALID_ARG;
+  for (int i = 0; i < max_sites && i < static_cast<int>(h->prof_tiles.size()); ++i) {
+    tiles[2 * i] = h->prof_tiles[i][0];
+    tiles[2 * i + 1] = h->prof_tiles[i][1];
+  }
   return GBCC_OK;
 }
 

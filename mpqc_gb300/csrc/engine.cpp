@@ -153,6 +153,7 @@ struct OperandPlan {
 
 struct GemmPlan {
   bool use_tc = false;
+  bool smallk = false;     // mixed precision, K <= kSmallK: FP32 CUDA-core kernel on FP64 panels
   bool a_is_first = true;  // GEMM M side is the call's A operand
   int64_t M = 0, N = 0, K = 0;
   OperandPlan P[2];        // [0] = M side, [1] = N side
@@ -166,6 +167,11 @@ struct GemmPlan {
   int64_t k_per_split = 0;  // FP64: K elements per split; tensor cores: k-blocks per split
   int pa[kMaxPairs] = {}, pb[kMaxPairs] = {};
   double flops = 0.0;
+  // tensor cores: (tile width, K split) candidates for the tuner, the plan's
+  // heuristic choice first
+  int ncand = 0;
+  int cand_bn[8] = {}, cand_ks[8] = {};
+  int64_t cand_kps[8] = {};
 };
 
 struct Site {
@@ -223,6 +229,8 @@ std::vector<SiteStat> Engine::site_stats(int precision) {
       st.M = p.M;
       st.N = p.N;
       st.K = p.K;
+      st.bn = p.use_tc ? p.bn : (p.smallk ? -1 : 0);
+      st.ksplit = p.ksplit;
     } else {
       st.M = sp->gather.R;
       st.N = sp->gather.C;
@@ -413,6 +421,124 @@ bool storage_is_panel(const Ix& x, const std::string& ext) {
 
 }  // namespace
 
+// The split panel of one operand of a tensor-core contraction: its constant
+// pack, the pack cache, or a fresh pack into the workspace.
+__nv_bfloat16* Engine::tc_panel(OperandPlan& op, int side) {
+  if (op.constant) {
+    if (!op.packed) throw Error(GBCC_ERR_STATE, "engine: constant operand not packed");
+    return op.packed;
+  }
+  if (op.cache_reuse) return op.cache_buf;
+  __nv_bfloat16* out = op.cache_first ? op.cache_buf : (side == 0 ? wbfa_ : wbfb_);
+  GatherArgs g = op.gather;
+  g.outs = out;
+  launch_gather(g, stream_);
+  ++n_launch_;
+  return out;
+}
+
+GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* const panel[2]) const {
+  GemmTcArgs t{};
+  t.M = p.M;
+  t.N = p.N;
+  t.Mpad = p.P[0].rows_pad;
+  t.Npad = round_up(p.N, p.bn);
+  t.a_rows = p.P[0].rows_pad;
+  t.b_rows = p.P[1].rows_pad;  // padded for every candidate tile width
+  t.Kpad = p.P[0].Kpad;
+  t.A = panel[0];
+  t.a_slices = p.slices;
+  t.B = panel[1];
+  t.b_slices = p.slices;
+  // a slice limit below the packed count keeps the pairs p + q < limit: the
+  // split is sequential, so these are exactly the products of a
+  // limit-slice split (used to measure the error of fewer slices)
+  const int lim = slice_limit_[cls];
+  t.npairs = 0;
+  for (int q = 0; q < p.npairs; ++q) {
+    if (lim > 0 && p.pa[q] + p.pb[q] >= lim) continue;
+    t.pa[t.npairs] = p.pa[q];
+    t.pb[t.npairs] = p.pb[q];
+    ++t.npairs;
+  }
+  t.C = p.C;
+  t.cm = p.cm;
+  t.cn = p.cn;
+  t.alpha = p.alpha;
+  t.beta = p.beta;
+  t.bn = p.bn;
+  t.chunk = chunk_;
+  t.err = err_;
+  t.ksplit = p.ksplit;
+  t.kb_per_split = static_cast<int>(p.k_per_split);
+  t.partial = wpart_;
+  t.m_major = p.m_major ? 1 : 0;
+  return t;
+}
+
+void Engine::launch_tc(const GemmPlan& p, const GemmTcArgs& t) {
+  if (!launch_gemm_tc(t, stream_)) throw Error(GBCC_ERR_CUDA, "tcgen05 GEMM launch rejected (tensor map or size)");
+  ++n_tc_;
+  ++n_launch_;
+  if (p.ksplit > 1) {
+    launch_splitk_reduce(p.M, p.N, p.ksplit, wpart_, t.Mpad, t.Npad, p.C, p.cm, p.cn, p.alpha, p.beta, stream_);
+    ++n_launch_;
+  }
+}
+
+// Tile width and K split of every tensor-core contraction chosen by timing
+// its candidates (plan-time lists) on its own operands: each candidate runs
+// once untimed and `reps` times between CUDA events, the fastest is kept.
+// The outputs of the timed launches are scratch (a residual recomputes them).
+void Engine::autotune(int reps) {
+  if (!planned_) throw Error(GBCC_ERR_STATE, "engine: autotune before PLAN");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  GBCC_CK(cudaEventCreate(&e0));
+  GBCC_CK(cudaEventCreate(&e1));
+  struct Ev {
+    cudaEvent_t a, b;
+    ~Ev() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } ev{e0, e1};
+  for (auto& sp : sites_) {
+    if (sp->kind != 1) continue;
+    GemmPlan& p = sp->plan[1];
+    if (!p.use_tc || p.ncand < 2) continue;
+    __nv_bfloat16* panel[2];
+    for (int side = 0; side < 2; ++side) panel[side] = tc_panel(p.P[side], side);
+    float best = 0.f;
+    int pick = -1;
+    for (int c = 0; c < p.ncand; ++c) {
+      GemmPlan q = p;
+      q.bn = p.cand_bn[c];
+      q.ksplit = p.cand_ks[c];
+      q.k_per_split = p.cand_kps[c];
+      const GemmTcArgs t = tc_args(q, sp->cls, panel);
+      if (!launch_gemm_tc(t, stream_)) continue;
+      if (q.ksplit > 1)
+        launch_splitk_reduce(q.M, q.N, q.ksplit, wpart_, t.Mpad, t.Npad, q.C, q.cm, q.cn, q.alpha, q.beta, stream_);
+      GBCC_CK(cudaEventRecord(e0, stream_));
+      for (int r = 0; r < reps; ++r) launch_tc(q, t);
+      GBCC_CK(cudaEventRecord(e1, stream_));
+      GBCC_CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      GBCC_CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (pick < 0 || ms < best) {
+        best = ms;
+        pick = c;
+      }
+    }
+    if (pick >= 0) {
+      p.bn = p.cand_bn[pick];
+      p.ksplit = p.cand_ks[pick];
+      p.k_per_split = p.cand_kps[pick];
+    }
+  }
+  GBCC_CK(cudaStreamSynchronize(stream_));
+}
+
 void Engine::custom(const std::function<void(cudaStream_t)>& fn, int launches) {
   Site& s = site();
   if (mode_ == Mode::kExec) {
@@ -436,64 +562,10 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     prof_begin(s);
     if (p.use_tc) {
       __nv_bfloat16* panel[2];
-      for (int side = 0; side < 2; ++side) {
-        OperandPlan& op = p.P[side];
-        if (op.constant) {
-          if (!op.packed) throw Error(GBCC_ERR_STATE, "engine: constant operand not packed");
-          panel[side] = op.packed;
-        } else if (op.cache_reuse) {
-          panel[side] = op.cache_buf;
-        } else {
-          panel[side] = op.cache_first ? op.cache_buf : (side == 0 ? wbfa_ : wbfb_);
-          GatherArgs g = op.gather;
-          g.outs = panel[side];
-          launch_gather(g, stream_);
-          ++n_launch_;
-        }
-      }
-      GemmTcArgs t{};
-      t.M = p.M;
-      t.N = p.N;
-      t.Mpad = p.P[0].rows_pad;
-      t.Npad = p.P[1].rows_pad;
-      t.Kpad = p.P[0].Kpad;
-      t.A = panel[0];
-      t.a_slices = p.slices;
-      t.B = panel[1];
-      t.b_slices = p.slices;
-      // a slice limit below the packed count keeps the pairs p + q < limit: the
-      // split is sequential, so these are exactly the products of a
-      // limit-slice split (used to measure the error of fewer slices)
-      const int lim = slice_limit_[cls];
-      t.npairs = 0;
-      for (int q = 0; q < p.npairs; ++q) {
-        if (lim > 0 && p.pa[q] + p.pb[q] >= lim) continue;
-        t.pa[t.npairs] = p.pa[q];
-        t.pb[t.npairs] = p.pb[q];
-        ++t.npairs;
-      }
-      t.C = p.C;
-      t.cm = p.cm;
-      t.cn = p.cn;
-      t.alpha = p.alpha;
-      t.beta = p.beta;
-      t.bn = p.bn;
-      t.chunk = chunk_;
-      t.err = err_;
-      t.ksplit = p.ksplit;
-      t.kb_per_split = static_cast<int>(p.k_per_split);
-      t.partial = wpart_;
-      t.m_major = p.m_major ? 1 : 0;
+      for (int side = 0; side < 2; ++side) panel[side] = tc_panel(p.P[side], side);
+      const GemmTcArgs t = tc_args(p, cls, panel);
       prof_gemm(s);
-      if (!launch_gemm_tc(t, stream_))
-        throw Error(GBCC_ERR_CUDA, "tcgen05 GEMM launch rejected (tensor map or size)");
-      ++n_tc_;
-      ++n_launch_;
-      if (p.ksplit > 1) {
-        launch_splitk_reduce(p.M, p.N, p.ksplit, wpart_, t.Mpad, t.Npad, p.C, p.cm, p.cn, p.alpha, p.beta,
-                             stream_);
-        ++n_launch_;
-      }
+      launch_tc(p, t);
     } else {
       const double* panel[2];
       for (int side = 0; side < 2; ++side) {
@@ -525,9 +597,15 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       f.ksplit = p.ksplit;
       f.k_per_split = p.k_per_split;
       f.partial = wpart_;
+      f.m_major = p.m_major ? 1 : 0;
       prof_gemm(s);
-      launch_gemm_f64(f, stream_);
-      n_launch_ += p.ksplit > 1 ? 2 : 1;
+      if (p.smallk) {
+        launch_gemm_smallk(f, stream_);
+        ++n_launch_;
+      } else {
+        launch_gemm_f64(f, stream_);
+        n_launch_ += p.ksplit > 1 ? 2 : 1;
+      }
     }
     prof_end(s);
     return;
@@ -566,6 +644,17 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     GemmPlan& p = s.plan[pm];
     p = GemmPlan{};
     p.flops = flops;
+    int slices = pm == 1 ? slices_for(cls, flops) : 0;
+    // a short contraction into a large output is memory-bound: CUDA cores
+    // (measured faster for N > 32; the tensor-core kernel wins below)
+    if (slices > 0 && K <= kSmallK && std::min(rowsA, rowsB) > 32 &&
+        static_cast<double>(rowsA) * static_cast<double>(rowsB) >= 1048576.0) {
+      slices = 0;
+      p.smallk = true;
+    }
+    // the larger operand on M: it is then re-read once per N tile, and N
+    // tiles are up to 256 wide (less padding alone, with the large operand on
+    // N, measured slower: more L2 re-reads of it)
     p.a_is_first = rowsA >= rowsB;
     const std::vector<Lin>& Ms = p.a_is_first ? A : B;
     const std::vector<Lin>& Ns = p.a_is_first ? B : A;
@@ -578,7 +667,6 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     p.K = K;
     p.beta = beta;
     p.C = c.t->d;
-    int slices = pm == 1 ? slices_for(cls, flops) : 0;
     p.use_tc = slices > 0;
     OperandPlan& PM = p.P[0];
     OperandPlan& PN = p.P[1];
@@ -670,7 +758,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       p.cm = upload(hm).d;
       p.cn = upload(hn).d;
     }
-    if (!p.use_tc) {
+    if (!p.use_tc && !p.smallk) {
       // fewer 64 x 64 output tiles than two per SM: split K over blocks (one SM
       // runs FP64 at ~1/150 of the GPU's already low FP64 rate, so even a
       // 1 MFLOP contraction is slow on a single block)
@@ -690,8 +778,13 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     }
     if (p.use_tc) {
       p.slices = slices;
-      // the ladder and ring contractions take the faster 256-wide tiles
-      p.bn = gemm_tc_pick_bn(p.N, cls == kClassLadder || cls == kClassRing);
+      // the ladder and ring contractions take the faster 192/256-wide tiles
+      const bool wide = cls == kClassLadder || cls == kClassRing;
+      p.bn = gemm_tc_pick_bn(p.N, wide);
+      int bns[4];
+      const int nbn = gemm_tc_bn_candidates(p.N, wide, bns);
+      int64_t npanel = 0;  // N-side panel rows: room for every candidate tile width
+      for (int c = 0; c < nbn; ++c) npanel = std::max<int64_t>(npanel, round_up(p.N, bns[c]));
       p.npairs = 0;
       for (int a = 0; a < slices; ++a)
         for (int b = 0; b < slices; ++b)
@@ -705,7 +798,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         OperandPlan& op = p.P[side];
         op.slices = slices;
         op.Kpad = Kpad;
-        op.rows_pad = round_up(op.rows, side == 0 ? kTcBM : p.bn);
+        op.rows_pad = side == 0 ? round_up(op.rows, kTcBM) : npanel;
         GatherArgs& g = op.gather;
         g.Rpad = op.rows_pad;
         g.Cpad = Kpad;
@@ -738,20 +831,40 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
           wsbf_b_ = std::max(wsbf_b_, need);
         }
       }
-      // fewer output tiles than SMs and a long K: split K over CTAs
-      const int64_t tiles = (p.P[0].rows_pad / kTcBM) * (p.P[1].rows_pad / p.bn);
+      // fewer output tiles than SMs and a long K: split K over CTAs.  The
+      // candidates: every tile width with that split, and unsplit where it splits
       const int64_t kblocks = Kpad / kTcBK;
       const int64_t sms = num_sms();
-      if (tiles < sms && kblocks >= 16) {
-        int64_t ks = std::min<int64_t>((sms + tiles - 1) / tiles, kblocks / 8);
-        if (ks > 1) {
-          const int64_t kbps = (kblocks + ks - 1) / ks;
-          ks = (kblocks + kbps - 1) / kbps;
-          p.ksplit = static_cast<int>(ks);
-          p.k_per_split = kbps;
-          wspart_ = std::max(wspart_, static_cast<size_t>(ks * p.P[0].rows_pad * p.P[1].rows_pad));
+      p.ncand = 0;
+      for (int c = 0; c < nbn; ++c) {
+        const int64_t npad = round_up(p.N, bns[c]);
+        const int64_t tiles = (p.P[0].rows_pad / kTcBM) * (npad / bns[c]);
+        int64_t ks = 1, kbps = 0;
+        if (tiles < sms && kblocks >= 16) {
+          ks = std::min<int64_t>((sms + tiles - 1) / tiles, kblocks / 8);
+          if (ks > 1) {
+            kbps = (kblocks + ks - 1) / ks;
+            ks = (kblocks + kbps - 1) / kbps;
+          } else {
+            ks = 1;
+          }
+        }
+        if (ks > 1) wspart_ = std::max(wspart_, static_cast<size_t>(ks * p.P[0].rows_pad * npad));
+        p.cand_bn[p.ncand] = bns[c];
+        p.cand_ks[p.ncand] = static_cast<int>(ks);
+        p.cand_kps[p.ncand] = kbps;
+        ++p.ncand;
+        if (ks > 1 && p.ncand < 8) {
+          p.cand_bn[p.ncand] = bns[c];
+          p.cand_ks[p.ncand] = 1;
+          p.cand_kps[p.ncand] = 0;
+          ++p.ncand;
         }
       }
+      // the heuristic choice: the first candidate
+      p.bn = p.cand_bn[0];
+      p.ksplit = p.cand_ks[0];
+      p.k_per_split = p.cand_kps[0];
     }
   }
 }

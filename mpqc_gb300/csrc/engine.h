@@ -106,7 +106,12 @@ struct SiteStat {
   int pairs = 0;       // BF16 slice products on the tensor cores (0: FP64 / elementwise)
   int cls = -1;        // TermClass of a contraction, -1 for an assignment
   int64_t M = 0, N = 0, K = 0;  // GEMM shape (assignment: rows, columns, 0)
+  int bn = 0;          // tensor cores: N tile width; -1: the short-K CUDA-core kernel
+  int ksplit = 1;      // K split over CTAs
 };
+
+struct OperandPlan;
+struct GemmPlan;
 
 class Engine {
  public:
@@ -159,6 +164,9 @@ class Engine {
   // a fixed kernel sequence of the program, enqueued in program order at EXEC;
   // `launches` is the number of kernels it enqueues
   void custom(const std::function<void(cudaStream_t)>& fn, int launches);
+  // time the candidate tile widths / K splits of every tensor-core contraction
+  // of the finalised mixed plan on its operands and keep the fastest
+  void autotune(int reps);
 
   // Statistics of the last EXEC pass (FLOPs of the contractions as planned).
   double flops() const { return flops_; }
@@ -172,6 +180,9 @@ class Engine {
   void prof_end(Site& s);
   void prof_gemm(Site& s);
   DevTable upload(const std::vector<int64_t>& v);
+  __nv_bfloat16* tc_panel(OperandPlan& op, int side);
+  GemmTcArgs tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* const panel[2]) const;
+  void launch_tc(const GemmPlan& p, const GemmTcArgs& t);
   int slices_for(TermClass cls, double flops) const;
 
   cudaStream_t stream_ = nullptr;

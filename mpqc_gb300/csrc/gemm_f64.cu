@@ -7,6 +7,8 @@
 // buffering.  FP64 FMA throughput, not memory, bounds this kernel on GB300.
 #include "kernels.h"
 
+#include <algorithm>
+
 namespace gbcc {
 namespace {
 
@@ -104,6 +106,158 @@ __global__ void __launch_bounds__(NT) gemm_f64_kernel(GemmF64Args g) {
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// short-K contraction on CUDA cores (see kernels.h)
+
+// double -> float, rounded to nearest (one FP32 addition of an exact head and
+// a rounded tail taken from the bit pattern; no FP64 instruction).  |x| below
+// FP32's normal range gives zero, beyond it infinity.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned sign = static_cast<unsigned>(u >> 63);
+  const int E = static_cast<int>((u >> 52) & 0x7FFull);
+  const int e32 = E - 896;
+  if (E == 0x7FF) return __uint_as_float((sign << 31) | 0x7F800000u | ((u & 0xFFFFFFFFFFFFFull) ? 0x400000u : 0u));
+  if (e32 >= 255) return __uint_as_float((sign << 31) | 0x7F800000u);
+  if (e32 <= 0) return __uint_as_float(sign << 31);
+  const float hi = __uint_as_float((sign << 31) | (static_cast<unsigned>(e32) << 23) |
+                                   (static_cast<unsigned>(u >> 29) & 0x7FFFFFu));
+  const unsigned lo_int = static_cast<unsigned>(u) & 0x1FFFFFFFu;
+  if (lo_int == 0u) return hi;
+  const int es = E - 948;
+  float lo = es >= 1 ? __uint2float_rn(lo_int) * __uint_as_float(static_cast<unsigned>(es) << 23)
+                     : (__uint2float_rn(lo_int) * 0x1p-64f) * __uint_as_float(static_cast<unsigned>(es + 64) << 23);
+  if (sign) lo = -lo;
+  return __fadd_rn(hi, lo);
+}
+
+// float -> double from the bit pattern (integer operations only)
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+  const unsigned long long sign = static_cast<unsigned long long>(b >> 31) << 63;
+  unsigned long long d;
+  if (e == 0xFFu) {
+    d = sign | (0x7FFull << 52) | (static_cast<unsigned long long>(m) << 29);
+  } else if (e != 0u) {
+    d = sign | (static_cast<unsigned long long>(e + 896u) << 52) | (static_cast<unsigned long long>(m) << 29);
+  } else if (m == 0u) {
+    d = sign;
+  } else {
+    const int p = 31 - __clz(static_cast<int>(m));
+    d = sign | (static_cast<unsigned long long>(p + 874) << 52) |
+        ((static_cast<unsigned long long>(m) << (52 - p)) & 0xFFFFFFFFFFFFFull);
+  }
+  return __longlong_as_double(static_cast<long long>(d));
+}
+
+// TM x TN output tiles (64 x 64, or 128 x 32 for N <= 32), 256 threads, 16
+// outputs per thread.  MMAJOR: lanes along M (C unit-stride in M), else along
+// N.  Threads (u, w) = (tid % 16, tid / 16) own rows u + 16 i and columns
+// w + 16 j (roles swapped for !MMAJOR), so 16 lanes touch 16 consecutive
+// elements of C.  The tile's reads of C are issued first, so their latency
+// overlaps the operand loads and the FMAs (the kernel is bound by the FP64
+// read-modify-write of C, not by arithmetic).
+template <bool MMAJOR, int TM, int TN>
+__global__ void __launch_bounds__(256, 2) gemm_smallk_kernel(GemmF64Args g) {
+  constexpr int IM = TM / 16, JN = TN / 16;
+  static_assert(IM * JN == 16, "16 outputs per thread");
+  __shared__ float As[kSmallK][TM + 1];
+  __shared__ float Bs[kSmallK][TN + 1];
+  const int tid = threadIdx.x;
+  const int K = static_cast<int>(g.K);
+  const int64_t mt = (g.M + TM - 1) / TM, nt = (g.N + TN - 1) / TN;
+  const int u = tid % 16, w = tid / 16;
+  const bool has_c = g.beta != 0.0;
+  for (int64_t tile = blockIdx.x; tile < mt * nt; tile += gridDim.x) {
+    const int64_t m0 = (tile / nt) * TM, n0 = (tile % nt) * TN;
+    int64_t om[IM], on[JN];  // -1 outside C
+#pragma unroll
+    for (int i = 0; i < IM; ++i) {
+      const int64_t m = m0 + (MMAJOR ? u : w) + 16 * i;
+      om[i] = m < g.M ? g.cm[m] : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < JN; ++j) {
+      const int64_t n = n0 + (MMAJOR ? w : u) + 16 * j;
+      on[j] = n < g.N ? g.cn[n] : -1;
+    }
+    double c[IM][JN];
+#pragma unroll
+    for (int i = 0; i < IM; ++i)
+#pragma unroll
+      for (int j = 0; j < JN; ++j) c[i][j] = (has_c && om[i] >= 0 && on[j] >= 0) ? g.C[om[i] + on[j]] : 0.0;
+    for (int e = tid; e < TM * K; e += blockDim.x) {
+      const int r = e / K, k = e % K;
+      const int64_t m = m0 + r;
+      As[k][r] = m < g.M ? d2f_rn(g.A[m * g.lda + k]) : 0.f;
+    }
+    for (int e = tid; e < TN * K; e += blockDim.x) {
+      const int r = e / K, k = e % K;
+      const int64_t n = n0 + r;
+      Bs[k][r] = n < g.N ? d2f_rn(g.B[n * g.ldb + k]) : 0.f;
+    }
+    __syncthreads();
+    float acc[IM][JN];
+#pragma unroll
+    for (int i = 0; i < IM; ++i)
+#pragma unroll
+      for (int j = 0; j < JN; ++j) acc[i][j] = 0.f;
+    for (int k = 0; k < K; ++k) {
+      float a[IM], b[JN];
+#pragma unroll
+      for (int i = 0; i < IM; ++i) a[i] = As[k][(MMAJOR ? u : w) + 16 * i];
+#pragma unroll
+      for (int j = 0; j < JN; ++j) b[j] = Bs[k][(MMAJOR ? w : u) + 16 * j];
+#pragma unroll
+      for (int i = 0; i < IM; ++i)
+#pragma unroll
+        for (int j = 0; j < JN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    // one FP64 operation per element; the beta cases in separate loops so no
+    // multiply by beta is evaluated where beta is 0 or 1
+    if (!has_c) {
+#pragma unroll
+      for (int i = 0; i < IM; ++i)
+#pragma unroll
+        for (int j = 0; j < JN; ++j)
+          if (om[i] >= 0 && on[j] >= 0) g.C[om[i] + on[j]] = g.alpha * f2d_bits(acc[i][j]);
+    } else if (g.beta == 1.0) {
+#pragma unroll
+      for (int i = 0; i < IM; ++i)
+#pragma unroll
+        for (int j = 0; j < JN; ++j)
+          if (om[i] >= 0 && on[j] >= 0) g.C[om[i] + on[j]] = fma(g.alpha, f2d_bits(acc[i][j]), c[i][j]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < IM; ++i)
+#pragma unroll
+        for (int j = 0; j < JN; ++j)
+          if (om[i] >= 0 && on[j] >= 0)
+            g.C[om[i] + on[j]] = fma(g.alpha, f2d_bits(acc[i][j]), g.beta * c[i][j]);
+    }
+    __syncthreads();
+  }
+}
+
+template <int TM, int TN>
+void launch_smallk_tiles(const GemmF64Args& g, cudaStream_t st) {
+  const int64_t tiles = ((g.M + TM - 1) / TM) * ((g.N + TN - 1) / TN);
+  const unsigned grid = static_cast<unsigned>(std::min<int64_t>(tiles, static_cast<int64_t>(num_sms()) * 2));
+  if (g.m_major)
+    gemm_smallk_kernel<true, TM, TN><<<grid, 256, 0, st>>>(g);
+  else
+    gemm_smallk_kernel<false, TM, TN><<<grid, 256, 0, st>>>(g);
+}
+
+void launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st) {
+  if (g.M <= 0 || g.N <= 0) return;
+  if (g.N <= 32)
+    launch_smallk_tiles<128, 32>(g, st);
+  else
+    launch_smallk_tiles<64, 64>(g, st);
+}
 
 void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return;

@@ -294,7 +294,31 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   lo = __fadd_rn(lo, e);
 }
 
-constexpr int kStgLd = 17;  // padded row of the per-warp output staging tile (doubles)
+constexpr int kStgLd = 17;  // padded row of the per-warp output staging tile (8-byte words)
+
+// float -> double by rewriting the bit pattern (exact), integer operations
+// only.  GB300 runs FP64 arithmetic and FP64 conversions at ~2 per clock per
+// SM, and the epilogue of a short-K contraction is bound by them (ncu: FP64
+// pipe 64 % busy, DRAM 14 % at K = 32).  Every class of input is handled
+// without a hardware conversion (a rare-case fallback would be evaluated for
+// every element once the compiler turns the branch into a select).
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+  const uint64_t sign = static_cast<uint64_t>(b >> 31) << 63;
+  uint64_t d;
+  if (e == 0xFFu) {
+    d = sign | (0x7FFull << 52) | (static_cast<uint64_t>(m) << 29);  // inf / nan
+  } else if (e != 0u) {
+    d = sign | (static_cast<uint64_t>(e + 896u) << 52) | (static_cast<uint64_t>(m) << 29);
+  } else if (m == 0u) {
+    d = sign;
+  } else {  // subnormal: m 2^-149 with leading bit p
+    const int p = 31 - __clz(static_cast<int>(m));
+    d = sign | (static_cast<uint64_t>(p + 874) << 52) | ((static_cast<uint64_t>(m) << (52 - p)) & 0xFFFFFFFFFFFFFull);
+  }
+  return __longlong_as_double(static_cast<long long>(d));
+}
 
 template <int BN, bool CTA2>
 struct TcCfg {
@@ -302,9 +326,6 @@ struct TcCfg {
   static constexpr int kBRows = CTA2 ? BN / 2 : BN;
   static constexpr uint32_t kABytes = BM * BK * 2;
   static constexpr uint32_t kBBytes = kBRows * BK * 2;
-  static constexpr int kStages = (kABytes + kBBytes) >= 49152 ? 3
-                                 : (kABytes + kBBytes) >= 32768 ? 5
-                                 : ((kABytes + kBBytes) >= 24576 ? 7 : 8);
   static constexpr uint32_t kStageBytes = kABytes + kBBytes;
   // warps 0 (TMA), 1 (MMA), 2-3 idle, 4-11 epilogue: three warps per
   // scheduler leave 168 registers a thread
@@ -312,11 +333,16 @@ struct TcCfg {
   static constexpr int kEpiWarp0 = 4;
   static constexpr int kThreads = 32 * (kEpiWarp0 + kEpiWarps);
   static constexpr uint32_t kStgBytes = kEpiWarps * 32 * kStgLd * 8;
+  // as many stages as fit in 227 KB next to the staging tile and barriers (3
+  // for BN = 256, 4 for 192, 5 for 128, 7 for 64, 8 for 32)
+  static constexpr int kStagesFit = static_cast<int>((232448u - 1024u - 256u - kStgBytes) / kStageBytes);
+  static constexpr int kStages = kStagesFit > 8 ? 8 : kStagesFit;
   static constexpr uint32_t kSmem = 1024 + kStages * kStageBytes + kStgBytes + 256;
   // BN <= 128: two accumulators [0, 2 BN) + float-float words [2 BN, 4 BN);
   // BN = 256: the two accumulators fill TMEM and the chunks of a tile sum in
   // FP32 registers (no float-float fold)
   static constexpr bool kFold = BN <= 128;
+  static_assert(BN % 32 == 0 && BN <= 256, "tile width");
   static constexpr uint32_t kTmemCols = BN >= 128 ? 512 : (BN >= 64 ? 256 : 128);
   static constexpr int kCols = BN / (kEpiWarps / 4);                // columns per epilogue thread
 };
@@ -605,13 +631,42 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
                 cv[j] = n < g.N ? g.C[om + g.cn[n]] : 0.0;
               }
             }
+            if constexpr (Cfg::kFold) {
+              // beta c + alpha (hi + lo): separate loops per beta, so no multiply by
+              // beta is evaluated (as a select) where beta is 0 or 1
+              if (g.beta == 0.0) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int64_t n = n0 + col0 + j0 + j;
-              if (n < g.N) {
-                const double val = g.alpha * (static_cast<double>(__uint_as_float(h[j])) +
-                                              static_cast<double>(__uint_as_float(l[j])));
-                g.C[om + g.cn[n]] = (g.beta == 0.0) ? val : fma(g.beta, cv[j], val);
+                for (int j = 0; j < 16; ++j) {
+                  const int64_t n = n0 + col0 + j0 + j;
+                  if (n < g.N)
+                    g.C[om + g.cn[n]] = g.alpha * (f2d_exact(__uint_as_float(h[j])) + f2d_exact(__uint_as_float(l[j])));
+                }
+              } else if (g.beta == 1.0) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                  const int64_t n = n0 + col0 + j0 + j;
+                  if (n < g.N)
+                    g.C[om + g.cn[n]] = fma(g.alpha, f2d_exact(__uint_as_float(h[j])),
+                                            fma(g.alpha, f2d_exact(__uint_as_float(l[j])), cv[j]));
+                }
+              } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                  const int64_t n = n0 + col0 + j0 + j;
+                  if (n < g.N)
+                    g.C[om + g.cn[n]] = fma(g.alpha, f2d_exact(__uint_as_float(h[j])),
+                                            fma(g.alpha, f2d_exact(__uint_as_float(l[j])), g.beta * cv[j]));
+                }
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                const int64_t n = n0 + col0 + j0 + j;
+                if (n < g.N) {
+                  const double val = g.alpha * (static_cast<double>(__uint_as_float(h[j])) +
+                                                static_cast<double>(__uint_as_float(l[j])));
+                  g.C[om + g.cn[n]] = (g.beta == 0.0) ? val : fma(g.beta, cv[j], val);
+                }
               }
             }
           }
@@ -636,10 +691,18 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
             l[j] = 0u;
           }
         }
+        if constexpr (Cfg::kFold) {
+          // (hi, lo) pairs, converted to FP64 at the store
+          float2* stg2 = reinterpret_cast<float2*>(stg);
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-          stg[lane * kStgLd + j] =
-              static_cast<double>(__uint_as_float(h[j])) + static_cast<double>(__uint_as_float(l[j]));
+          for (int j = 0; j < 16; ++j)
+            stg2[lane * kStgLd + j] = make_float2(__uint_as_float(h[j]), __uint_as_float(l[j]));
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            stg[lane * kStgLd + j] =
+                static_cast<double>(__uint_as_float(h[j])) + static_cast<double>(__uint_as_float(l[j]));
+        }
         __syncwarp();
         const int64_t n = n0 + col0 + j0 + cj;
         if (ksplit > 1) {
@@ -648,7 +711,12 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
 #pragma unroll
           for (int rr = lane >> 4; rr < 32; rr += 2) {
             const int64_t m = m0 + q * 32 + rr;
-            P[m * g.Npad] = stg[rr * kStgLd + cj];
+            if constexpr (Cfg::kFold) {
+              const float2 hl = reinterpret_cast<const float2*>(stg)[rr * kStgLd + cj];
+              P[m * g.Npad] = f2d_exact(hl.x) + f2d_exact(hl.y);
+            } else {
+              P[m * g.Npad] = stg[rr * kStgLd + cj];
+            }
           }
         } else if (cj < COLS && n < g.N) {
           const int64_t on = g.cn[n];
@@ -664,11 +732,37 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
 #pragma unroll
             for (int r = 0; r < 16; ++r) cv[r] = off[r] >= 0 ? g.C[off[r]] : 0.0;
           }
+          if constexpr (Cfg::kFold) {
+            const float2* stg2 = reinterpret_cast<const float2*>(stg);
+            if (g.beta == 0.0) {
 #pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            if (off[r] < 0) continue;
-            const double val = g.alpha * stg[((lane >> 4) + 2 * r) * kStgLd + cj];
-            g.C[off[r]] = (g.beta == 0.0) ? val : fma(g.beta, cv[r], val);
+              for (int r = 0; r < 16; ++r) {
+                if (off[r] < 0) continue;
+                const float2 hl = stg2[((lane >> 4) + 2 * r) * kStgLd + cj];
+                g.C[off[r]] = g.alpha * (f2d_exact(hl.x) + f2d_exact(hl.y));
+              }
+            } else if (g.beta == 1.0) {
+#pragma unroll
+              for (int r = 0; r < 16; ++r) {
+                if (off[r] < 0) continue;
+                const float2 hl = stg2[((lane >> 4) + 2 * r) * kStgLd + cj];
+                g.C[off[r]] = fma(g.alpha, f2d_exact(hl.x), fma(g.alpha, f2d_exact(hl.y), cv[r]));
+              }
+            } else {
+#pragma unroll
+              for (int r = 0; r < 16; ++r) {
+                if (off[r] < 0) continue;
+                const float2 hl = stg2[((lane >> 4) + 2 * r) * kStgLd + cj];
+                g.C[off[r]] = fma(g.alpha, f2d_exact(hl.x), fma(g.alpha, f2d_exact(hl.y), g.beta * cv[r]));
+              }
+            }
+          } else {
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+              if (off[r] < 0) continue;
+              const double val = g.alpha * stg[((lane >> 4) + 2 * r) * kStgLd + cj];
+              g.C[off[r]] = (g.beta == 0.0) ? val : fma(g.beta, cv[r], val);
+            }
           }
         }
         __syncwarp();
@@ -723,8 +817,8 @@ template <int BN, bool CTA2>
 bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
   using Cfg = TcCfg<BN, CTA2>;
   CUtensorMap ma, mb;
-  if (!make_map(&ma, g.A, g.a_slices, g.Mpad, g.Kpad, BM)) return false;
-  if (!make_map(&mb, g.B, g.b_slices, g.Npad, g.Kpad, Cfg::kBRows)) return false;
+  if (!make_map(&ma, g.A, g.a_slices, g.a_rows ? g.a_rows : g.Mpad, g.Kpad, BM)) return false;
+  if (!make_map(&mb, g.B, g.b_slices, g.b_rows ? g.b_rows : g.Npad, g.Kpad, Cfg::kBRows)) return false;
   static bool attr_set = false;
   if (!attr_set) {
     if (cudaFuncSetAttribute(gemm_tc_kernel<BN, CTA2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -769,8 +863,30 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
 int gemm_tc_pick_bn(int64_t N, bool allow256) {
   if (N <= 32) return 32;
   if (N <= 64) return 64;
-  if (allow256 && N >= 256) return 256;
+  if (allow256 && N >= 256) {
+    // 256- or 192-wide tiles, whichever pads N less (e.g. 528 = 3 x 176 -> 576 vs 768)
+    const int64_t p256 = (N + 255) / 256 * 256, p192 = (N + 191) / 192 * 192;
+    return p192 < p256 ? 192 : 256;
+  }
   return 128;
+}
+
+int gemm_tc_bn_candidates(int64_t N, bool allow256, int* out) {
+  int n = 0;
+  const int first = gemm_tc_pick_bn(N, allow256);
+  out[n++] = first;
+  auto add = [&](int bn) {
+    for (int i = 0; i < n; ++i)
+      if (out[i] == bn) return;
+    out[n++] = bn;
+  };
+  if (N > 32) add(N <= 64 ? 32 : 64);
+  if (N > 64) add(128);
+  if (allow256 && N >= 256) {
+    add(192);
+    add(256);
+  }
+  return n;
 }
 
 bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
@@ -779,6 +895,7 @@ bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
       g.npairs > kMaxPairs)
     return false;
   if (g.Mpad > (1LL << 31) - 1 || g.Npad > (1LL << 31) - 1 || g.Kpad > (1LL << 31) - 1) return false;
+  if ((g.a_rows && g.a_rows < g.Mpad) || (g.b_rows && g.b_rows < g.Npad)) return false;
   if ((g.Npad / g.bn) * (g.Mpad / BM) * (g.ksplit > 1 ? g.ksplit : 1) > (1LL << 31) - 1) return false;
   if (g.ksplit > 1 && (!g.partial || g.kb_per_split < 1 ||
                        static_cast<int64_t>(g.ksplit - 1) * g.kb_per_split >= g.Kpad / BK))
@@ -795,6 +912,7 @@ bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
     case 32: return launch_bn<32, false>(g, st);
     case 64: return launch_bn<64, false>(g, st);
     case 128: return launch_bn<128, false>(g, st);
+    case 192: return launch_bn<192, false>(g, st);
     case 256: return launch_bn<256, false>(g, st);
     default: return false;
   }

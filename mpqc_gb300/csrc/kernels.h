@@ -75,8 +75,17 @@ struct GemmF64Args {
   const int64_t* cm;
   const int64_t* cn;
   double alpha, beta;
+  int m_major;           // C unit-stride along M (small-K kernel: lanes along M)
 };
 void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st);
+
+// Short contractions (K <= kSmallK) with large outputs on CUDA cores: FP64
+// panels rounded to FP32, FP32 products and sums, one FP64 FMA per output.
+// Memory-bound on the FP64 read-modify-write of C; used in mixed precision
+// instead of the tensor-core pipeline, whose per-tile handshakes leave such
+// outputs latency-bound.  Same argument conventions as launch_gemm_f64 (no K split).
+constexpr int64_t kSmallK = 64;
+void launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Split-BF16 tcgen05 GEMM (sm_103a):
@@ -106,6 +115,9 @@ struct GemmTcArgs {
   int m_major;           // C is contiguous along M: epilogue lanes run along M
   int cta2;              // CTA pairs (tcgen05 cta_group::2, 256-row tiles); Mpad % 256 == 0, bn >= 64
   int* err;              // device error word
+  // rows per slice of the A / B panels as stored (0: Mpad / Npad); a panel may
+  // hold more rows than the launch covers (padded for every candidate tile)
+  int64_t a_rows, b_rows;
 };
 // Deterministic K-split reduction: C[cm[m] + cn[n]] = beta*C + alpha * sum_s
 // partial[s][m][n] (splits summed in order), partial rows of length ldp and
@@ -117,9 +129,12 @@ int num_sms();
 
 // Returns false if the tensor maps could not be encoded (bad alignment / size).
 bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st);
-// N tile for a GEMM of N columns; allow256: 256-wide tiles (faster, FP32
-// register accumulation of the chunks) for N >= 256
+// N tile for a GEMM of N columns; allow256: 256- or 192-wide tiles (faster,
+// FP32 register accumulation of the chunks) for N >= 256
 int gemm_tc_pick_bn(int64_t N, bool allow256);
+// N tiles worth timing for a GEMM of N columns (the tuner's candidates), the
+// heuristic choice first; returns their number (<= 4)
+int gemm_tc_bn_candidates(int64_t N, bool allow256, int* out);
 constexpr int kTcBM = 128;
 constexpr int kTcBK = 64;
 

@@ -37,7 +37,8 @@ extern "C" int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const doubl
   using namespace gbcc;
   if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1 || ksplit < 1)
     return GBCC_ERR_INVALID_ARG;
-  if (bn_req != 0 && bn_req != 32 && bn_req != 64 && bn_req != 128 && bn_req != 256) return GBCC_ERR_INVALID_ARG;
+  if (bn_req != 0 && bn_req != 32 && bn_req != 64 && bn_req != 128 && bn_req != 192 && bn_req != 256)
+    return GBCC_ERR_INVALID_ARG;
   std::vector<void*> owned;
   auto alloc = [&](size_t bytes) {
     void* p = dev_alloc(bytes);

@@ -31,7 +31,7 @@ def test_header_and_binding_agree():
 def test_library_exports_every_declared_symbol(lib):
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.gbcc_abi_version() == 2
+    assert lib.gbcc_abi_version() == 3
 
 
 def test_defaults_follow_the_reference(lib):
@@ -43,7 +43,7 @@ def test_defaults_follow_the_reference(lib):
     assert c.diis_damp == 0.0 and c.diis_ngroup == 1 and c.diis_group_nstart == 1
     assert c.target_precision == 1e-9 and c.precision == 0 and c.use_graphs == 1
     assert (c.slices_ladder, c.slices_ring, c.slices_other) == (0, 0, 0) and c.slice_tolerance == 1e-5
-    assert c.mixed_switch_precision == 0.0
+    assert c.mixed_switch_precision == 0.0 and c.autotune == 1
 
 
 @pytest.mark.parametrize("field,value", [("o", 0), ("v", -1), ("n_diis", 0), ("n_diis", 17),

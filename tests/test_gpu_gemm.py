@@ -84,13 +84,14 @@ def test_gemm_split_k(tlib, M, N, K, ksplit, slices):
     assert np.array_equal(out, out2)
 
 
-# kernel variants: (bn, cta2, chunk, fold); bn 256 sums chunks in FP32 registers
-VARIANTS = [(256, 0, 4, 0), (256, 0, 8, 0), (128, 1, 4, 16), (64, 1, 4, 16), (128, 0, 1, 1), (64, 0, 16, 64)]
+# kernel variants: (bn, cta2, chunk, fold); bn 192 and 256 sum chunks in FP32 registers
+VARIANTS = [(256, 0, 4, 0), (256, 0, 8, 0), (192, 0, 4, 0), (128, 1, 4, 16), (64, 1, 4, 16), (128, 0, 1, 1),
+            (64, 0, 16, 64)]
 
 
 @pytest.mark.parametrize("bn,cta2,chunk,fold", VARIANTS)
 @pytest.mark.parametrize("M,N,K,ksplit", [(256, 256, 64, 1), (300, 520, 1000, 1), (700, 300, 2000, 3),
-                                          (128, 256, 6000, 5)])
+                                          (128, 256, 6000, 5), (260, 528, 1500, 1)])
 def test_gemm_kernel_variants(tlib, M, N, K, ksplit, bn, cta2, chunk, fold):
     rng = np.random.default_rng(M + N + K + bn)
     A = rng.normal(size=(M, K))

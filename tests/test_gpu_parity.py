@@ -42,8 +42,10 @@ def test_residual_fp64_random(o, v, naux):
 
 
 @pytest.mark.parametrize("slices", [3, 2, 1])
-@pytest.mark.parametrize("o,v,naux", [(4, 9, 12), (8, 40, 30), (12, 70, 60)])
+@pytest.mark.parametrize("o,v,naux", [(4, 9, 12), (8, 40, 30), (12, 70, 60), (16, 72, 40)])
 def test_residual_mixed(o, v, naux, slices):
+    """(16, 72): the short (K = o) contractions into o^2 v^2 outputs run on the
+    CUDA-core kernel; every size runs the tensor-core contractions."""
     inp = synth.make_inputs(o, v, naux, seed=o * 10 + v, t1_scale=1e-2)
     r1_ref, r2_ref = R.residual(inp.t1, inp.t2, oracle_ints(inp))
     with _solver(inp, precision="mixed", slices=(slices,) * 3) as s:
@@ -199,3 +201,17 @@ def test_mixed_solve_with_automatic_slices():
         e, t1, t2, rep = s.solve()
     assert rep.converged and rep.fp64_iters >= 2
     assert abs(e - ref.e_corr) < 1e-6 and np.max(np.abs(t2 - ref.t2)) < 1e-6
+
+
+def test_autotuned_tiles_give_the_same_residual():
+    """The tuner only picks tile widths and K splits among candidates: the
+    residual agrees with the untuned plan to rounding (K splits sum in FP64)."""
+    inp = synth.make_inputs(10, 60, 30, seed=61, t1_scale=1e-2)
+    with _solver(inp, precision="mixed", autotune=True) as s:
+        a1, a2 = s.residual(inp.t1, inp.t2)
+        prof = s.profile_residual()
+    with _solver(inp, precision="mixed", autotune=False) as s:
+        b1, b2 = s.residual(inp.t1, inp.t2)
+    assert rel_err(a2, b2) < 1e-9 and rel_err(a1, b1) < 1e-9
+    tc = [p for p in prof if p["pairs"] > 0]
+    assert tc and all(p["bn"] in (32, 64, 128, 192, 256) and p["ksplit"] >= 1 for p in tc)
