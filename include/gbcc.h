@@ -145,7 +145,8 @@ gbcc_status gbcc_commit_inputs(gbcc_handle* h);
 /* One residual: tau = t2 + t1 t1, R1 then R2 (R1 sets the FIJ/FAB
  * intermediates R2 reads), in the handle's precision.  t2 must be
  * pair-symmetric, t2(a,b,i,j) = t2(b,a,j,i), as closed-shell CCSD amplitudes
- * are: the particle-particle ladder is evaluated over a <= b, i <= j. */
+ * are: the particle-particle ladder is evaluated over a <= b, i <= j.  A t2
+ * further than 1e-12 max|t2| from that symmetry gives GBCC_ERR_INVALID_ARG. */
 gbcc_status gbcc_residual(gbcc_handle* h, const double* t1_ai, const double* t2_abij,
                           double* r1_ai, double* r2_abij);
 

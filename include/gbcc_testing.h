@@ -34,6 +34,13 @@ int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const double* A, const
  * (host), the bit patterns of slices s = 0..nslices-1 (nslices 1..3). */
 int gbcc_testing_split(const double* x, int64_t n, int nslices, uint16_t* out);
 
+/* As gbcc_testing_gemm_ex with the number of slices per pipeline stage:
+ * sps = 1, one (A, B) slice pair per stage; 2, both slices of a k-block per
+ * stage (slices = 2, bn 64 / 128 / 192). */
+int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+                          int slices, int ksplit, int bn, int cta2, int chunk, int fold, int sps, int repeat,
+                          float* ms);
+
 /* Peak probe: FP64 FMA throughput of this GPU in GFLOP/s (a register-resident
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);
@@ -64,8 +71,8 @@ int gbcc_testing_elapsed(struct gbcc_handle* h, int slot0, int slot1, float* ms)
 int gbcc_testing_profile_gemm_ms(struct gbcc_handle* h, int max_sites, double* ms);
 
 /* Per operation of the last profiled residual: N tile width of a tensor-core
- * contraction (-1: the short-K CUDA-core kernel, 0: FP64 / elementwise) and
- * its K split, as pairs tiles[2 i], tiles[2 i + 1]. */
+ * contraction (-1: the short-K CUDA-core kernel, 0: FP64 / elementwise), its
+ * K split and its slices per pipeline stage, as tiles[3 i .. 3 i + 2]. */
 int gbcc_testing_profile_tiles(gbcc_handle* h, int max_sites, int32_t* tiles);
 
 /* GEMM shape (M, N, K) of each operation of the last profiled residual,

@@ -47,7 +47,7 @@ struct gbcc_handle {
   cudaEvent_t slots[8] = {};
   std::vector<double> prof_gemm_ms;
   std::vector<std::array<int64_t, 3>> prof_dims;
-  std::vector<std::array<int32_t, 2>> prof_tiles;
+  std::vector<std::array<int32_t, 3>> prof_tiles;
   // residual program captured as a CUDA graph, one per precision (FP64, mixed)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_launches[2] = {0, 0};
@@ -249,6 +249,19 @@ void tune_plan(gbcc_handle* h) {
   sync_check(h);
 }
 
+// The particle-particle ladder runs over a <= b, i <= j: amplitudes must be
+// pair-symmetric, t2(a,b,i,j) = t2(b,a,j,i) (closed-shell CCSD amplitudes are)
+void check_pair_symmetric(gbcc_handle* h) {
+  auto* out = reinterpret_cast<unsigned long long*>(h->d_out + 8);
+  GBCC_CK(cudaMemsetAsync(out, 0, 2 * sizeof(double), h->stream));
+  gbcc::launch_pair_asym(h->cfg.o, h->cfg.v, h->S.t2->d, out, h->stream);
+  GBCC_CK(cudaMemcpyAsync(h->h_out + 8, h->d_out + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  sync_check(h);
+  if (!(h->h_out[8] <= 1e-12 * h->h_out[9]))
+    throw Error(GBCC_ERR_INVALID_ARG, "t2 is not pair-symmetric (t2(a,b,i,j) != t2(b,a,j,i)): max difference " +
+                                          std::to_string(h->h_out[8]) + " of max |t2| " + std::to_string(h->h_out[9]));
+}
+
 void plan_residual(gbcc_handle* h) {
   drop_graphs(h);
   h->eng->reset_plans();
@@ -295,6 +308,7 @@ void calibrate_slices(gbcc_handle* h, const double* t1_in, const double* t2_in) 
   if (t1_in && t2_in) {
     GBCC_CK(cudaMemcpyAsync(S.t1->d, t1_in, n1 * sizeof(double), cudaMemcpyDefault, st));
     GBCC_CK(cudaMemcpyAsync(S.t2->d, t2_in, n2 * sizeof(double), cudaMemcpyDefault, st));
+    check_pair_symmetric(h);
   } else {
     GBCC_CK(cudaMemsetAsync(S.t1->d, 0, n1 * sizeof(double), st));
     GBCC_CK(cudaMemsetAsync(S.t2->d, 0, n2 * sizeof(double), st));
@@ -524,6 +538,7 @@ gbcc_status gbcc_residual_ex(gbcc_handle* h, int32_t precision, const double* t1
       throw Error(GBCC_ERR_INVALID_ARG, "gbcc_residual: NULL argument");
     copy_in(h->S.t1->d, t1_ai, n1_of(h), h->stream);
     copy_in(h->S.t2->d, t2_abij, n2_of(h), h->stream);
+    check_pair_symmetric(h);
     run_residual(h, precision);
     copy_out(r1_ai, h->S.r1->d, n1_of(h), h->stream);
     copy_out(r2_abij, h->S.r2->d, n2_of(h), h->stream);
@@ -771,7 +786,7 @@ int gbcc_testing_profile_residual(gbcc_handle* h, int precision, int max_sites, 
     for (const auto& x : st) {
       h->prof_gemm_ms.push_back(x.gemm_ms);
       h->prof_dims.push_back({x.M, x.N, x.K});
-      h->prof_tiles.push_back({x.bn, x.ksplit});
+      h->prof_tiles.push_back({x.bn, x.ksplit, x.sps});
     }
     if (nsites) *nsites = static_cast<int>(st.size());
     for (int i = 0; i < max_sites && i < static_cast<int>(st.size()); ++i) {
@@ -792,10 +807,8 @@ int gbcc_testing_profile_gemm_ms(gbcc_handle* h, int max_sites, double* ms) {
 
 int gbcc_testing_profile_tiles(gbcc_handle* h, int max_sites, int32_t* tiles) {
   if (!h || !tiles) return GBCC_ERR_INVALID_ARG;
-  for (int i = 0; i < max_sites && i < static_cast<int>(h->prof_tiles.size()); ++i) {
-    tiles[2 * i] = h->prof_tiles[i][0];
-    tiles[2 * i + 1] = h->prof_tiles[i][1];
-  }
+  for (int i = 0; i < max_sites && i < static_cast<int>(h->prof_tiles.size()); ++i)
+    for (int k = 0; k < 3; ++k) tiles[3 * i + k] = h->prof_tiles[i][k];
   return GBCC_OK;
 }
 

@@ -167,11 +167,12 @@ struct GemmPlan {
   int64_t k_per_split = 0;  // FP64: K elements per split; tensor cores: k-blocks per split
   int pa[kMaxPairs] = {}, pb[kMaxPairs] = {};
   double flops = 0.0;
-  // tensor cores: (tile width, K split) candidates for the tuner, the plan's
-  // heuristic choice first
+  int sps = 1;             // tensor cores: slices per pipeline stage (2: both slices of a k-block)
+  // tensor cores: (tile width, K split, slices per stage) candidates for the
+  // tuner, the plan's heuristic choice first
   int ncand = 0;
-  int cand_bn[8] = {}, cand_ks[8] = {};
-  int64_t cand_kps[8] = {};
+  int cand_bn[16] = {}, cand_ks[16] = {}, cand_sps[16] = {};
+  int64_t cand_kps[16] = {};
 };
 
 struct Site {
@@ -231,6 +232,7 @@ std::vector<SiteStat> Engine::site_stats(int precision) {
       st.K = p.K;
       st.bn = p.use_tc ? p.bn : (p.smallk ? -1 : 0);
       st.ksplit = p.ksplit;
+      st.sps = p.use_tc ? p.sps : 0;
     } else {
       st.M = sp->gather.R;
       st.N = sp->gather.C;
@@ -473,6 +475,9 @@ GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* cons
   t.kb_per_split = static_cast<int>(p.k_per_split);
   t.partial = wpart_;
   t.m_major = p.m_major ? 1 : 0;
+  // a slice limit makes the packed slices a superset of the used ones: one
+  // pair per stage then
+  t.sps = (lim > 0 && lim < p.slices) ? 1 : p.sps;
   return t;
 }
 
@@ -515,6 +520,7 @@ void Engine::autotune(int reps) {
       q.bn = p.cand_bn[c];
       q.ksplit = p.cand_ks[c];
       q.k_per_split = p.cand_kps[c];
+      q.sps = p.cand_sps[c];
       const GemmTcArgs t = tc_args(q, sp->cls, panel);
       if (!launch_gemm_tc(t, stream_)) continue;
       if (q.ksplit > 1)
@@ -534,6 +540,7 @@ void Engine::autotune(int reps) {
       p.bn = p.cand_bn[pick];
       p.ksplit = p.cand_ks[pick];
       p.k_per_split = p.cand_kps[pick];
+      p.sps = p.cand_sps[pick];
     }
   }
   GBCC_CK(cudaStreamSynchronize(stream_));
@@ -850,21 +857,24 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
           }
         }
         if (ks > 1) wspart_ = std::max(wspart_, static_cast<size_t>(ks * p.P[0].rows_pad * npad));
-        p.cand_bn[p.ncand] = bns[c];
-        p.cand_ks[p.ncand] = static_cast<int>(ks);
-        p.cand_kps[p.ncand] = kbps;
-        ++p.ncand;
-        if (ks > 1 && p.ncand < 8) {
-          p.cand_bn[p.ncand] = bns[c];
-          p.cand_ks[p.ncand] = 1;
-          p.cand_kps[p.ncand] = 0;
-          ++p.ncand;
+        // both slices of a k-block per stage: two slices, tiles up to 192 wide
+        const int nsps = (slices == 2 && bns[c] >= 64 && bns[c] <= 192) ? 2 : 1;
+        for (int sp = 1; sp <= nsps; ++sp) {
+          for (int split = 0; split < (ks > 1 ? 2 : 1); ++split) {
+            if (p.ncand >= 16) break;
+            p.cand_bn[p.ncand] = bns[c];
+            p.cand_ks[p.ncand] = split == 0 ? static_cast<int>(ks) : 1;
+            p.cand_kps[p.ncand] = split == 0 ? kbps : 0;
+            p.cand_sps[p.ncand] = sp;
+            ++p.ncand;
+          }
         }
       }
       // the heuristic choice: the first candidate
       p.bn = p.cand_bn[0];
       p.ksplit = p.cand_ks[0];
       p.k_per_split = p.cand_kps[0];
+      p.sps = p.cand_sps[0];
     }
   }
 }

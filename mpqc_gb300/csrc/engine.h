@@ -108,6 +108,7 @@ struct SiteStat {
   int64_t M = 0, N = 0, K = 0;  // GEMM shape (assignment: rows, columns, 0)
   int bn = 0;          // tensor cores: N tile width; -1: the short-K CUDA-core kernel
   int ksplit = 1;      // K split over CTAs
+  int sps = 1;         // tensor cores: slices per pipeline stage
 };
 
 struct OperandPlan;

@@ -320,23 +320,38 @@ __device__ __forceinline__ double f2d_exact(float f) {
   return __longlong_as_double(static_cast<long long>(d));
 }
 
-template <int BN, bool CTA2>
+// SPS: slices per pipeline stage.  1: a stage holds one (A slice, B slice)
+// pair of a k-block and feeds one pair of MMAs; 2: a stage holds both slices
+// of A and of B of a k-block and feeds all three pair products (no tile is
+// loaded twice; two slices only).
+template <int BN, bool CTA2, int SPS = 1>
 struct TcCfg {
   // a CTA pair splits B along N: each CTA stages BN/2 rows of it
   static constexpr int kBRows = CTA2 ? BN / 2 : BN;
-  static constexpr uint32_t kABytes = BM * BK * 2;
+  static constexpr uint32_t kABytes = BM * BK * 2;  // one slice tile
   static constexpr uint32_t kBBytes = kBRows * BK * 2;
-  static constexpr uint32_t kStageBytes = kABytes + kBBytes;
+  static constexpr uint32_t kAStage = SPS * kABytes;
+  static constexpr uint32_t kBStage = SPS * kBBytes;
+  static constexpr uint32_t kStageBytes = kAStage + kBStage;
   // warps 0 (TMA), 1 (MMA), 2-3 idle, 4-11 epilogue: three warps per
   // scheduler leave 168 registers a thread
   static constexpr int kEpiWarps = 8;
   static constexpr int kEpiWarp0 = 4;
   static constexpr int kThreads = 32 * (kEpiWarp0 + kEpiWarps);
-  static constexpr uint32_t kStgBytes = kEpiWarps * 32 * kStgLd * 8;
-  // as many stages as fit in 227 KB next to the staging tile and barriers (3
-  // for BN = 256, 4 for 192, 5 for 128, 7 for 64, 8 for 32)
+  // staging tile per epilogue warp: (hi, lo) float pairs with the float-float
+  // fold (BN <= 128), single floats at BN = 192 (room for a fifth stage, or two
+  // stages of both slices), doubles at BN = 256.  The BN = 256 kernel spills
+  // and keeps its spills in L1: enlarging its shared memory (a fourth stage)
+  // measured 1.14 -> 0.88 PFLOP/s, so it keeps three stages.
+  static constexpr uint32_t kStgElem = BN == 192 ? 4u : 8u;
+  static constexpr uint32_t kStgBytes = kEpiWarps * 32 * kStgLd * kStgElem;
+  // as many stages as fit in 227 KB next to the staging tile and barriers (one
+  // pair per stage: 3 for BN = 256, 5 for 192 and 128, 7 for 64, 8 for 32; both
+  // slices per stage: 2 for BN = 128 and 192)
   static constexpr int kStagesFit = static_cast<int>((232448u - 1024u - 256u - kStgBytes) / kStageBytes);
   static constexpr int kStages = kStagesFit > 8 ? 8 : kStagesFit;
+  static_assert(kStages >= 2, "at least two pipeline stages");
+  static_assert(SPS == 1 || !CTA2, "CTA pairs stage one slice pair");
   static constexpr uint32_t kSmem = 1024 + kStages * kStageBytes + kStgBytes + 256;
   // BN <= 128: two accumulators [0, 2 BN) + float-float words [2 BN, 4 BN);
   // BN = 256: the two accumulators fill TMEM and the chunks of a tile sum in
@@ -347,11 +362,11 @@ struct TcCfg {
   static constexpr int kCols = BN / (kEpiWarps / 4);                // columns per epilogue thread
 };
 
-template <int BN, bool CTA2>
-__global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
+template <int BN, bool CTA2, int SPS>
+__global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const GemmTcArgs g) {
-  using Cfg = TcCfg<BN, CTA2>;
+  using Cfg = TcCfg<BN, CTA2, SPS>;
   // CTA pair: rank 0 (leader) issues the MMAs for the 256-row tile; rank r
   // owns rows [128 r, 128 r + 128) of it and B rows [r BN/2, (r+1) BN/2)
   constexpr int BMP = CTA2 ? 2 * BM : BM;
@@ -365,9 +380,9 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
   uint8_t* sA = smem;
-  uint8_t* sB = smem + S * Cfg::kABytes;
-  double* stg_all = reinterpret_cast<double*>(sB + S * Cfg::kBBytes);
-  uint64_t* full = reinterpret_cast<uint64_t*>(sB + S * Cfg::kBBytes + Cfg::kStgBytes);
+  uint8_t* sB = smem + S * Cfg::kAStage;
+  double* stg_all = reinterpret_cast<double*>(sB + S * Cfg::kBStage);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + S * Cfg::kBStage + Cfg::kStgBytes);
   constexpr int kEpiWarps = Cfg::kEpiWarps;
   constexpr int kEpiWarp0 = Cfg::kEpiWarp0;
   uint64_t* empty = full + S;
@@ -394,7 +409,7 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
     m0 = (mn / ntn) * BMP + static_cast<int>(rank) * BM;
     kb0 = split * kb_per_split;
     const int nkb = kblocks - kb0 < kb_per_split ? kblocks - kb0 : kb_per_split;
-    n_iter = nkb * g.npairs;
+    n_iter = SPS == 1 ? nkb * g.npairs : nkb;
   };
 
   if (threadIdx.x == 0) {
@@ -444,14 +459,22 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
             // the leader's full barrier counts the bytes of both CTAs
             const uint32_t bar = full0 + static_cast<uint32_t>(s) * 8u;
             if (leader) mbar_expect_tx(&full[s], 2 * Cfg::kStageBytes);
-            tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kABytes, kb * BK, m0, g.pa[pr]);
-            tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBBytes, kb * BK, nb0, g.pb[pr]);
-          } else {
+            tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kAStage, kb * BK, m0, g.pa[pr]);
+            tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBStage, kb * BK, nb0, g.pb[pr]);
+          } else if constexpr (SPS == 1) {
             mbar_expect_tx(&full[s], Cfg::kStageBytes);
-            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kABytes, kb * BK, m0, g.pa[pr]);
-            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBBytes, kb * BK, nb0, g.pb[pr]);
+            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage, kb * BK, m0, g.pa[pr]);
+            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage, kb * BK, nb0, g.pb[pr]);
+          } else {
+            // every slice of A and B of this k-block
+            mbar_expect_tx(&full[s], Cfg::kStageBytes);
+#pragma unroll
+            for (int j = 0; j < SPS; ++j) {
+              tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage + j * Cfg::kABytes, kb * BK, m0, j);
+              tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage + j * Cfg::kBBytes, kb * BK, nb0, j);
+            }
           }
-          if (++pr == g.npairs) {
+          if (SPS > 1 || ++pr == g.npairs) {
             pr = 0;
             ++kb;
           }
@@ -498,14 +521,29 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
             break;
           }
           tc_fence_after();
-          const uint64_t ad = adesc0 + ((static_cast<uint64_t>(s) * Cfg::kABytes) >> 4);
-          const uint64_t bd = bdesc0 + ((static_cast<uint64_t>(s) * Cfg::kBBytes) >> 4);
           const uint32_t d = tmem + b * BN;
+          if constexpr (SPS == 1) {
+            const uint64_t ad = adesc0 + ((static_cast<uint64_t>(s) * Cfg::kAStage) >> 4);
+            const uint64_t bd = bdesc0 + ((static_cast<uint64_t>(s) * Cfg::kBStage) >> 4);
 #pragma unroll
-          for (int k = 0; k < BK / 16; ++k) {
-            const uint32_t acc = (pos > 0 || k > 0) ? 1u : 0u;
-            if constexpr (CTA2) mma_bf16_pair(d, ad + 2 * k, bd + 2 * k, idesc, acc);
-            else mma_bf16(d, ad + 2 * k, bd + 2 * k, idesc, acc);
+            for (int k = 0; k < BK / 16; ++k) {
+              const uint32_t acc = (pos > 0 || k > 0) ? 1u : 0u;
+              if constexpr (CTA2) mma_bf16_pair(d, ad + 2 * k, bd + 2 * k, idesc, acc);
+              else mma_bf16(d, ad + 2 * k, bd + 2 * k, idesc, acc);
+            }
+          } else {
+            // all slice pairs of the k-block from the one stage
+            for (int q = 0; q < g.npairs; ++q) {
+              const uint64_t ad = adesc0 + ((static_cast<uint64_t>(s) * Cfg::kAStage +
+                                             static_cast<uint64_t>(g.pa[q]) * Cfg::kABytes) >> 4);
+              const uint64_t bd = bdesc0 + ((static_cast<uint64_t>(s) * Cfg::kBStage +
+                                             static_cast<uint64_t>(g.pb[q]) * Cfg::kBBytes) >> 4);
+#pragma unroll
+              for (int k = 0; k < BK / 16; ++k) {
+                const uint32_t acc = (pos > 0 || q > 0 || k > 0) ? 1u : 0u;
+                mma_bf16(d, ad + 2 * k, bd + 2 * k, idesc, acc);
+              }
+            }
           }
           if constexpr (CTA2) mma_commit_pair(&empty[s], 0x3);
           else mma_commit(&empty[s]);
@@ -675,7 +713,9 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
       }
       // stage 32 rows x 16 columns through shared memory, then write with the
       // lanes along N (coalesced when C is contiguous in N)
-      double* stg = stg_all + (warp - kEpiWarp0) * 32 * kStgLd;
+      uint8_t* stg_w = reinterpret_cast<uint8_t*>(stg_all) + (warp - kEpiWarp0) * 32 * kStgLd * Cfg::kStgElem;
+      double* stg = reinterpret_cast<double*>(stg_w);  // float-float variants: read as float2
+      float* stgf = reinterpret_cast<float*>(stg_w);   // FP32 variants
       const int cj = lane & 15;
 #pragma unroll
       for (int j0 = 0; j0 < COLS; j0 += 16) {
@@ -697,6 +737,9 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
 #pragma unroll
           for (int j = 0; j < 16; ++j)
             stg2[lane * kStgLd + j] = make_float2(__uint_as_float(h[j]), __uint_as_float(l[j]));
+        } else if constexpr (Cfg::kStgElem == 4) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) stgf[lane * kStgLd + j] = __uint_as_float(h[j]);
         } else {
 #pragma unroll
           for (int j = 0; j < 16; ++j)
@@ -714,6 +757,8 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
             if constexpr (Cfg::kFold) {
               const float2 hl = reinterpret_cast<const float2*>(stg)[rr * kStgLd + cj];
               P[m * g.Npad] = f2d_exact(hl.x) + f2d_exact(hl.y);
+            } else if constexpr (Cfg::kStgElem == 4) {
+              P[m * g.Npad] = static_cast<double>(stgf[rr * kStgLd + cj]);
             } else {
               P[m * g.Npad] = stg[rr * kStgLd + cj];
             }
@@ -760,7 +805,10 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2>::kThreads, 1)
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
               if (off[r] < 0) continue;
-              const double val = g.alpha * stg[((lane >> 4) + 2 * r) * kStgLd + cj];
+              double sv;
+              if constexpr (Cfg::kStgElem == 4) sv = static_cast<double>(stgf[((lane >> 4) + 2 * r) * kStgLd + cj]);
+              else sv = stg[((lane >> 4) + 2 * r) * kStgLd + cj];
+              const double val = g.alpha * sv;
               g.C[off[r]] = (g.beta == 0.0) ? val : fma(g.beta, cv[r], val);
             }
           }
@@ -813,15 +861,15 @@ bool make_map(CUtensorMap* map, const void* base, int64_t slices, int64_t rows, 
 }
 
 
-template <int BN, bool CTA2>
+template <int BN, bool CTA2, int SPS = 1>
 bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
-  using Cfg = TcCfg<BN, CTA2>;
+  using Cfg = TcCfg<BN, CTA2, SPS>;
   CUtensorMap ma, mb;
   if (!make_map(&ma, g.A, g.a_slices, g.a_rows ? g.a_rows : g.Mpad, g.Kpad, BM)) return false;
   if (!make_map(&mb, g.B, g.b_slices, g.b_rows ? g.b_rows : g.Npad, g.Kpad, Cfg::kBRows)) return false;
   static bool attr_set = false;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(gemm_tc_kernel<BN, CTA2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(gemm_tc_kernel<BN, CTA2, SPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              Cfg::kSmem) != cudaSuccess)
       return false;
     attr_set = true;
@@ -829,7 +877,7 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
   const int64_t units = (g.Npad / BN) * (g.Mpad / (CTA2 ? 2 * BM : BM)) * (g.ksplit > 1 ? g.ksplit : 1);
   if (!CTA2) {
     const int grid = static_cast<int>(units < num_sms() ? units : num_sms());
-    gemm_tc_kernel<BN, false><<<grid, Cfg::kThreads, Cfg::kSmem, st>>>(ma, mb, g);
+    gemm_tc_kernel<BN, false, SPS><<<grid, Cfg::kThreads, Cfg::kSmem, st>>>(ma, mb, g);
     return true;
   }
   cudaLaunchConfig_t cfg = {};
@@ -847,7 +895,7 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
   if (!max_pairs) {
     cfg.gridDim = dim3(2 * (num_sms() / 2));
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, gemm_tc_kernel<BN, true>, &cfg) != cudaSuccess || n < 1) {
+    if (cudaOccupancyMaxActiveClusters(&n, gemm_tc_kernel<BN, true, 1>, &cfg) != cudaSuccess || n < 1) {
       cudaGetLastError();
       n = num_sms() / 2;
     }
@@ -855,7 +903,7 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
   }
   const int64_t pairs = units < max_pairs ? units : max_pairs;
   cfg.gridDim = dim3(static_cast<unsigned>(2 * pairs));
-  return cudaLaunchKernelEx(&cfg, gemm_tc_kernel<BN, true>, ma, mb, g) == cudaSuccess;
+  return cudaLaunchKernelEx(&cfg, gemm_tc_kernel<BN, true, 1>, ma, mb, g) == cudaSuccess;
 }
 
 }  // namespace
@@ -905,6 +953,22 @@ bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
     switch (g.bn) {
       case 64: return launch_bn<64, true>(g, st);
       case 128: return launch_bn<128, true>(g, st);
+      default: return false;
+    }
+  }
+  if (g.sps == 2) {
+    // both slices per stage: two slices, every pair (p, q) with p, q < 2
+    if (g.a_slices != 2 || g.b_slices != 2) return false;
+    for (int q = 0; q < g.npairs; ++q)
+      if (g.pa[q] > 1 || g.pb[q] > 1) return false;
+    // one TMEM accumulation spans the same number of MMAs as with one pair
+    // per stage: chunk counts stages
+    GemmTcArgs h = g;
+    h.chunk = std::max(1, (g.chunk > 0 ? g.chunk : 4) / g.npairs);
+    switch (g.bn) {
+      case 64: return launch_bn<64, false, 2>(h, st);
+      case 128: return launch_bn<128, false, 2>(h, st);
+      case 192: return launch_bn<192, false, 2>(h, st);
       default: return false;
     }
   }

@@ -406,6 +406,39 @@ __global__ void __launch_bounds__(kThreads) jacobi_inplace_kernel(int64_t o, int
     t1[e] += r1[e] / (eps_o[e % o] - eps_v[e / o]);
 }
 
+// out[0] = max |t2(a,b,i,j) - t2(b,a,j,i)|, out[1] = max |t2| (out zeroed by
+// the caller), maxima combined as in maxabs_diff_kernel
+__global__ void __launch_bounds__(kThreads) pair_asym_kernel(int64_t o, int64_t v, const double* t2,
+                                                             unsigned long long* out) {
+  __shared__ double sd[kThreads], sb[kThreads];
+  const int64_t o2 = o * o;
+  double md = 0.0, mb = 0.0;
+  for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
+    const int64_t a = p / v, b = p % v;
+    const double* x = t2 + p * o2;
+    const double* y = t2 + (b * v + a) * o2;
+    for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
+      const int64_t i = ij / o, j = ij % o;
+      md = fmax(md, fabs(x[ij] - y[j * o + i]));
+      mb = fmax(mb, fabs(x[ij]));
+    }
+  }
+  sd[threadIdx.x] = md;
+  sb[threadIdx.x] = mb;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sd[threadIdx.x] = fmax(sd[threadIdx.x], sd[threadIdx.x + w]);
+      sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(sd[0])));
+    atomicMax(out + 1, static_cast<unsigned long long>(__double_as_longlong(sb[0])));
+  }
+}
+
 // out[0] = max |a - b|, out[1] = max |b| (out zeroed by the caller): block
 // maxima combined with atomicMax on the bit patterns, which order like the
 // values for non-negative doubles
@@ -740,6 +773,10 @@ void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, con
 void launch_jacobi_inplace(int64_t o, int64_t v, const double* eps_o, const double* eps_v, const double* r1,
                            const double* r2, double* t1, double* t2, cudaStream_t st) {
   jacobi_inplace_kernel<<<grid_for(v * v, 1), kThreads, 0, st>>>(o, v, eps_o, eps_v, r1, r2, t1, t2);
+}
+
+void launch_pair_asym(int64_t o, int64_t v, const double* t2, unsigned long long* out, cudaStream_t st) {
+  pair_asym_kernel<<<grid_for(v * v, 1), kThreads, 0, st>>>(o, v, t2, out);
 }
 
 void launch_maxabs_diff(int64_t n, const double* a, const double* b, unsigned long long* out, cudaStream_t st) {

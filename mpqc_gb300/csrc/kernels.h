@@ -118,6 +118,9 @@ struct GemmTcArgs {
   // rows per slice of the A / B panels as stored (0: Mpad / Npad); a panel may
   // hold more rows than the launch covers (padded for every candidate tile)
   int64_t a_rows, b_rows;
+  // slices per pipeline stage: 0 or 1, one (A, B) slice pair per stage; 2, both
+  // slices of A and B of a k-block per stage (2 slices, bn 64 / 128 / 192)
+  int sps;
 };
 // Deterministic K-split reduction: C[cm[m] + cn[n]] = beta*C + alpha * sum_s
 // partial[s][m][n] (splits summed in order), partial rows of length ldp and
@@ -163,6 +166,10 @@ void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, con
 // t1 += r1 / D1, t2 += r2 / D2 in place
 void launch_jacobi_inplace(int64_t o, int64_t v, const double* eps_o, const double* eps_v, const double* r1,
                            const double* r2, double* t1, double* t2, cudaStream_t st);
+
+// out[0] = bits of max|t2(a,b,i,j) - t2(b,a,j,i)|, out[1] = bits of max|t2|;
+// out must be zeroed first
+void launch_pair_asym(int64_t o, int64_t v, const double* t2, unsigned long long* out, cudaStream_t st);
 
 // out[0] = bits of max|a - b|, out[1] = bits of max|b|; out must be zeroed first
 void launch_maxabs_diff(int64_t n, const double* a, const double* b, unsigned long long* out, cudaStream_t st);

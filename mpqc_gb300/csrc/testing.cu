@@ -34,6 +34,12 @@ extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* 
 extern "C" int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
                                     double* Cout, int slices, int ksplit, int bn_req, int cta2, int chunk,
                                     int fold, int repeat, float* ms) {
+  return gbcc_testing_gemm_ex2(M, N, K, A, B, Cout, slices, ksplit, bn_req, cta2, chunk, fold, 1, repeat, ms);
+}
+
+extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
+                                     double* Cout, int slices, int ksplit, int bn_req, int cta2, int chunk,
+                                     int fold, int sps, int repeat, float* ms) {
   using namespace gbcc;
   if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1 || ksplit < 1)
     return GBCC_ERR_INVALID_ARG;
@@ -111,6 +117,7 @@ extern "C" int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const doubl
       t.cta2 = cta2 ? 1 : 0;
       t.chunk = chunk;
       t.fold = fold;
+      t.sps = sps;
       if (ksplit > 1) {
         const int64_t kblocks = Kpad / kTcBK;
         t.kb_per_split = static_cast<int>((kblocks + ksplit - 1) / ksplit);

@@ -105,3 +105,29 @@ def test_gemm_kernel_variants(tlib, M, N, K, ksplit, bn, cta2, chunk, fold):
     # FP32 accumulation of the chunks (bn 256) grows like sqrt(number of chunks)
     tol = TOL[3] + 8 * 2.0**-24 * np.sqrt(K)
     assert np.max(np.abs(out - ref)) <= tol * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("bn", [64, 128, 192])
+@pytest.mark.parametrize("M,N,K,ksplit", [(256, 256, 64, 1), (300, 520, 1000, 1), (260, 528, 1500, 1),
+                                          (700, 300, 2000, 3)])
+def test_gemm_both_slices_per_stage(tlib, M, N, K, ksplit, bn):
+    """Two slices staged together (one stage per k-block feeding all three pair
+    products) against FP64: the same sums as one pair per stage."""
+    rng = np.random.default_rng(M + N + K + bn + 7)
+    A = rng.normal(size=(M, K))
+    B = rng.normal(size=(N, K))
+    ref = A @ B.T
+    out = np.empty((M, N))
+    out1 = np.empty((M, N))
+    ms = C.c_float()
+    tlib.gbcc_testing_gemm_ex2.restype = C.c_int
+    tlib.gbcc_testing_gemm_ex2.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p] + \
+        [C.c_int] * 8 + [C.POINTER(C.c_float)]
+    st = tlib.gbcc_testing_gemm_ex2(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, 2, ksplit, bn, 0, 0, 0,
+                                    2, 1, C.byref(ms))
+    st1 = tlib.gbcc_testing_gemm_ex2(M, N, K, A.ctypes.data, B.ctypes.data, out1.ctypes.data, 2, ksplit, bn, 0, 0,
+                                     0, 1, 1, C.byref(ms))
+    assert st == 0 and st1 == 0
+    tol = TOL[2] + 8 * 2.0**-24 * np.sqrt(K)
+    assert np.max(np.abs(out - ref)) <= tol * np.max(np.abs(ref))
+    assert np.max(np.abs(out - out1)) <= 2 * tol * np.max(np.abs(ref))

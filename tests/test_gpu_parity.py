@@ -215,3 +215,17 @@ def test_autotuned_tiles_give_the_same_residual():
     assert rel_err(a2, b2) < 1e-9 and rel_err(a1, b1) < 1e-9
     tc = [p for p in prof if p["pairs"] > 0]
     assert tc and all(p["bn"] in (32, 64, 128, 192, 256) and p["ksplit"] >= 1 for p in tc)
+
+
+def test_residual_rejects_amplitudes_without_pair_symmetry():
+    from mpqc_gb300._lib import GbccError
+    inp = synth.make_inputs(4, 10, 12, seed=71, t1_scale=1e-2)
+    bad = inp.t2.copy()
+    bad[1, 2, 0, 3] += 1e-6
+    with _solver(inp) as s:
+        s.residual(inp.t1, inp.t2)
+        with pytest.raises(GbccError) as e:
+            s.residual(inp.t1, bad)
+        assert e.value.status == 1 and "pair-symmetric" in str(e.value)
+        r1, r2 = s.residual(inp.t1, inp.t2)   # the handle stays usable
+    assert np.all(np.isfinite(r2))
