@@ -261,7 +261,7 @@ def ours(args):
     F = flop_count(o, v)
     log(f"[bench] rank {rank}: building inputs o={o} v={v} naux={naux} on {torch.cuda.get_device_name(dev)}")
     t_setup = time.perf_counter()
-    s = Solver(o, v, precision="mixed", slices=(args.slices,) * 3, device=local)
+    s = Solver(o, v, precision="mixed", slices=(args.slices,) * 3, autotune=not args.no_autotune, device=local)
     t1, t2 = build_inputs(torch, s, o, v, naux, args.seed, dev,
                           b_scale=0.05 if args.b_scale is None else args.b_scale)
     log(f"[bench] inputs + split packing ready in {time.perf_counter() - t_setup:.1f} s")
@@ -279,7 +279,9 @@ def ours(args):
 
     if args.residual_only:
         # profiling driver: warmup + steps mixed residuals and nothing else;
-        # reports which tensor-core GEMM launch of a residual is the ladder
+        # reports which tensor-core GEMM launch of a residual is the ladder and
+        # how many tensor-core launches (calibration, tuning) came before
+        tc_before = s.tc_launches_total()
         for _ in range(args.warmup + args.steps):
             s.residual(t1, t2, r1, r2, precision="mixed")
         torch.cuda.synchronize()
@@ -292,6 +294,8 @@ def ours(args):
             print(json.dumps({"residual_only": True, "o": o, "v": v, "naux": naux,
                               "tc_launches_per_residual": len(tc), "ladder_tc_ordinal": ordinal,
                               "launches_per_residual": launches,
+                              "tc_launches_before_first_residual": tc_before,
+                              "ladder_ncu_skip": tc_before + ordinal,
                               "tc_sites_mnk_class": [[p["M"], p["N"], p["K"], p["cls"]] for p in tc]}),
                   flush=True)
         return 0
@@ -342,7 +346,7 @@ def ours(args):
         peak = pk.get("bf16_tflops_sustained") or 1700.0
         ach = executed / (lp["gemm_ms"] * 1e-3) / 1e12
         roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "traffic": ncu_traffic(), "kernel": "gemm_tc_kernel (particle-particle ladder)",
+                "traffic": ncu_traffic(), "kernel": "gemm_tc_kernel (particle-particle ladder, G+ tau+ pair products)",
                 "executed_flops_per_launch": executed, "launch_ms": lp["gemm_ms"],
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"}
     terms = {}
@@ -466,6 +470,8 @@ def main():
                     help="BF16 slices per operand for every class; 0 (default): chosen per class "
                          "from the measured residual error")
     ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default tile per contraction (fewer launches before the first residual)")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--residual-only", action="store_true",

@@ -34,6 +34,11 @@ int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const double* A, const
  * (host), the bit patterns of slices s = 0..nslices-1 (nslices 1..3). */
 int gbcc_testing_split(const double* x, int64_t n, int nslices, uint16_t* out);
 
+/* out[i] = coef * x[i] (host arrays) as the packing kernels scale a term of a
+ * linear combination: exponent arithmetic for coef = +-2^k, an FP64 multiply
+ * otherwise.  Must equal the IEEE product bit for bit. */
+int gbcc_testing_scale(const double* x, int64_t n, double coef, double* out);
+
 /* As gbcc_testing_gemm_ex with the number of slices per pipeline stage:
  * sps = 1, one (A, B) slice pair per stage; 2, both slices of a k-block per
  * stage (slices = 2, bn 64 / 128 / 192). */
@@ -56,6 +61,10 @@ int gbcc_testing_fp64_peak(double* gflops);
 struct gbcc_handle;
 int gbcc_testing_profile_residual(struct gbcc_handle* h, int precision, int max_sites, double* ms,
                                   double* flops, int* pairs, int* cls, int* nsites);
+
+/* Tensor-core GEMM launches of handle h since its creation, slice
+ * calibration and tile tuning included (for choosing an ncu launch to skip to). */
+int gbcc_testing_tc_launches_total(gbcc_handle* h, int64_t* launches);
 
 /* Kernel launches of the last residual (every kernel of this library). */
 int gbcc_testing_last_launches(struct gbcc_handle* h, int* launches);

@@ -28,10 +28,10 @@ EXPORTS = (
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error",
 )
 # test hooks of include/gbcc_testing.h
-TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_split", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
+TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims",
-                   "gbcc_testing_profile_tiles")
+                   "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total")
 
 
 class Config(C.Structure):
@@ -101,6 +101,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         [C.POINTER(C.c_float)]
     lib.gbcc_testing_split.restype = C.c_int
     lib.gbcc_testing_split.argtypes = [vp, C.c_int64, C.c_int, vp]
+    lib.gbcc_testing_scale.restype = C.c_int
+    lib.gbcc_testing_scale.argtypes = [vp, C.c_int64, C.c_double, vp]
     lib.gbcc_testing_fp64_peak.restype = C.c_int
     lib.gbcc_testing_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     ip = C.POINTER(C.c_int)
@@ -116,6 +118,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_testing_profile_gemm_ms.argtypes = [vp, C.c_int, dp]
     lib.gbcc_testing_profile_dims.restype = C.c_int
     lib.gbcc_testing_profile_dims.argtypes = [vp, C.c_int, C.POINTER(C.c_int64)]
+    lib.gbcc_testing_tc_launches_total.restype = C.c_int
+    lib.gbcc_testing_tc_launches_total.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.gbcc_testing_profile_tiles.restype = C.c_int
     lib.gbcc_testing_profile_tiles.argtypes = [vp, C.c_int, C.POINTER(C.c_int32)]
     lib.gbcc_residual.restype = C.c_int

@@ -163,6 +163,11 @@ class Solver:
                      sps=tl[3 * i + 2])
                 for i in range(min(n.value, max_sites))]
 
+    def tc_launches_total(self):
+        n = C.c_int64()
+        self.lib.gbcc_testing_tc_launches_total(self.h, C.byref(n))
+        return n.value
+
     def record(self, slot):
         _check(self.lib, self.h, self.lib.gbcc_testing_record(self.h, slot))
 

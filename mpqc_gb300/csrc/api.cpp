@@ -838,6 +838,12 @@ int gbcc_testing_elapsed(gbcc_handle* h, int slot0, int slot1, float* ms) {
   });
 }
 
+int gbcc_testing_tc_launches_total(gbcc_handle* h, int64_t* launches) {
+  if (!h || !launches || !h->eng) return GBCC_ERR_INVALID_ARG;
+  *launches = h->eng->gemm_tc_launches_total();
+  return GBCC_OK;
+}
+
 int gbcc_testing_last_launches(gbcc_handle* h, int* launches) {
   if (!h || !launches) return GBCC_ERR_INVALID_ARG;
   *launches = h->last_launches;

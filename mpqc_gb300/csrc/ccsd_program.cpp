@@ -9,11 +9,21 @@
 // Gijab[i][j][a][b], ...); a label string names the stored dimensions in
 // order, so Giabc("kadc") is <k a|d c> stored as Giabc[k][a][d][c].
 //
-// Two expressions are regrouped to avoid materialising an o v^3 temporary:
-// the reference's (Giabc(i,c,a,b) - Giajb(k,b,i,c) t1(a,k)) t1(c,j) is
-// evaluated as Giabc(i,c,a,b) t1(c,j) - (Giajb(k,b,i,c) t1(c,j)) t1(a,k), and
-// (Gijka(j,i,k,a) + Gijab(i,k,a,c) t1(c,j)) t1(b,k) as two products.  Both are
-// exact rearrangements of the same sums.
+// Some expressions are regrouped; each is an exact rearrangement of the same
+// sums:
+//  - no o v^3 temporary: the reference's (Giabc(i,c,a,b) - Giajb(k,b,i,c)
+//    t1(a,k)) t1(c,j) is Giabc(i,c,a,b) t1(c,j) - (Giajb(k,b,i,c) t1(c,j))
+//    t1(a,k), and (Gijka(j,i,k,a) + Gijab(i,k,a,c) t1(c,j)) t1(b,k) two
+//    products;
+//  - r2 = r2u(a,b,i,j) + r2u(b,a,j,i) + ..., so a term X(a,b,i,j) of r2u may be
+//    replaced by X(b,a,j,i).  Done for -Y1(k,b,i,j) t1(a,k), and the ladder's
+//    -tmp2(k,a,j,i) t1(b,k) - tmp2(k,b,i,j) t1(a,k) of r2 becomes one term of
+//    r2u: the four products with t1(b,k) form one contraction;
+//  - r1's (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i) is read off tmp2
+//    (tau(c,d,k,i) = tau(d,c,i,k) for pair-symmetric amplitudes), so tmp2 is
+//    evaluated first;
+//  - h_kc(k,c) (2 t2(c,a,k,i) - t2(c,a,i,k) + t1(c,i) t1(a,k)) is not
+//    materialised: the t1 t1 part is t1(a,k) (h_kc(k,c) t1(c,i)).
 #include "ccsd_program.h"
 
 namespace gbcc {
@@ -41,7 +51,6 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v) {
   FAB = &E.tensor("FAB", {v, v});
   FIJ = &E.tensor("FIJ", {o, o});
   hkc = &E.tensor("hkc", {o, v});
-  X1 = &E.tensor("X1", {v, v, o, o});
   r2u = &E.tensor("r2u", {v, v, o, o});
   Y1 = &E.tensor("Y1", {o, v, o, o});
   Y2 = &E.tensor("Y2", {o, o, v, o});
@@ -84,6 +93,18 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   const Tensor &t1 = *S.t1, &t2 = *S.t2, &tau = *S.tau;
   const Tensor &r1 = *S.r1, &r2 = *S.r2;
   const TermClass O = kClassOther, R = kClassRing, L = kClassLadder;
+  const int64_t v = t1.dim[0], o = t1.dim[1];
+  const bool minus = v > 1 && o > 1;  // otherwise the antisymmetric pair parts are empty
+  const double* tau_d = tau.d;
+  double *taup = S.taup->d, *taum = S.taum->d, *Bp = S.Bp->d, *Bm = S.Bm->d, *Xp = S.Xp->d, *Xm = S.Xm->d;
+  double *r1d = r1.d, *r2d = r2.d, *tmp2 = S.tmp2->d;
+
+  // tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j) (ccsd_r1_r2.h:277) as sums over
+  // c <= d of the pair-(anti)symmetric combinations (kernels.cu), unpacked
+  E.custom([=](cudaStream_t st) { launch_tau_pm(o, v, tau_d, taup, taum, st); }, 1);
+  E.contract(ix(*S.Xp, "RS"), 0.0, 1.0, {{1.0, ix(*S.Gip, "RQ")}}, {{1.0, ix(*S.taup, "QS")}}, R);
+  if (minus) E.contract(ix(*S.Xm, "RZ"), 0.0, 1.0, {{1.0, ix(*S.Gim, "RY")}}, {{1.0, ix(*S.taum, "YZ")}}, R);
+  E.custom([=](cudaStream_t st) { launch_pair_unpack(o, v, o, false, Xp, minus ? Xm : nullptr, 0.0, tmp2, st); }, 1);
 
   // ----- R1 (ccsd_r1_r2.h:70-124) -----
   // r1(a,i) = Fia(i,a) - 2 (Fia(k,c) t1(c,i)) t1(a,k)
@@ -105,15 +126,15 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.assign(ix(*S.hkc, "kc"), 0.0, {f1(1.0, ix(Fia, "kc"))});
   E.contract(ix(*S.hkc, "kc"), 1.0, 1.0, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "lkcd")}},
              {{1.0, ix(t1, "dl")}}, O);
-  E.assign(ix(*S.X1, "caki"), 0.0,
-           {f1(2.0, ix(t2, "caki")), f1(-1.0, ix(t2, "caik")), f2(1.0, ix(t1, "ci"), ix(t1, "ak"))});
-  E.contract(ix(r1, "ai"), 1.0, 1.0, {{1.0, ix(*S.hkc, "kc")}}, {{1.0, ix(*S.X1, "caki")}}, O);
+  // (t2(c,a,i,k) read as t2(a,c,k,i): both terms then run along i in storage)
+  E.contract(ix(r1, "ai"), 1.0, 1.0, {{1.0, ix(*S.hkc, "kc")}}, {{2.0, ix(t2, "caki")}, {-1.0, ix(t2, "acki")}}, O);
+  E.contract(ix(*S.tki, "ki"), 0.0, 1.0, {{1.0, ix(*S.hkc, "kc")}}, {{1.0, ix(t1, "ci")}}, O);
+  E.contract(ix(r1, "ai"), 1.0, 1.0, {{1.0, ix(t1, "ak")}}, {{1.0, ix(*S.tki, "ki")}}, O);
   // r1 += (2 Gijab(k,i,c,a) - Giajb(k,a,i,c)) t1(c,k)
   E.contract(ix(r1, "ai"), 1.0, 1.0, {{2.0, ix(Gijab, "kica")}, {-1.0, ix(Giajb, "kaic")}},
              {{1.0, ix(t1, "ck")}}, O);
-  // r1 += (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i)
-  E.contract(ix(r1, "ai"), 1.0, 1.0, {{2.0, ix(Giabc, "kacd")}, {-1.0, ix(Giabc, "kadc")}},
-             {{1.0, ix(tau, "cdki")}}, O);
+  // r1 += (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i) (:111-114) = 2 tmp2(k,a,k,i) - tmp2(k,a,i,k)
+  E.custom([=](cudaStream_t st) { launch_r1_from_tmp2(o, v, tmp2, r1d, st); }, 1);
   // r1 -= (2 Gijka(l,k,i,c) - Gijka(k,l,i,c)) tau(c,a,k,l)
   E.contract(ix(r1, "ai"), 1.0, -1.0, {{2.0, ix(Gijka, "lkic")}, {-1.0, ix(Gijka, "klic")}},
              {{1.0, ix(tau, "cakl")}}, O);
@@ -121,12 +142,14 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   // ----- R2 (ccsd_r1_r2.h:198-293) -----
   const Tensor& r2u = *S.r2u;
   // permutation part (:206-212)
+  // r2u -= Y1(k,a,j,i) t1(b,k) [image of Y1(k,b,i,j) t1(a,k)] + Gijka(j,i,k,a) t1(b,k)
+  //        + Y2(i,k,a,j) t1(b,k) + tmp2(k,a,j,i) t1(b,k) [the ladder's t1 terms, :278-280]
   E.contract(ix(r2u, "abij"), 0.0, 1.0, {{1.0, ix(Giabc, "icab")}}, {{1.0, ix(t1, "cj")}}, O);
   E.contract(ix(*S.Y1, "kbij"), 0.0, 1.0, {{1.0, ix(Giajb, "kbic")}}, {{1.0, ix(t1, "cj")}}, O);
-  E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(*S.Y1, "kbij")}}, {{1.0, ix(t1, "ak")}}, O);
-  E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(Gijka, "jika")}}, {{1.0, ix(t1, "bk")}}, O);
   E.contract(ix(*S.Y2, "ikaj"), 0.0, 1.0, {{1.0, ix(Gijab, "ikac")}}, {{1.0, ix(t1, "cj")}}, O);
-  E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(*S.Y2, "ikaj")}}, {{1.0, ix(t1, "bk")}}, O);
+  E.contract(ix(r2u, "abij"), 1.0, -1.0,
+             {{1.0, ix(*S.Y1, "kaji")}, {1.0, ix(Gijka, "jika")}, {1.0, ix(*S.Y2, "ikaj")}, {1.0, ix(*S.tmp2, "kaji")}},
+             {{1.0, ix(t1, "bk")}}, O);
   // g_ki = F_OO(FIJ, Fia, gbar_ijka, t1), gbar_ijka(k,l,i,c) = 2 Gijka(k,l,i,c) - Gijka(l,k,i,c)
   E.assign(ix(*S.gki, "ki"), 0.0, {f1(1.0, ix(*S.FIJ, "ki"))});
   E.contract(ix(*S.gki, "ki"), 1.0, 1.0, {{1.0, ix(Fia, "kc")}}, {{1.0, ix(t1, "ci")}}, O);
@@ -161,8 +184,9 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.contract(ix(*S.tmp, "abij"), 0.0, 1.0, {{1.0, ix(K, "kaic")}}, {{1.0, ix(t2, "cbjk")}}, R);
   E.assign(ix(r2u, "abij"), 1.0, {f1(-0.5, ix(*S.tmp, "abij")), f1(-1.0, ix(*S.tmp, "baij"))});
   // r2(a,b,i,j) = r2(a,b,i,j) + r2(b,a,j,i) + Gijab(i,j,a,b)   (:260-262)
+  // (g_abij(a,b,i,j) = Gijab(i,j,a,b), stored in r2's order)
   E.assign(ix(r2, "abij"), 0.0,
-           {f1(1.0, ix(r2u, "abij")), f1(1.0, ix(r2u, "baji")), f1(1.0, ix(Gijab, "ijab"))});
+           {f1(1.0, ix(r2u, "abij")), f1(1.0, ix(r2u, "baji")), f1(1.0, ix(*S.g_abij, "abij"))});
   // hole-hole ladder: W_oooo (intermediates :182-193), r2 += W(k,l,i,j) tau(a,b,k,l)
   const Tensor& W = *S.W;
   E.assign(ix(W, "klij"), 0.0, {f1(1.0, ix(Gijkl, "klij"))});
@@ -170,26 +194,11 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijka, "lkjc")}}, {{1.0, ix(t1, "ci")}}, O);
   E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijab, "klcd")}}, {{1.0, ix(tau, "cdij")}}, O);
   E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(W, "klij")}}, {{1.0, ix(tau, "abkl")}}, O);
-  // particle-particle ladder (:272-280): r2 += tau(c,d,i,j) Gabcd(a,b,c,d) and
-  // tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j), both as sums over c <= d of the
-  // pair-(anti)symmetric combinations (kernels.cu), unpacked into r2 / tmp2
-  {
-    const int64_t v = t1.dim[0], o = t1.dim[1];
-    const bool minus = v > 1 && o > 1;  // otherwise the antisymmetric parts are empty
-    const double* tau_d = tau.d;
-    double *taup = S.taup->d, *taum = S.taum->d, *Bp = S.Bp->d, *Bm = S.Bm->d, *Xp = S.Xp->d, *Xm = S.Xm->d;
-    double *r2d = r2.d, *tmp2 = S.tmp2->d;
-    E.custom([=](cudaStream_t st) { launch_tau_pm(o, v, tau_d, taup, taum, st); }, 1);
-    E.contract(ix(*S.Bp, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
-    if (minus) E.contract(ix(*S.Bm, "XZ"), 0.0, 1.0, {{1.0, ix(*S.Gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);
-    E.custom([=](cudaStream_t st) { launch_pair_unpack(v, v, o, true, Bp, minus ? Bm : nullptr, 1.0, r2d, st); }, 1);
-    E.contract(ix(*S.Xp, "RS"), 0.0, 1.0, {{1.0, ix(*S.Gip, "RQ")}}, {{1.0, ix(*S.taup, "QS")}}, R);
-    if (minus) E.contract(ix(*S.Xm, "RZ"), 0.0, 1.0, {{1.0, ix(*S.Gim, "RY")}}, {{1.0, ix(*S.taum, "YZ")}}, R);
-    E.custom([=](cudaStream_t st) { launch_pair_unpack(o, v, o, false, Xp, minus ? Xm : nullptr, 0.0, tmp2, st); },
-             1);
-  }
-  E.contract(ix(r2, "abij"), 1.0, -1.0, {{1.0, ix(*S.tmp2, "kaji")}}, {{1.0, ix(t1, "bk")}}, O);
-  E.contract(ix(r2, "abij"), 1.0, -1.0, {{1.0, ix(*S.tmp2, "kbij")}}, {{1.0, ix(t1, "ak")}}, O);
+  // particle-particle ladder (:275, :289): r2 += tau(c,d,i,j) Gabcd(a,b,c,d) as sums
+  // over c <= d of the pair-(anti)symmetric combinations (taup / taum from above)
+  E.contract(ix(*S.Bp, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
+  if (minus) E.contract(ix(*S.Bm, "XZ"), 0.0, 1.0, {{1.0, ix(*S.Gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);
+  E.custom([=](cudaStream_t st) { launch_pair_unpack(v, v, o, true, Bp, minus ? Bm : nullptr, 1.0, r2d, st); }, 1);
 }
 
 }  // namespace gbcc

@@ -388,13 +388,14 @@ void Engine::assign(const Ix& c, double beta, const std::vector<Factor>& terms) 
   g.nterms = static_cast<int>(terms.size());
   for (size_t t = 0; t < terms.size(); ++t) {
     GatherTerm& T = g.t[t];
-    T.coef = terms[t].coef;
+    gather_set_coef(T, terms[t].coef);
     T.a = terms[t].a.t->d;
     const std::vector<int64_t> hra = offsets(rlab, e, terms[t].a), hca = offsets(clab, e, terms[t].a);
     if (t == 0) g.transpose = pick_transpose(hra, hca);
     T.ra = upload(hra).d;
     T.ca = upload(hca).d;
     if (terms[t].b.t) {
+      g.products = 1;
       T.b = terms[t].b.t->d;
       T.rb = upload(offsets(rlab, e, terms[t].b)).d;
       T.cb = upload(offsets(clab, e, terms[t].b)).d;
@@ -405,6 +406,7 @@ void Engine::assign(const Ix& c, double beta, const std::vector<Factor>& terms) 
   g.out = c.t->d;
   g.ldo = g.C;
   g.beta = beta;
+  gather_finish(g);
 }
 
 // ---------------------------------------------------------------------------
@@ -484,6 +486,7 @@ GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* cons
 void Engine::launch_tc(const GemmPlan& p, const GemmTcArgs& t) {
   if (!launch_gemm_tc(t, stream_)) throw Error(GBCC_ERR_CUDA, "tcgen05 GEMM launch rejected (tensor map or size)");
   ++n_tc_;
+  ++tc_total_;
   ++n_launch_;
   if (p.ksplit > 1) {
     launch_splitk_reduce(p.M, p.N, p.ksplit, wpart_, t.Mpad, t.Npad, p.C, p.cm, p.cn, p.alpha, p.beta, stream_);
@@ -523,6 +526,7 @@ void Engine::autotune(int reps) {
       q.sps = p.cand_sps[c];
       const GemmTcArgs t = tc_args(q, sp->cls, panel);
       if (!launch_gemm_tc(t, stream_)) continue;
+      ++tc_total_;
       if (q.ksplit > 1)
         launch_splitk_reduce(q.M, q.N, q.ksplit, wpart_, t.Mpad, t.Npad, q.C, q.cm, q.cn, q.alpha, q.beta, stream_);
       GBCC_CK(cudaEventRecord(e0, stream_));
@@ -735,13 +739,19 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       if (single) coef_direct *= op.terms[0].coef;
       g.plain = single ? 1 : 0;
       for (size_t t = 0; t < op.terms.size(); ++t) {
-        g.t[t].coef = single ? 1.0 : op.terms[t].coef;
+        gather_set_coef(g.t[t], single ? 1.0 : op.terms[t].coef);
         g.t[t].a = op.terms[t].x.t->d;
         const std::vector<int64_t> hra = offsets(op.ext, e, op.terms[t].x), hca = offsets(op.kord, e, op.terms[t].x);
         if (t == 0) g.transpose = pick_transpose(hra, hca);
+        if (single) {
+          bool unit = reinterpret_cast<uintptr_t>(g.t[t].a) % 16 == 0;
+          for (size_t q = 0; unit && q < hca.size(); ++q) unit = hca[q] == static_cast<int64_t>(q);
+          g.cunit = unit ? 1 : 0;
+        }
         g.t[t].ra = upload(hra).d;
         g.t[t].ca = upload(hca).d;
       }
+      gather_finish(g);
       g.R = op.rows;
       g.C = op.K;
       if (!p.use_tc) {

@@ -173,6 +173,8 @@ class Engine {
   double flops() const { return flops_; }
   size_t device_bytes() const { return bytes_; }
   int gemm_tc_launches() const { return n_tc_; }
+  // tensor-core GEMM launches since the engine was created (tuning included)
+  int64_t gemm_tc_launches_total() const { return tc_total_; }
   int kernel_launches() const { return n_launch_; }
 
  private:
@@ -211,6 +213,7 @@ class Engine {
   double flops_ = 0.0;
   size_t bytes_ = 0;
   int n_tc_ = 0;
+  int64_t tc_total_ = 0;
   int n_launch_ = 0;
 };
 

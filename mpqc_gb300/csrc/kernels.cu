@@ -23,6 +23,17 @@ inline unsigned grid_for(int64_t n, int threads, int64_t cap = 152 * 32) {
   return static_cast<unsigned>(b);
 }
 
+// q = x / d and r = x % d for 0 <= x, d < 2^32 (every index split in these
+// kernels: x < v^2, v o, o^2).  32-bit division is a few integer and FP32
+// instructions; 64-bit integer division is a long sequence that also occupies
+// the FP64 pipe, which measurably slowed the elementwise kernels.
+__device__ __forceinline__ void divmod32(int64_t x, int64_t d, int64_t& q, int64_t& r) {
+  const unsigned xx = static_cast<unsigned>(x), dd = static_cast<unsigned>(d);
+  const unsigned qq = xx / dd;
+  q = qq;
+  r = xx - qq * dd;
+}
+
 // BF16 bits of a finite float, rounded to nearest even (integer operations only)
 __device__ __forceinline__ unsigned bf16_rne(float f) {
   const unsigned b = __float_as_uint(f);
@@ -87,83 +98,236 @@ __device__ __forceinline__ void split_store(double x, __nv_bfloat16* out, int ns
   for (int s = 0; s < nslices; ++s) out[s * slice_stride + idx] = __ushort_as_bfloat16(b[s]);
 }
 
-// value of one packed element: a single unscaled term is a plain load (its
-// coefficient was folded into the GEMM's alpha), otherwise an FP64 sum
+// GB300 executes FP64 at about 2 operations per clock per SM, so an elementwise
+// pass that spends two FP64 instructions per 8-byte element is bound by the
+// FP64 pipe rather than by HBM.  Scaling by a power of two and changing a sign
+// are therefore done on the bit pattern (integer pipes); only the sums of terms
+// use FP64 adds.
+
+// Magnitude bits of |x| 2^k for the magnitude bits m of a finite nonzero x
+// whose scaled exponent leaves the normal range or that is subnormal (the
+// rare case of scale_pow2), in integer arithmetic: IEEE round to nearest even
+// for results below the normal range, infinity above it.
+__device__ __forceinline__ unsigned long long scale_pow2_rare(unsigned long long m, int k) {
+  const int e = static_cast<int>(m >> 52);
+  // significand s and exponent q with |x| = s 2^(q - 1074), s < 2^53
+  unsigned long long s = e ? ((m & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : m;
+  int q = (e ? e - 1 : 0) + k;
+  // normalise so that bit 52 of s is set (subnormal inputs)
+  const int lz = __clzll(static_cast<long long>(s)) - 11;  // leading zeros within 53 bits
+  s <<= lz;
+  q -= lz;
+  if (q >= 0x7FE) return 0x7FFull << 52;                    // overflow: infinity
+  if (q >= 0) return (static_cast<unsigned long long>(q + 1) << 52) | (s & 0xFFFFFFFFFFFFFull);
+  // subnormal result: s 2^q in units of 2^-1074, shift right by -q with RNE
+  const int sh = -q;
+  if (sh > 54) return 0ull;
+  const unsigned long long r = s >> sh, rem = s & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  return r + ((rem > half || (rem == half && (r & 1ull))) ? 1ull : 0ull);
+}
+
+// x * 2^k (|k| <= 64) on the bit pattern, exact as the IEEE product: the
+// exponent field shifts when x is normal and the result stays normal; zeros,
+// infinities and NaN pass through; the rest goes to scale_pow2_rare.  No FP64
+// instruction is issued.
+__device__ __forceinline__ double scale_pow2(double x, int k) {
+  // common case on the high word: exponent field (bits 20-30) + k
+  const int hi = __double2hiint(x);
+  const int e = (hi >> 20) & 0x7FF;
+  const int ek = e + k;
+  if (e != 0 && e != 0x7FF && ek >= 1 && ek <= 0x7FE) return __hiloint2double(hi + k * (1 << 20), __double2loint(x));
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+  const unsigned long long m = b & 0x7FFFFFFFFFFFFFFFull;
+  if (m == 0ull || e == 0x7FF) return x;
+  return __longlong_as_double(static_cast<long long>((b & 0x8000000000000000ull) | scale_pow2_rare(m, k)));
+}
+
+// -x when neg (sign bit flip), x otherwise
+__device__ __forceinline__ double flip_sign(double x, bool neg) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (neg ? static_cast<long long>(1ull << 63) : 0ll));
+}
+
+// coef * x for one gather term whose coefficient is +-2^k (GatherTerm.pow2)
+__device__ __forceinline__ double term_scale(const GatherTerm& T, double x) {
+  return flip_sign(scale_pow2(x, T.pow2_k), T.pow2_sign != 0ull);
+}
+
+// Value of one packed element from NT terms: NT = 0 is a plain load (a single
+// unscaled term whose coefficient was folded into the GEMM's alpha), otherwise
+// the sum of the scaled terms, one FP64 add per term after the first.  PROD:
+// some terms carry a second factor.  The term count, PROD and the
+// read-modify-write of the output are template parameters, dispatched once per
+// launch: as runtime conditions inside the element loop the compiler
+// if-converts them, and the predicated FP64 instructions still occupy the FP64
+// pipe.
+// NT = -1: any coefficients (GatherArgs.general), an FP64 multiply-add per term.
+template <int NT, bool PROD>
 __device__ __forceinline__ double gather_value(const GatherArgs& g, int64_t r, int64_t c) {
-  if (g.plain) return g.t[0].a[g.t[0].ra[r] + g.t[0].ca[c]];
-  double val = 0.0;
-#pragma unroll
-  for (int t = 0; t < kMaxTerms; ++t) {
-    if (t < g.nterms) {
+  if constexpr (NT == 0) {
+    return g.t[0].a[g.t[0].ra[r] + g.t[0].ca[c]];
+  } else if constexpr (NT < 0) {
+    double val = 0.0;
+    for (int t = 0; t < g.nterms; ++t) {
       const GatherTerm& T = g.t[t];
       double x = T.a[T.ra[r] + T.ca[c]];
       if (T.b) x *= T.b[T.rb[r] + T.cb[c]];
       val = fma(T.coef, x, val);
     }
+    return val;
+  } else {
+    double x[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const GatherTerm& T = g.t[t];
+      x[t] = T.a[T.ra[r] + T.ca[c]];
+      if constexpr (PROD) {
+        if (T.b) x[t] *= T.b[T.rb[r] + T.cb[c]];
+      }
+    }
+    double val = term_scale(g.t[0], x[0]);
+#pragma unroll
+    for (int t = 1; t < NT; ++t) val += term_scale(g.t[t], x[t]);
+    return val;
   }
-  return val;
 }
 
-__global__ void __launch_bounds__(kThreads) gather_kernel(GatherArgs g) {
-  // blockDim = (bx, by): threads along C, rows along R.
+// calls BODY(NT, PROD) for the launch's term count and product flag
+#define GBCC_GATHER_DISPATCH(g, BODY)                        \
+  do {                                                       \
+    const int nt_ = (g).plain ? 0 : (g).nterms;              \
+    if ((g).general && nt_ > 0) {                            \
+      BODY(-1, true);                                        \
+    } else if ((g).products) {                               \
+      switch (nt_) {                                         \
+        case 1: BODY(1, true); break;                        \
+        case 2: BODY(2, true); break;                        \
+        case 3: BODY(3, true); break;                        \
+        default: BODY(4, true); break;                       \
+      }                                                      \
+    } else {                                                 \
+      switch (nt_) {                                         \
+        case 0: BODY(0, false); break;                       \
+        case 1: BODY(1, false); break;                       \
+        case 2: BODY(2, false); break;                       \
+        case 3: BODY(3, false); break;                       \
+        default: BODY(4, false); break;                      \
+      }                                                      \
+    }                                                        \
+  } while (0)
+
+// blockDim = (bx, by): threads along C, rows along R.  Each thread takes
+// kGatherRows rows per step and issues all their loads (and the old output
+// values when beta != 0) before its stores, so that several DRAM loads per
+// thread are in flight; one load at a time leaves a pass latency-bound.
+constexpr int kGatherRows = 4;
+
+template <int NT, bool PROD, bool RMW>
+__device__ __forceinline__ void gather_rows(const GatherArgs& g) {
   const int64_t c0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t cstep = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const int64_t r0 = static_cast<int64_t>(blockIdx.y) * blockDim.y + threadIdx.y;
   const int64_t rstep = static_cast<int64_t>(gridDim.y) * blockDim.y;
-  for (int64_t r = r0; r < g.Rpad; r += rstep) {
-    const bool rin = r < g.R;
-    for (int64_t c = c0; c < g.Cpad; c += cstep) {
-      const double val = (rin && c < g.C) ? gather_value(g, r, c) : 0.0;
-      if (g.out) {
-        double* p = g.out + r * g.ldo + c;
-        *p = (g.beta == 0.0) ? val : fma(g.beta, *p, val);
-      } else {
-        split_store(val, g.outs, g.nslices, g.slice_stride, r * g.ldo + c);
+  for (int64_t c = c0; c < g.Cpad; c += cstep) {
+    const bool cin = c < g.C;
+    for (int64_t r = r0; r < g.Rpad; r += kGatherRows * rstep) {
+      double val[kGatherRows], old[kGatherRows];
+#pragma unroll
+      for (int u = 0; u < kGatherRows; ++u) {
+        const int64_t ru = r + u * rstep;
+        val[u] = (cin && ru < g.R) ? gather_value<NT, PROD>(g, ru, c) : 0.0;
+        if constexpr (RMW) old[u] = ru < g.Rpad ? g.out[ru * g.ldo + c] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kGatherRows; ++u) {
+        const int64_t ru = r + u * rstep;
+        if (ru >= g.Rpad) break;
+        if (g.out) {
+          if constexpr (RMW) g.out[ru * g.ldo + c] = fma(g.beta, old[u], val[u]);
+          else g.out[ru * g.ldo + c] = val[u];
+        } else {
+          split_store(val[u], g.outs, g.nslices, g.slice_stride, ru * g.ldo + c);
+        }
       }
     }
   }
 }
 
+__global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs g) {
+  const bool rmw = g.out && g.beta != 0.0;
+#define GBCC_ROWS(N, P) (rmw ? gather_rows<N, P, true>(g) : gather_rows<N, P, false>(g))
+  GBCC_GATHER_DISPATCH(g, GBCC_ROWS);
+#undef GBCC_ROWS
+}
+
 // Plain single-term packs into BF16 slices (the common case), 4 consecutive
-// K elements per thread: the row offset is loaded once per row, the K offsets
-// as 16-byte vectors, and every slice gets one 8-byte store per thread.  The
-// launcher checks Cpad, ldo and slice_stride are multiples of 4 (K is padded
-// to 64) so the stores are 8-byte aligned.
-__global__ void __launch_bounds__(kThreads) gather_split4_kernel(GatherArgs g) {
+// K elements of kSplitRows rows per thread step, all loads issued before the
+// stores.  A source that is contiguous along K (cunit) is read with 16-byte
+// vector loads where the row start is even; otherwise the K offsets are read
+// as 16-byte vectors and the elements one by one.  Every slice gets one 8-byte
+// store per thread and row; the launcher checks Cpad, ldo and slice_stride are
+// multiples of 4 (K is padded to 64) so the stores are 8-byte aligned.
+constexpr int kSplitRows = 2;
+
+__device__ __forceinline__ void split4_load(const GatherArgs& g, int64_t r, int64_t c, double x[4]) {
+  const double* __restrict__ a = g.t[0].a;
+  const int64_t* __restrict__ ca = g.t[0].ca;
+  if (r >= g.R) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) x[j] = 0.0;
+    return;
+  }
+  const int64_t rb = g.t[0].ra[r];
+  if (c + 3 < g.C) {
+    if (g.cunit && (rb & 1) == 0) {
+      const double2 v01 = *reinterpret_cast<const double2*>(a + rb + c);
+      const double2 v23 = *reinterpret_cast<const double2*>(a + rb + c + 2);
+      x[0] = v01.x;
+      x[1] = v01.y;
+      x[2] = v23.x;
+      x[3] = v23.y;
+    } else {
+      const longlong2 o01 = *reinterpret_cast<const longlong2*>(ca + c);
+      const longlong2 o23 = *reinterpret_cast<const longlong2*>(ca + c + 2);
+      x[0] = a[rb + o01.x];
+      x[1] = a[rb + o01.y];
+      x[2] = a[rb + o23.x];
+      x[3] = a[rb + o23.y];
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) x[j] = c + j < g.C ? a[rb + ca[c + j]] : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 5) gather_split4_kernel(GatherArgs g) {
   const int64_t nq = g.Cpad / 4;
   const int64_t q0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t qstep = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const int64_t r0 = static_cast<int64_t>(blockIdx.y) * blockDim.y + threadIdx.y;
   const int64_t rstep = static_cast<int64_t>(gridDim.y) * blockDim.y;
-  const double* __restrict__ a = g.t[0].a;
-  const int64_t* __restrict__ ca = g.t[0].ca;
   const int ns = g.nslices;
-  for (int64_t r = r0; r < g.Rpad; r += rstep) {
-    const bool rin = r < g.R;
-    const int64_t rb = rin ? g.t[0].ra[r] : 0;
-    unsigned short* orow = reinterpret_cast<unsigned short*>(g.outs) + r * g.ldo;
+  for (int64_t r = r0; r < g.Rpad; r += kSplitRows * rstep) {
     for (int64_t q = q0; q < nq; q += qstep) {
       const int64_t c = 4 * q;
-      double x[4];
-      if (rin && c + 3 < g.C) {
-        const longlong2 o01 = *reinterpret_cast<const longlong2*>(ca + c);
-        const longlong2 o23 = *reinterpret_cast<const longlong2*>(ca + c + 2);
-        x[0] = a[rb + o01.x];
-        x[1] = a[rb + o01.y];
-        x[2] = a[rb + o23.x];
-        x[3] = a[rb + o23.y];
-      } else {
+      double x[kSplitRows][4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) x[j] = (rin && c + j < g.C) ? a[rb + ca[c + j]] : 0.0;
-      }
-      unsigned short b[4][3];
+      for (int u = 0; u < kSplitRows; ++u) split4_load(g, r + u * rstep, c, x[u]);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) split_bits(x[j], b[j], ns);
-      for (int s = 0; s < ns; ++s) {
-        uint2 w;
-        w.x = static_cast<unsigned>(b[0][s]) | (static_cast<unsigned>(b[1][s]) << 16);
-        w.y = static_cast<unsigned>(b[2][s]) | (static_cast<unsigned>(b[3][s]) << 16);
-        *reinterpret_cast<uint2*>(orow + s * g.slice_stride + c) = w;
+      for (int u = 0; u < kSplitRows; ++u) {
+        const int64_t ru = r + u * rstep;
+        if (ru >= g.Rpad) break;
+        unsigned short* orow = reinterpret_cast<unsigned short*>(g.outs) + ru * g.ldo;
+        unsigned short b[4][3];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) split_bits(x[u][j], b[j], ns);
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          if (s >= ns) break;
+          uint2 w;
+          w.x = static_cast<unsigned>(b[0][s]) | (static_cast<unsigned>(b[1][s]) << 16);
+          w.y = static_cast<unsigned>(b[2][s]) | (static_cast<unsigned>(b[3][s]) << 16);
+          *reinterpret_cast<uint2*>(orow + s * g.slice_stride + c) = w;
+        }
       }
     }
   }
@@ -172,17 +336,19 @@ __global__ void __launch_bounds__(kThreads) gather_split4_kernel(GatherArgs g) {
 // Same contract as gather_kernel for sources contiguous along R: a 32 x 32
 // tile is read with the lanes along R (coalesced), transposed through shared
 // memory and written with the lanes along C (coalesced).  Block 32 x 8.
-__global__ void __launch_bounds__(256) gather_t_kernel(GatherArgs g) {
-  __shared__ double tile[32][33];
+template <int NT, bool PROD, bool RMW>
+__device__ __forceinline__ void gather_tiles(const GatherArgs& g, double (*tile)[33]) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t nrt = (g.Rpad + 31) / 32, nct = (g.Cpad + 31) / 32;
   for (int64_t t = blockIdx.x; t < nrt * nct; t += gridDim.x) {
-    const int64_t r0 = (t / nct) * 32, c0 = (t % nct) * 32;
+    int64_t tr, tc;
+    divmod32(t, nct, tr, tc);
+    const int64_t r0 = tr * 32, c0 = tc * 32;
     // read: lanes along r
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int64_t r = r0 + tx, c = c0 + ty + 8 * k;
-      tile[ty + 8 * k][tx] = (r < g.R && c < g.C) ? gather_value(g, r, c) : 0.0;
+      tile[ty + 8 * k][tx] = (r < g.R && c < g.C) ? gather_value<NT, PROD>(g, r, c) : 0.0;
     }
     __syncthreads();
     // write: lanes along c
@@ -193,7 +359,8 @@ __global__ void __launch_bounds__(256) gather_t_kernel(GatherArgs g) {
         const double val = tile[tx][ty + 8 * k];
         if (g.out) {
           double* p = g.out + r * g.ldo + c;
-          *p = (g.beta == 0.0) ? val : fma(g.beta, *p, val);
+          if constexpr (RMW) *p = fma(g.beta, *p, val);
+          else *p = val;
         } else {
           split_store(val, g.outs, g.nslices, g.slice_stride, r * g.ldo + c);
         }
@@ -201,6 +368,14 @@ __global__ void __launch_bounds__(256) gather_t_kernel(GatherArgs g) {
     }
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(256) gather_t_kernel(GatherArgs g) {
+  __shared__ double tile[32][33];
+  const bool rmw = g.out && g.beta != 0.0;
+#define GBCC_TILES(N, P) (rmw ? gather_tiles<N, P, true>(g, tile) : gather_tiles<N, P, false>(g, tile))
+  GBCC_GATHER_DISPATCH(g, GBCC_TILES);
+#undef GBCC_TILES
 }
 
 // ---------------------------------------------------------------------------
@@ -227,7 +402,8 @@ __global__ void __launch_bounds__(kThreads) energy_partial_kernel(
   const int64_t o2 = o * o;
   double s_r1 = 0.0, s_r2 = 0.0, s_e1 = 0.0, s_e2 = 0.0;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    const int64_t a = p / v, b = p % v;
+    int64_t a, b;
+    divmod32(p, v, a, b);
     const double* r2p = r2 + p * o2;
     const double* gp = g_abij + p * o2;
     const double* tp = tau + p * o2;
@@ -274,9 +450,11 @@ __global__ void __launch_bounds__(kThreads) make_tau_kernel(int64_t o, int64_t v
                                                             double* __restrict__ tau) {
   const int64_t o2 = o * o;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    const int64_t a = p / v, b = p % v;
+    int64_t a, b;
+    divmod32(p, v, a, b);
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      const int64_t i = ij / o, j = ij % o;
+      int64_t i, j;
+      divmod32(ij, o, i, j);
       tau[p * o2 + ij] = fma(t1[a * o + i], t1[b * o + j], t2[p * o2 + ij]);
     }
   }
@@ -312,7 +490,8 @@ __global__ void __launch_bounds__(kThreads) build_gpm_kernel(int64_t rows_v, int
                                                              double* __restrict__ Gm) {
   const int64_t np = v * (v + 1) / 2, nm = v * (v - 1) / 2;
   for (int64_t row = blockIdx.x; row < rows_v * v; row += gridDim.x) {
-    const int64_t a = row / v, b = row % v;
+    int64_t a, b;
+    divmod32(row, v, a, b);
     int64_t rp = row, rm = row;
     if (ab_pairs) {
       if (a > b) continue;
@@ -337,20 +516,22 @@ __global__ void __launch_bounds__(kThreads) tau_pm_kernel(int64_t o, int64_t v, 
                                                           double* __restrict__ taup, double* __restrict__ taum) {
   const int64_t o2 = o * o, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    const int64_t c = p / v, d = p % v;
+    int64_t c, d;
+    divmod32(p, v, c, d);
     if (c > d) continue;
     const double* x = tau + (c * v + d) * o2;
     const double* y = tau + (d * v + c) * o2;
     double* tp = taup + pair_sym(c, d, v) * sp;
     double* tm = c < d ? taum + pair_anti(c, d, v) * sm : nullptr;
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      const int64_t i = ij / o, j = ij % o;
+      int64_t i, j;
+      divmod32(ij, o, i, j);
       if (i > j) continue;
       if (c == d) {
         tp[pair_sym(i, j, o)] = x[ij];
       } else {
-        tp[pair_sym(i, j, o)] = 0.5 * (x[ij] + y[ij]);
-        if (i < j) tm[pair_anti(i, j, o)] = 0.5 * (x[ij] - y[ij]);
+        tp[pair_sym(i, j, o)] = scale_pow2(x[ij] + y[ij], -1);
+        if (i < j) tm[pair_anti(i, j, o)] = scale_pow2(x[ij] - y[ij], -1);
       }
     }
   }
@@ -359,31 +540,58 @@ __global__ void __launch_bounds__(kThreads) tau_pm_kernel(int64_t o, int64_t v, 
 // out(a,b,i,j) (+)= Bp[sym(ab)][sym(ij)] + s_ab s_ij Bm[anti(ab)][anti(ij)], s = +1 for an
 // ordered pair, -1 for a swapped one, 0 on the diagonal.  With ab_pairs false the
 // row index r = a*v + b addresses Bp / Bm directly (no symmetry in the row pair).
+// ACC: add to out (beta = 1) rather than overwrite it.
+template <bool ACC>
 __global__ void __launch_bounds__(kThreads) pair_unpack_kernel(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs,
                                                                const double* __restrict__ Bp,
-                                                               const double* __restrict__ Bm, double beta,
+                                                               const double* __restrict__ Bm,
                                                                double* __restrict__ out) {
   const int64_t o2 = o * o, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
   for (int64_t row = blockIdx.x; row < rows_v * v; row += gridDim.x) {
-    const int64_t a = row / v, b = row % v;
+    int64_t a, b;
+    divmod32(row, v, a, b);
     int64_t rp = row, rm = row;
-    double sab = 1.0;
+    bool sab_pos = true;  // s_ab = +1
     if (ab_pairs) {
       const int64_t lo = a < b ? a : b, hi = a < b ? b : a;
       rp = pair_sym(lo, hi, v);
       rm = lo < hi ? pair_anti(lo, hi, v) : -1;
-      sab = a < b ? 1.0 : -1.0;
+      sab_pos = a < b;
     }
     const double* bp = Bp + rp * sp;
     const double* bm = (Bm && rm >= 0) ? Bm + rm * sm : nullptr;
     double* op = out + row * o2;
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      const int64_t i = ij / o, j = ij % o;
+      int64_t i, j;
+      divmod32(ij, o, i, j);
       const int64_t li = i < j ? i : j, hj = i < j ? j : i;
       double val = bp[pair_sym(li, hj, o)];
-      if (bm && li < hj) val += (i < j ? sab : -sab) * bm[pair_anti(li, hj, o)];
-      op[ij] = beta == 0.0 ? val : op[ij] + val;
+      if (bm && li < hj) val += flip_sign(bm[pair_anti(li, hj, o)], (i < j) != sab_pos);
+      if constexpr (ACC) op[ij] += val;
+      else op[ij] = val;
     }
+  }
+}
+
+// r1(a,i) += sum_k 2 tmp2(k,a,k,i) - tmp2(k,a,i,k) with tmp2[o][v][o][o]: the
+// (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i) term of r1 read off the
+// ladder's tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j), using
+// tau(c,d,k,i) = tau(d,c,i,k)
+__global__ void __launch_bounds__(kThreads) r1_from_tmp2_kernel(int64_t o, int64_t v,
+                                                                const double* __restrict__ tmp2,
+                                                                double* __restrict__ r1) {
+  const int64_t n = v * o;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int64_t a, i;
+    divmod32(e, o, a, i);
+    double s = 0.0;
+    for (int64_t k = 0; k < o; ++k) {
+      const double* p = tmp2 + (k * v + a) * o * o;
+      s = fma(2.0, p[k * o + i], s);
+      s -= p[i * o + k];
+    }
+    r1[e] += s;
   }
 }
 
@@ -394,16 +602,21 @@ __global__ void __launch_bounds__(kThreads) jacobi_inplace_kernel(int64_t o, int
                                                                   const double* r2, double* t1, double* t2) {
   const int64_t o2 = o * o;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    const int64_t a = p / v, b = p % v;
+    int64_t a, b;
+    divmod32(p, v, a, b);
     const double eab = eps_v[a] + eps_v[b];
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      const int64_t i = ij / o, j = ij % o;
+      int64_t i, j;
+      divmod32(ij, o, i, j);
       t2[p * o2 + ij] += r2[p * o2 + ij] / (eps_o[i] + eps_o[j] - eab);
     }
   }
   for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < v * o;
-       e += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    t1[e] += r1[e] / (eps_o[e % o] - eps_v[e / o]);
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int64_t a, i;
+    divmod32(e, o, a, i);
+    t1[e] += r1[e] / (eps_o[i] - eps_v[a]);
+  }
 }
 
 // out[0] = max |t2(a,b,i,j) - t2(b,a,j,i)|, out[1] = max |t2| (out zeroed by
@@ -414,11 +627,13 @@ __global__ void __launch_bounds__(kThreads) pair_asym_kernel(int64_t o, int64_t 
   const int64_t o2 = o * o;
   double md = 0.0, mb = 0.0;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    const int64_t a = p / v, b = p % v;
+    int64_t a, b;
+    divmod32(p, v, a, b);
     const double* x = t2 + p * o2;
     const double* y = t2 + (b * v + a) * o2;
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      const int64_t i = ij / o, j = ij % o;
+      int64_t i, j;
+      divmod32(ij, o, i, j);
       md = fmax(md, fabs(x[ij] - y[j * o + i]));
       mb = fmax(mb, fabs(x[ij]));
     }
@@ -481,10 +696,12 @@ __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) 
   double* x2n = d.x2 + static_cast<int64_t>(d.slot) * n2;
   double* e2n = d.e2 + static_cast<int64_t>(d.slot) * n2;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    const int64_t a = p / v, b = p % v;
+    int64_t a, b;
+    divmod32(p, v, a, b);
     const double eab = d.eps_v[a] + d.eps_v[b];
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      const int64_t i = ij / o, j = ij % o;
+      int64_t i, j;
+      divmod32(ij, o, i, j);
       const int64_t e = p * o2 + ij;
       const double r = d.r2[e];
       const double den = d.eps_o[i] + d.eps_o[j] - eab;
@@ -503,7 +720,8 @@ __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) 
   double* e1n = d.e1 + static_cast<int64_t>(d.slot) * n1;
   for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n1;
        e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int64_t a = e / o, i = e % o;
+    int64_t a, i;
+    divmod32(e, o, a, i);
     const double r = d.r1[e];
     x1n[e] = d.t1[e] + r / (d.eps_o[i] - d.eps_v[a]);
     e1n[e] = r;
@@ -637,9 +855,11 @@ __global__ void __launch_bounds__(kThreads) extrapolate_t2_tau_kernel(ExtrapArgs
   double c[kDiisMax];
   for (int q = 0; q < kDiisMax; ++q) c[q] = (q < x.nvec) ? x.coef[x.slots[q]] : 0.0;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    const int64_t a = p / v, b = p % v;
+    int64_t a, b;
+    divmod32(p, v, a, b);
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      const int64_t i = ij / o, j = ij % o;
+      int64_t i, j;
+      divmod32(ij, o, i, j);
       const int64_t e = p * o2 + ij;
       double acc = 0.0;
       for (int q = 0; q < x.nvec; ++q) acc = fma(c[q], x.x2[x.slots[q] * n2 + e], acc);
@@ -677,7 +897,20 @@ __global__ void split_test_kernel(const double* x, int64_t n, int nslices, unsig
   }
 }
 
+__global__ void scale_test_kernel(const double* x, int64_t n, GatherTerm T, double* out) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    out[i] = T.pow2 ? term_scale(T, x[i]) : x[i] * T.coef;  // as the gathers dispatch
+}
+
 }  // namespace
+
+void launch_scale_test(const double* x, int64_t n, double coef, double* out, cudaStream_t st) {
+  if (n <= 0) return;
+  GatherTerm T{};
+  gather_set_coef(T, coef);
+  scale_test_kernel<<<static_cast<unsigned>(std::min<int64_t>((n + 255) / 256, 4096)), 256, 0, st>>>(x, n, T, out);
+}
 
 void launch_split_test(const double* x, int64_t n, int nslices, unsigned short* out, cudaStream_t st) {
   if (n <= 0) return;
@@ -767,7 +1000,14 @@ void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double
 
 void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, const double* Bp, const double* Bm,
                         double beta, double* out, cudaStream_t st) {
-  pair_unpack_kernel<<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, o, ab_pairs, Bp, Bm, beta, out);
+  if (beta == 0.0)
+    pair_unpack_kernel<false><<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, o, ab_pairs, Bp, Bm, out);
+  else
+    pair_unpack_kernel<true><<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, o, ab_pairs, Bp, Bm, out);
+}
+
+void launch_r1_from_tmp2(int64_t o, int64_t v, const double* tmp2, double* r1, cudaStream_t st) {
+  r1_from_tmp2_kernel<<<grid_for(v * o, kThreads), kThreads, 0, st>>>(o, v, tmp2, r1);
 }
 
 void launch_jacobi_inplace(int64_t o, int64_t v, const double* eps_o, const double* eps_v, const double* r1,

@@ -5,6 +5,8 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include <cmath>
+
 namespace gbcc {
 
 // Error word written by bounded device-side waits; read by the host after a step.
@@ -30,7 +32,21 @@ struct GatherTerm {
   const double* b;   // nullptr: single factor
   const int64_t* rb;
   const int64_t* cb;
+  // coef = (-1)^sign 2^pow2_k exactly (pow2 != 0): the kernels scale by
+  // exponent arithmetic instead of an FP64 multiply (set by gather_set_coef)
+  int pow2;
+  int pow2_k;
+  unsigned long long pow2_sign;
 };
+
+inline void gather_set_coef(GatherTerm& T, double coef) {
+  T.coef = coef;
+  int e = 0;
+  const double m = std::frexp(coef, &e);  // coef = m 2^e, 0.5 <= |m| < 1
+  T.pow2 = (m == 0.5 || m == -0.5) && e - 1 >= -64 && e - 1 <= 64;
+  T.pow2_k = e - 1;
+  T.pow2_sign = coef < 0 ? (1ull << 63) : 0ull;
+}
 
 struct GatherArgs {
   int nterms;
@@ -50,9 +66,27 @@ struct GatherArgs {
   int transpose;
   // 1: one term, no second factor, coefficient 1 -- a plain load (set by the planner)
   int plain;
+  // 1 (plain packs only): the term's column offsets are 0, 1, 2, ... and its
+  // base is 16-byte aligned, so rows can be read with 16-byte vector loads
+  int cunit;
+  // 1: some term has a second factor (b != nullptr)
+  int products;
+  // 1: some coefficient is not +-2^k (set by gather_finish)
+  int general;
 };
 
+// derived flags of a filled GatherArgs (call after its terms are set)
+inline void gather_finish(GatherArgs& g) {
+  g.general = 0;
+  for (int t = 0; t < g.nterms; ++t)
+    if (!g.t[t].pow2) g.general = 1;
+}
+
 void launch_gather(const GatherArgs& args, cudaStream_t st);
+
+// out[i] = coef * x[i] as the gather kernels scale a term (exponent arithmetic
+// for power-of-two coefficients)
+void launch_scale_test(const double* x, int64_t n, double coef, double* out, cudaStream_t st);
 
 // FP64 -> nslices BF16 bit patterns (out[s*n + i]) with the packing kernels' split
 void launch_split_test(const double* x, int64_t n, int nslices, unsigned short* out, cudaStream_t st);
@@ -156,12 +190,15 @@ void launch_energy_terms(int64_t o, int64_t v, const double* r1, const double* r
 // tau(a,b,i,j) = t2(a,b,i,j) + t1(a,i) t1(b,j)
 // Pair-(anti)symmetric ladder (see kernels.cu): G+/G- over (a <= b or any row
 // pair) x (c <= d) from G[rows_v][v][v][v]; tau+/tau- over (c <= d) x (i <= j);
-// out(row, i, j) = beta out + B+ +- B- unpacked from the pair products.
+// out(row, i, j) = beta out + B+ +- B- unpacked from the pair products (beta 0 or 1).
 void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G, double* Gp, double* Gm,
                       cudaStream_t st);
 void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double* taum, cudaStream_t st);
 void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, const double* Bp, const double* Bm,
                         double beta, double* out, cudaStream_t st);
+
+// r1(a,i) += sum_k 2 tmp2(k,a,k,i) - tmp2(k,a,i,k), tmp2[o][v][o][o], r1[v][o]
+void launch_r1_from_tmp2(int64_t o, int64_t v, const double* tmp2, double* r1, cudaStream_t st);
 
 // t1 += r1 / D1, t2 += r2 / D2 in place
 void launch_jacobi_inplace(int64_t o, int64_t v, const double* eps_o, const double* eps_v, const double* r1,

@@ -172,6 +172,23 @@ extern "C" int gbcc_testing_split(const double* x, int64_t n, int nslices, uint1
   }
 }
 
+extern "C" int gbcc_testing_scale(const double* x, int64_t n, double coef, double* out) {
+  using namespace gbcc;
+  if (!x || !out || n < 0) return GBCC_ERR_INVALID_ARG;
+  if (n == 0) return GBCC_OK;
+  try {
+    double* dx = static_cast<double*>(dev_alloc(2 * n * sizeof(double)));
+    GBCC_CK(cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice));
+    launch_scale_test(dx, n, coef, dx + n, nullptr);
+    GBCC_CK(cudaGetLastError());
+    GBCC_CK(cudaMemcpy(out, dx + n, n * sizeof(double), cudaMemcpyDeviceToHost));
+    dev_free(dx);
+    return GBCC_OK;
+  } catch (const Error& e) {
+    return e.status;
+  }
+}
+
 extern "C" int gbcc_testing_fp64_peak(double* gflops) {
   using namespace gbcc;
   if (!gflops) return GBCC_ERR_INVALID_ARG;

@@ -123,3 +123,33 @@ def test_device_split_matches_emulation(gbcc_lib, nslices):
     got = out.reshape(nslices, x.size)
     bad = np.nonzero(got != ref)
     assert bad[0].size == 0, [(x[i], s, hex(got[s, i]), hex(ref[s, i])) for s, i in zip(*bad)][:5]
+
+
+def scale_sample(seed=0):
+    """Normals of all magnitudes, values at the edges of the normal range,
+    subnormals, signed zeros, infinities and NaN."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(4000) * np.exp2(rng.integers(-1070, 1020, 4000))
+    edge = [np.finfo(np.float64).tiny, np.finfo(np.float64).tiny * 2, np.finfo(np.float64).max,
+            np.finfo(np.float64).max / 2, 5e-324, 1e-310, 2.0 ** -1020, 2.0 ** 1023, 0.0, -0.0,
+            np.inf, -np.inf, np.nan, 1.0, -3.0]
+    edge = np.array(edge)
+    return np.concatenate([x, edge, -edge])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("coef", [1.0, -1.0, 2.0, -2.0, 0.5, -0.5, 4.0, 0.25, 2.0 ** -60, -(2.0 ** 60), 3.0, -0.1])
+def test_device_term_scaling_is_the_ieee_product(gbcc_lib, coef):
+    """The packing kernels scale a term by +-2^k on the exponent bits (no FP64
+    instruction); every value, including those whose product leaves the normal
+    range, must come out as the IEEE product."""
+    x = scale_sample(seed=int(abs(np.log2(abs(coef)))) + (coef < 0))
+    out = np.empty_like(x)
+    st = gbcc_lib.gbcc_testing_scale(x.ctypes.data_as(C.c_void_p), x.size, coef, out.ctypes.data_as(C.c_void_p))
+    assert st == 0
+    with np.errstate(over="ignore", under="ignore", invalid="ignore"):
+        ref = x * coef
+    nan = np.isnan(ref)
+    bad = np.nonzero((np.isnan(out) != nan) | (~nan & (out.view(np.uint64) != ref.view(np.uint64))))[0]
+    assert bad.size == 0, [(hex(x[i:i + 1].view(np.uint64)[0]), hex(out[i:i + 1].view(np.uint64)[0]),
+                            hex(ref[i:i + 1].view(np.uint64)[0])) for i in bad[:6]]
