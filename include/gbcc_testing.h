@@ -46,6 +46,17 @@ int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const double* A, cons
                           int slices, int ksplit, int bn, int cta2, int chunk, int fold, int sps, int repeat,
                           float* ms);
 
+/* As gbcc_testing_gemm_ex2 with the tile order and the output form: group > 1
+ * runs the output tiles in bands of `group` M tiles, N outer within a band;
+ * cmode bit 0 accumulates into C (beta = 1; the timed launches add up, the
+ * returned C is one product added to zeros), bit 1 stores C column-major on
+ * the device (unit stride along M, the m-major epilogue).  C is returned
+ * row-major either way. */
+int gbcc_testing_gemm_ex3(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+                          int slices, int ksplit, int bn, int cta2, int chunk, int fold, int sps, int group,
+                          int cmode, int repeat, float* ms);
+
+
 /* Peak probe: FP64 FMA throughput of this GPU in GFLOP/s (a register-resident
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);
@@ -81,7 +92,8 @@ int gbcc_testing_profile_gemm_ms(struct gbcc_handle* h, int max_sites, double* m
 
 /* Per operation of the last profiled residual: N tile width of a tensor-core
  * contraction (-1: the short-K CUDA-core kernel, 0: FP64 / elementwise), its
- * K split and its slices per pipeline stage, as tiles[3 i .. 3 i + 2]. */
+ * K split, its slices per pipeline stage and the M tiles per band of its tile
+ * order (1: whole rows), as tiles[4 i .. 4 i + 3]. */
 int gbcc_testing_profile_tiles(gbcc_handle* h, int max_sites, int32_t* tiles);
 
 /* GEMM shape (M, N, K) of each operation of the last profiled residual,

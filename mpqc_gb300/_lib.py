@@ -28,7 +28,7 @@ EXPORTS = (
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error",
 )
 # test hooks of include/gbcc_testing.h
-TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
+TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_gemm_ex3", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims",
                    "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total")
@@ -98,6 +98,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         [C.POINTER(C.c_float)]
     lib.gbcc_testing_gemm_ex2.restype = C.c_int
     lib.gbcc_testing_gemm_ex2.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp] + [C.c_int] * 8 + \
+        [C.POINTER(C.c_float)]
+    lib.gbcc_testing_gemm_ex3.restype = C.c_int
+    lib.gbcc_testing_gemm_ex3.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp] + [C.c_int] * 10 + \
         [C.POINTER(C.c_float)]
     lib.gbcc_testing_split.restype = C.c_int
     lib.gbcc_testing_split.argtypes = [vp, C.c_int64, C.c_int, vp]

@@ -156,11 +156,11 @@ class Solver:
         self.lib.gbcc_testing_profile_gemm_ms(self.h, max_sites, gm)
         mnk = (C.c_int64 * (3 * max_sites))()
         self.lib.gbcc_testing_profile_dims(self.h, max_sites, mnk)
-        tl = (C.c_int32 * (3 * max_sites))()
+        tl = (C.c_int32 * (4 * max_sites))()
         self.lib.gbcc_testing_profile_tiles(self.h, max_sites, tl)
         return [dict(ms=ms[i], gemm_ms=gm[i], flops=fl[i], pairs=pr[i], cls=cl[i],
-                     M=mnk[3 * i], N=mnk[3 * i + 1], K=mnk[3 * i + 2], bn=tl[3 * i], ksplit=tl[3 * i + 1],
-                     sps=tl[3 * i + 2])
+                     M=mnk[3 * i], N=mnk[3 * i + 1], K=mnk[3 * i + 2], bn=tl[4 * i], ksplit=tl[4 * i + 1],
+                     sps=tl[4 * i + 2], group=tl[4 * i + 3])
                 for i in range(min(n.value, max_sites))]
 
     def tc_launches_total(self):

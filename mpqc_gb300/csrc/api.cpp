@@ -47,7 +47,7 @@ struct gbcc_handle {
   cudaEvent_t slots[8] = {};
   std::vector<double> prof_gemm_ms;
   std::vector<std::array<int64_t, 3>> prof_dims;
-  std::vector<std::array<int32_t, 3>> prof_tiles;
+  std::vector<std::array<int32_t, 4>> prof_tiles;
   // residual program captured as a CUDA graph, one per precision (FP64, mixed)
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_launches[2] = {0, 0};
@@ -786,7 +786,7 @@ int gbcc_testing_profile_residual(gbcc_handle* h, int precision, int max_sites, 
     for (const auto& x : st) {
       h->prof_gemm_ms.push_back(x.gemm_ms);
       h->prof_dims.push_back({x.M, x.N, x.K});
-      h->prof_tiles.push_back({x.bn, x.ksplit, x.sps});
+      h->prof_tiles.push_back({x.bn, x.ksplit, x.sps, x.group});
     }
     if (nsites) *nsites = static_cast<int>(st.size());
     for (int i = 0; i < max_sites && i < static_cast<int>(st.size()); ++i) {
@@ -808,7 +808,7 @@ int gbcc_testing_profile_gemm_ms(gbcc_handle* h, int max_sites, double* ms) {
 int gbcc_testing_profile_tiles(gbcc_handle* h, int max_sites, int32_t* tiles) {
   if (!h || !tiles) return GBCC_ERR_INVALID_ARG;
   for (int i = 0; i < max_sites && i < static_cast<int>(h->prof_tiles.size()); ++i)
-    for (int k = 0; k < 3; ++k) tiles[3 * i + k] = h->prof_tiles[i][k];
+    for (int k = 0; k < 4; ++k) tiles[4 * i + k] = h->prof_tiles[i][k];
   return GBCC_OK;
 }
 

@@ -168,11 +168,13 @@ struct GemmPlan {
   int pa[kMaxPairs] = {}, pb[kMaxPairs] = {};
   double flops = 0.0;
   int sps = 1;             // tensor cores: slices per pipeline stage (2: both slices of a k-block)
-  // tensor cores: (tile width, K split, slices per stage) candidates for the
-  // tuner, the plan's heuristic choice first
+  int group = 1;           // tensor cores: M tiles per band of the tile order (1: rows)
+  // tensor cores: (tile width, K split, slices per stage, band) candidates
+  // for the tuner, the plan's heuristic choice first
+  static constexpr int kMaxCand = 24;
   int ncand = 0;
-  int cand_bn[16] = {}, cand_ks[16] = {}, cand_sps[16] = {};
-  int64_t cand_kps[16] = {};
+  int cand_bn[kMaxCand] = {}, cand_ks[kMaxCand] = {}, cand_sps[kMaxCand] = {}, cand_group[kMaxCand] = {};
+  int64_t cand_kps[kMaxCand] = {};
 };
 
 struct Site {
@@ -233,6 +235,7 @@ std::vector<SiteStat> Engine::site_stats(int precision) {
       st.bn = p.use_tc ? p.bn : (p.smallk ? -1 : 0);
       st.ksplit = p.ksplit;
       st.sps = p.use_tc ? p.sps : 0;
+      st.group = p.use_tc ? p.group : 0;
     } else {
       st.M = sp->gather.R;
       st.N = sp->gather.C;
@@ -480,6 +483,7 @@ GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* cons
   // a slice limit makes the packed slices a superset of the used ones: one
   // pair per stage then
   t.sps = (lim > 0 && lim < p.slices) ? 1 : p.sps;
+  t.group = p.group;
   return t;
 }
 
@@ -524,6 +528,7 @@ void Engine::autotune(int reps) {
       q.ksplit = p.cand_ks[c];
       q.k_per_split = p.cand_kps[c];
       q.sps = p.cand_sps[c];
+      q.group = p.cand_group[c];
       const GemmTcArgs t = tc_args(q, sp->cls, panel);
       if (!launch_gemm_tc(t, stream_)) continue;
       ++tc_total_;
@@ -545,6 +550,7 @@ void Engine::autotune(int reps) {
       p.ksplit = p.cand_ks[pick];
       p.k_per_split = p.cand_kps[pick];
       p.sps = p.cand_sps[pick];
+      p.group = p.cand_group[pick];
     }
   }
   GBCC_CK(cudaStreamSynchronize(stream_));
@@ -869,14 +875,19 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         if (ks > 1) wspart_ = std::max(wspart_, static_cast<size_t>(ks * p.P[0].rows_pad * npad));
         // both slices of a k-block per stage: two slices, tiles up to 192 wide
         const int nsps = (slices == 2 && bns[c] >= 64 && bns[c] <= 192) ? 2 : 1;
+        // bands of 8 M tiles: many N tiles per row and enough rows
+        const bool banded = npad / bns[c] >= 8 && p.P[0].rows_pad / kTcBM >= 16;
         for (int sp = 1; sp <= nsps; ++sp) {
           for (int split = 0; split < (ks > 1 ? 2 : 1); ++split) {
-            if (p.ncand >= 16) break;
-            p.cand_bn[p.ncand] = bns[c];
-            p.cand_ks[p.ncand] = split == 0 ? static_cast<int>(ks) : 1;
-            p.cand_kps[p.ncand] = split == 0 ? kbps : 0;
-            p.cand_sps[p.ncand] = sp;
-            ++p.ncand;
+            for (int band = 0; band < (banded && (split == 1 || ks == 1) ? 2 : 1); ++band) {
+              if (p.ncand >= GemmPlan::kMaxCand) break;
+              p.cand_bn[p.ncand] = bns[c];
+              p.cand_ks[p.ncand] = split == 0 ? static_cast<int>(ks) : 1;
+              p.cand_kps[p.ncand] = split == 0 ? kbps : 0;
+              p.cand_sps[p.ncand] = sp;
+              p.cand_group[p.ncand] = band ? 8 : 1;
+              ++p.ncand;
+            }
           }
         }
       }
@@ -885,6 +896,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       p.ksplit = p.cand_ks[0];
       p.k_per_split = p.cand_kps[0];
       p.sps = p.cand_sps[0];
+      p.group = p.cand_group[0];
     }
   }
 }

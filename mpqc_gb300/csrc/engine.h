@@ -109,6 +109,7 @@ struct SiteStat {
   int bn = 0;          // tensor cores: N tile width; -1: the short-K CUDA-core kernel
   int ksplit = 1;      // K split over CTAs
   int sps = 1;         // tensor cores: slices per pipeline stage
+  int group = 1;       // tensor cores: M tiles per band of the tile order
 };
 
 struct OperandPlan;

@@ -43,6 +43,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "fp_bits.cuh"
 #include "kernels.h"
 
 namespace gbcc {
@@ -296,30 +297,6 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 
 constexpr int kStgLd = 17;  // padded row of the per-warp output staging tile (8-byte words)
 
-// float -> double by rewriting the bit pattern (exact), integer operations
-// only.  GB300 runs FP64 arithmetic and FP64 conversions at ~2 per clock per
-// SM, and the epilogue of a short-K contraction is bound by them (ncu: FP64
-// pipe 64 % busy, DRAM 14 % at K = 32).  Every class of input is handled
-// without a hardware conversion (a rare-case fallback would be evaluated for
-// every element once the compiler turns the branch into a select).
-__device__ __forceinline__ double f2d_exact(float f) {
-  const uint32_t b = __float_as_uint(f);
-  const uint32_t e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
-  const uint64_t sign = static_cast<uint64_t>(b >> 31) << 63;
-  uint64_t d;
-  if (e == 0xFFu) {
-    d = sign | (0x7FFull << 52) | (static_cast<uint64_t>(m) << 29);  // inf / nan
-  } else if (e != 0u) {
-    d = sign | (static_cast<uint64_t>(e + 896u) << 52) | (static_cast<uint64_t>(m) << 29);
-  } else if (m == 0u) {
-    d = sign;
-  } else {  // subnormal: m 2^-149 with leading bit p
-    const int p = 31 - __clz(static_cast<int>(m));
-    d = sign | (static_cast<uint64_t>(p + 874) << 52) | ((static_cast<uint64_t>(m) << (52 - p)) & 0xFFFFFFFFFFFFFull);
-  }
-  return __longlong_as_double(static_cast<long long>(d));
-}
-
 // SPS: slices per pipeline stage.  1: a stage holds one (A slice, B slice)
 // pair of a k-block and feeds one pair of MMAs; 2: a stage holds both slices
 // of A and of B of a k-block and feeds all three pair products (no tile is
@@ -400,13 +377,27 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
   const int kblocks = static_cast<int>(g.Kpad / BK);
   const int kb_per_split = ksplit > 1 ? g.kb_per_split : kblocks;
   const int chunk = g.chunk > 0 ? g.chunk : 4;
+  const int ntm = static_cast<int>(g.Mpad / BMP);
+  const int group = g.group > 1 ? g.group : 1;
   // tile -> (K split, M block, N block); N fastest so CTAs running together
-  // share the A panel in L2
+  // share the A panel in L2, or, with group > 1, bands of `group` M blocks
+  // with N outer inside a band (fewer B columns live at once)
   auto decode = [&](int tile, int& m0, int& n0, int& kb0, int& n_iter, int& split) {
     split = tile / ntiles_mn;
     const int mn = tile - split * ntiles_mn;
-    n0 = (mn % ntn) * BN;
-    m0 = (mn / ntn) * BMP + static_cast<int>(rank) * BM;
+    int mt, nt;
+    if (group > 1) {
+      const int band = mn / (group * ntn);
+      const int rows = ntm - band * group < group ? ntm - band * group : group;
+      const int idx = mn - band * group * ntn;
+      mt = band * group + idx % rows;
+      nt = idx / rows;
+    } else {
+      mt = mn / ntn;
+      nt = mn - mt * ntn;
+    }
+    n0 = nt * BN;
+    m0 = mt * BMP + static_cast<int>(rank) * BM;
     kb0 = split * kb_per_split;
     const int nkb = kblocks - kb0 < kb_per_split ? kblocks - kb0 : kb_per_split;
     n_iter = SPS == 1 ? nkb * g.npairs : nkb;

@@ -6,6 +6,7 @@
 // (1/64 of FP32), so per-element FP64 work is kept to a few operations: the
 // BF16 split works on bit patterns and FP32 remainders, and single-term packs
 // are plain copies (their coefficient scales the GEMM instead).
+#include "fp_bits.cuh"
 #include "kernels.h"
 
 #include <algorithm>
@@ -96,55 +97,6 @@ __device__ __forceinline__ void split_store(double x, __nv_bfloat16* out, int ns
   unsigned short b[3];
   split_bits(x, b, nslices);
   for (int s = 0; s < nslices; ++s) out[s * slice_stride + idx] = __ushort_as_bfloat16(b[s]);
-}
-
-// GB300 executes FP64 at about 2 operations per clock per SM, so an elementwise
-// pass that spends two FP64 instructions per 8-byte element is bound by the
-// FP64 pipe rather than by HBM.  Scaling by a power of two and changing a sign
-// are therefore done on the bit pattern (integer pipes); only the sums of terms
-// use FP64 adds.
-
-// Magnitude bits of |x| 2^k for the magnitude bits m of a finite nonzero x
-// whose scaled exponent leaves the normal range or that is subnormal (the
-// rare case of scale_pow2), in integer arithmetic: IEEE round to nearest even
-// for results below the normal range, infinity above it.
-__device__ __forceinline__ unsigned long long scale_pow2_rare(unsigned long long m, int k) {
-  const int e = static_cast<int>(m >> 52);
-  // significand s and exponent q with |x| = s 2^(q - 1074), s < 2^53
-  unsigned long long s = e ? ((m & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : m;
-  int q = (e ? e - 1 : 0) + k;
-  // normalise so that bit 52 of s is set (subnormal inputs)
-  const int lz = __clzll(static_cast<long long>(s)) - 11;  // leading zeros within 53 bits
-  s <<= lz;
-  q -= lz;
-  if (q >= 0x7FE) return 0x7FFull << 52;                    // overflow: infinity
-  if (q >= 0) return (static_cast<unsigned long long>(q + 1) << 52) | (s & 0xFFFFFFFFFFFFFull);
-  // subnormal result: s 2^q in units of 2^-1074, shift right by -q with RNE
-  const int sh = -q;
-  if (sh > 54) return 0ull;
-  const unsigned long long r = s >> sh, rem = s & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-  return r + ((rem > half || (rem == half && (r & 1ull))) ? 1ull : 0ull);
-}
-
-// x * 2^k (|k| <= 64) on the bit pattern, exact as the IEEE product: the
-// exponent field shifts when x is normal and the result stays normal; zeros,
-// infinities and NaN pass through; the rest goes to scale_pow2_rare.  No FP64
-// instruction is issued.
-__device__ __forceinline__ double scale_pow2(double x, int k) {
-  // common case on the high word: exponent field (bits 20-30) + k
-  const int hi = __double2hiint(x);
-  const int e = (hi >> 20) & 0x7FF;
-  const int ek = e + k;
-  if (e != 0 && e != 0x7FF && ek >= 1 && ek <= 0x7FE) return __hiloint2double(hi + k * (1 << 20), __double2loint(x));
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
-  const unsigned long long m = b & 0x7FFFFFFFFFFFFFFFull;
-  if (m == 0ull || e == 0x7FF) return x;
-  return __longlong_as_double(static_cast<long long>((b & 0x8000000000000000ull) | scale_pow2_rare(m, k)));
-}
-
-// -x when neg (sign bit flip), x otherwise
-__device__ __forceinline__ double flip_sign(double x, bool neg) {
-  return __longlong_as_double(__double_as_longlong(x) ^ (neg ? static_cast<long long>(1ull << 63) : 0ll));
 }
 
 // coef * x for one gather term whose coefficient is +-2^k (GatherTerm.pow2)

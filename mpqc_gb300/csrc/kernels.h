@@ -39,13 +39,20 @@ struct GatherTerm {
   unsigned long long pow2_sign;
 };
 
+// true when c = (-1)^neg 2^k exactly with |k| <= 64
+inline bool pow2_parts(double c, int& k, bool& neg) {
+  int e = 0;
+  const double m = std::frexp(c, &e);  // c = m 2^e, 0.5 <= |m| < 1
+  k = e - 1;
+  neg = c < 0;
+  return (m == 0.5 || m == -0.5) && k >= -64 && k <= 64;
+}
+
 inline void gather_set_coef(GatherTerm& T, double coef) {
   T.coef = coef;
-  int e = 0;
-  const double m = std::frexp(coef, &e);  // coef = m 2^e, 0.5 <= |m| < 1
-  T.pow2 = (m == 0.5 || m == -0.5) && e - 1 >= -64 && e - 1 <= 64;
-  T.pow2_k = e - 1;
-  T.pow2_sign = coef < 0 ? (1ull << 63) : 0ull;
+  bool neg = false;
+  T.pow2 = pow2_parts(coef, T.pow2_k, neg) ? 1 : 0;
+  T.pow2_sign = neg ? (1ull << 63) : 0ull;
 }
 
 struct GatherArgs {
@@ -155,6 +162,10 @@ struct GemmTcArgs {
   // slices per pipeline stage: 0 or 1, one (A, B) slice pair per stage; 2, both
   // slices of A and B of a k-block per stage (2 slices, bn 64 / 128 / 192)
   int sps;
+  // > 1: output tiles run in bands of `group` M tiles, N outer within a band
+  // (CTAs working at the same time then share fewer, wider operand panels in
+  // L2); 0 or 1: N fastest over whole rows of tiles
+  int group;
 };
 // Deterministic K-split reduction: C[cm[m] + cn[n]] = beta*C + alpha * sum_s
 // partial[s][m][n] (splits summed in order), partial rows of length ldp and

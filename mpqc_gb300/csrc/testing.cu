@@ -40,8 +40,16 @@ extern "C" int gbcc_testing_gemm_ex(int64_t M, int64_t N, int64_t K, const doubl
 extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
                                      double* Cout, int slices, int ksplit, int bn_req, int cta2, int chunk,
                                      int fold, int sps, int repeat, float* ms) {
+  return gbcc_testing_gemm_ex3(M, N, K, A, B, Cout, slices, ksplit, bn_req, cta2, chunk, fold, sps, 1, 0, repeat, ms);
+}
+
+extern "C" int gbcc_testing_gemm_ex3(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
+                                     double* Cout, int slices, int ksplit, int bn_req, int cta2, int chunk,
+                                     int fold, int sps, int group, int cmode, int repeat, float* ms) {
   using namespace gbcc;
-  if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1 || ksplit < 1)
+  const bool accumulate = (cmode & 1) != 0, m_major = (cmode & 2) != 0;
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || slices < 0 || slices > 3 || repeat < 1 || ksplit < 1 ||
+      group < 0)
     return GBCC_ERR_INVALID_ARG;
   if (bn_req != 0 && bn_req != 32 && bn_req != 64 && bn_req != 128 && bn_req != 192 && bn_req != 256)
     return GBCC_ERR_INVALID_ARG;
@@ -69,8 +77,10 @@ extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const doub
       GBCC_CK(cudaMemcpy(d, h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
       return d;
     };
-    const int64_t* cm = table(M, N);
-    const int64_t* cn = table(N, 1);
+    // C row-major, or column-major (unit stride along M) with cmode bit 1
+    const int64_t* cm = m_major ? table(M, 1) : table(M, N);
+    const int64_t* cn = m_major ? table(N, M) : table(N, 1);
+    const double beta = accumulate ? 1.0 : 0.0;
     cudaEvent_t e0, e1;
     GBCC_CK(cudaEventCreate(&e0));
     GBCC_CK(cudaEventCreate(&e1));
@@ -78,7 +88,7 @@ extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const doub
       GemmF64Args g{};
       g.M = M; g.N = N; g.K = K;
       g.A = dA; g.lda = K; g.B = dB; g.ldb = K;
-      g.C = dC; g.cm = cm; g.cn = cn; g.alpha = 1.0; g.beta = 0.0;
+      g.C = dC; g.cm = cm; g.cn = cn; g.alpha = 1.0; g.beta = beta; g.m_major = m_major ? 1 : 0;
       if (ksplit > 1) {
         g.ksplit = ksplit;
         g.k_per_split = (K + ksplit - 1) / ksplit;
@@ -89,6 +99,10 @@ extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const doub
       GBCC_CK(cudaEventRecord(e0, st));
       for (int r = 0; r < repeat; ++r) launch_gemm_f64(g, st);
       GBCC_CK(cudaEventRecord(e1, st));
+      if (accumulate) {  // the output of one product added to zeros
+        GBCC_CK(cudaMemsetAsync(dC, 0, M * N * sizeof(double), st));
+        launch_gemm_f64(g, st);
+      }
     } else {
       const int bn = bn_req ? bn_req : (cta2 ? (N <= 64 ? 64 : 128) : gemm_tc_pick_bn(N, false));
       const int64_t Mpad = rup(M, cta2 ? 2 * kTcBM : kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
@@ -113,11 +127,13 @@ extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const doub
       for (int a = 0; a < slices; ++a)
         for (int b = 0; b < slices; ++b)
           if (a + b < slices) { t.pa[t.npairs] = a; t.pb[t.npairs] = b; ++t.npairs; }
-      t.C = dC; t.cm = cm; t.cn = cn; t.alpha = 1.0; t.beta = 0.0; t.bn = bn; t.err = err;
+      t.C = dC; t.cm = cm; t.cn = cn; t.alpha = 1.0; t.beta = beta; t.bn = bn; t.err = err;
+      t.m_major = m_major ? 1 : 0;
       t.cta2 = cta2 ? 1 : 0;
       t.chunk = chunk;
       t.fold = fold;
       t.sps = sps;
+      t.group = group;
       if (ksplit > 1) {
         const int64_t kblocks = Kpad / kTcBK;
         t.kb_per_split = static_cast<int>((kblocks + ksplit - 1) / ksplit);
@@ -127,12 +143,16 @@ extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const doub
       auto run = [&]() {
         if (!launch_gemm_tc(t, st)) throw Error(GBCC_ERR_CUDA, "tcgen05 launch rejected");
         if (t.ksplit > 1)
-          launch_splitk_reduce(M, N, t.ksplit, t.partial, Mpad, Npad, dC, cm, cn, 1.0, 0.0, st);
+          launch_splitk_reduce(M, N, t.ksplit, t.partial, Mpad, Npad, dC, cm, cn, 1.0, beta, st);
       };
       run();
       GBCC_CK(cudaEventRecord(e0, st));
       for (int r = 0; r < repeat; ++r) run();
       GBCC_CK(cudaEventRecord(e1, st));
+      if (accumulate) {  // the output of one product added to zeros
+        GBCC_CK(cudaMemsetAsync(dC, 0, M * N * sizeof(double), st));
+        run();
+      }
     }
     GBCC_CK(cudaEventSynchronize(e1));
     GBCC_CK(cudaGetLastError());
@@ -142,7 +162,14 @@ extern "C" int gbcc_testing_gemm_ex2(int64_t M, int64_t N, int64_t K, const doub
     int herr = 0;
     GBCC_CK(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
     if (herr != kDevOk) status = GBCC_ERR_TIMEOUT;
-    GBCC_CK(cudaMemcpy(Cout, dC, M * N * sizeof(double), cudaMemcpyDefault));
+    if (m_major) {
+      std::vector<double> cc(static_cast<size_t>(M * N));
+      GBCC_CK(cudaMemcpy(cc.data(), dC, M * N * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int64_t m = 0; m < M; ++m)
+        for (int64_t n = 0; n < N; ++n) Cout[m * N + n] = cc[n * M + m];
+    } else {
+      GBCC_CK(cudaMemcpy(Cout, dC, M * N * sizeof(double), cudaMemcpyDefault));
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
   } catch (const Error& e) {

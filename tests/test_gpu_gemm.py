@@ -131,3 +131,58 @@ def test_gemm_both_slices_per_stage(tlib, M, N, K, ksplit, bn):
     tol = TOL[2] + 8 * 2.0**-24 * np.sqrt(K)
     assert np.max(np.abs(out - ref)) <= tol * np.max(np.abs(ref))
     assert np.max(np.abs(out - out1)) <= 2 * tol * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("bn,sps", [(192, 2), (256, 1), (128, 1)])
+@pytest.mark.parametrize("M,N,K,group,ksplit", [(2000, 1700, 640, 8, 1), (1500, 1900, 512, 8, 1),
+                                                (1500, 1900, 512, 3, 1), (900, 1300, 2048, 8, 2)])
+def test_gemm_banded_tile_order(tlib, M, N, K, group, ksplit, bn, sps):
+    """Output tiles run in bands of `group` M tiles (the last band short where
+    the M tiles do not divide): the same tiles in another order, so the
+    result equals the row-order one bit for bit."""
+    rng = np.random.default_rng(M + N + K + group + bn)
+    A = rng.normal(size=(M, K))
+    B = rng.normal(size=(N, K))
+    ms = C.c_float()
+    tlib.gbcc_testing_gemm_ex3.restype = C.c_int
+    tlib.gbcc_testing_gemm_ex3.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p] + \
+        [C.c_int] * 10 + [C.POINTER(C.c_float)]
+    outs = []
+    for g in (1, group):
+        out = np.empty((M, N))
+        st = tlib.gbcc_testing_gemm_ex3(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, 2, ksplit, bn, 0, 0,
+                                        0, sps, g, 0, 1, C.byref(ms))
+        assert st == 0
+        outs.append(out)
+    assert np.array_equal(outs[0], outs[1])
+    ref = A @ B.T
+    tol = TOL[2] + 8 * 2.0**-24 * np.sqrt(K)
+    assert np.max(np.abs(outs[1] - ref)) <= tol * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("slices,bn,sps", [(2, 192, 2), (2, 256, 1), (2, 64, 1), (0, 0, 1)])
+@pytest.mark.parametrize("cmode", [1, 2, 3])
+@pytest.mark.parametrize("ksplit", [1, 3])
+def test_gemm_output_forms(tlib, slices, bn, sps, cmode, ksplit):
+    """Accumulating epilogue (beta = 1) and column-major C (the m-major
+    epilogue) give the product of the row-major, beta = 0 form."""
+    M, N, K = 700, 900, 384
+    rng = np.random.default_rng(cmode * 10 + slices + bn + ksplit)
+    A = rng.normal(size=(M, K))
+    B = rng.normal(size=(N, K))
+    ms = C.c_float()
+    tlib.gbcc_testing_gemm_ex3.restype = C.c_int
+    tlib.gbcc_testing_gemm_ex3.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p] + \
+        [C.c_int] * 10 + [C.POINTER(C.c_float)]
+    outs = []
+    for mode in (0, cmode):
+        out = np.empty((M, N))
+        st = tlib.gbcc_testing_gemm_ex3(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, slices, ksplit, bn,
+                                        0, 0, 0, sps, 1, mode, 2, C.byref(ms))
+        assert st == 0
+        outs.append(out)
+    # beta = 1 on zeros and a column-major store change no bits of the product
+    assert np.array_equal(outs[0], outs[1])
+    ref = A @ B.T
+    tol = (TOL[slices] + 8 * 2.0**-24 * np.sqrt(K)) if slices else TOL[0]
+    assert np.max(np.abs(outs[1] - ref)) <= tol * np.max(np.abs(ref))
