@@ -474,7 +474,10 @@ GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* cons
   t.alpha = p.alpha;
   t.beta = p.beta;
   t.bn = p.bn;
-  t.chunk = chunk_;
+  // the accumulation length of the slice count in effect (a calibration trial
+  // under a slice limit measures the error the smaller plan will have)
+  const int eff_slices = (slice_limit_[cls] > 0 && slice_limit_[cls] < p.slices) ? slice_limit_[cls] : p.slices;
+  t.chunk = eff_slices >= 3 ? chunk_ : chunk_lo_;
   t.err = err_;
   t.ksplit = p.ksplit;
   t.kb_per_split = static_cast<int>(p.k_per_split);

@@ -137,7 +137,12 @@ class Engine {
     slice_limit_[1] = ring;
     slice_limit_[2] = other;
   }
-  void set_chunk(int k) { chunk_ = k; }
+  // MMAs per TMEM accumulation, in (k-block, slice pair) steps, for
+  // contractions with 3 slices and with fewer
+  void set_chunk(int three_slices, int fewer) {
+    chunk_ = three_slices;
+    chunk_lo_ = fewer;
+  }
   // Record CUDA events around every operation of EXEC passes.
   void set_profile(bool on) { profile_ = on; }
   // Tensors a residual program reads but never writes (its amplitude inputs);
@@ -207,7 +212,15 @@ class Engine {
   __nv_bfloat16* wbfa_ = nullptr;
   __nv_bfloat16* wbfb_ = nullptr;
   int* err_ = nullptr;
-  int chunk_ = 4;  // k-blocks per TMEM accumulation in the tensor-core GEMM
+  // (k-block, slice pair) steps per TMEM accumulation of the tensor-core GEMM.
+  // The tensor core's FP32 accumulation loses about an ulp of the running sum
+  // per MMA, so 3-slice contractions (split error ~2^-24) accumulate 4 steps
+  // at a time.  With 2 slices the split error (~2^-17) dominates even for 24
+  // steps (measured: max error 4.67e-6 at 4 steps, 4.68e-6 at 24, K = 10240),
+  // and the longer accumulations let the MMAs run further ahead of the
+  // epilogue warps that drain them: 10240^3 at 2 slices 5.25 -> 4.79 ms.
+  int chunk_ = 4;
+  int chunk_lo_ = 24;
   bool profile_ = false;
   std::unordered_set<const Tensor*> frozen_;
   std::unordered_map<std::string, std::vector<struct OperandPlan*>> pack_uses_;
