@@ -752,11 +752,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         g.t[t].a = op.terms[t].x.t->d;
         const std::vector<int64_t> hra = offsets(op.ext, e, op.terms[t].x), hca = offsets(op.kord, e, op.terms[t].x);
         if (t == 0) g.transpose = pick_transpose(hra, hca);
-        if (single) {
-          bool unit = reinterpret_cast<uintptr_t>(g.t[t].a) % 16 == 0;
-          for (size_t q = 0; unit && q < hca.size(); ++q) unit = hca[q] == static_cast<int64_t>(q);
-          g.cunit = unit ? 1 : 0;
-        }
+        gather_set_c4(g.t[t], hca.data(), static_cast<int64_t>(hca.size()));
         g.t[t].ra = upload(hra).d;
         g.t[t].ca = upload(hca).d;
       }

@@ -211,28 +211,25 @@ __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs g) {
 #undef GBCC_ROWS
 }
 
-// Plain single-term packs into BF16 slices (the common case), 4 consecutive
-// K elements of kSplitRows rows per thread step, all loads issued before the
-// stores.  A source that is contiguous along K (cunit) is read with 16-byte
-// vector loads where the row start is even; otherwise the K offsets are read
-// as 16-byte vectors and the elements one by one.  Every slice gets one 8-byte
-// store per thread and row; the launcher checks Cpad, ldo and slice_stride are
-// multiples of 4 (K is padded to 64) so the stores are 8-byte aligned.
+// Packs into BF16 slices, 4 consecutive K elements of kSplitRows rows per
+// thread step, all loads issued before the stores, any number of terms.  A
+// term whose K offsets run in contiguous, even-aligned groups of four (c4) is
+// read with two 16-byte vector loads per group where its row offset is even;
+// otherwise its K offsets are read as 16-byte vectors and the elements one by
+// one.  Every slice gets one 8-byte store per thread and row; the launcher
+// checks Cpad, ldo and slice_stride are multiples of 4 (K is padded to 64) so
+// the stores are 8-byte aligned.
 constexpr int kSplitRows = 2;
 
-__device__ __forceinline__ void split4_load(const GatherArgs& g, int64_t r, int64_t c, double x[4]) {
-  const double* __restrict__ a = g.t[0].a;
-  const int64_t* __restrict__ ca = g.t[0].ca;
-  if (r >= g.R) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) x[j] = 0.0;
-    return;
-  }
-  const int64_t rb = g.t[0].ra[r];
-  if (c + 3 < g.C) {
-    if (g.cunit && (rb & 1) == 0) {
-      const double2 v01 = *reinterpret_cast<const double2*>(a + rb + c);
-      const double2 v23 = *reinterpret_cast<const double2*>(a + rb + c + 2);
+// x[0..3] = the term's source at row offset rb and K elements c..c+3
+__device__ __forceinline__ void load4(const GatherTerm& T, int64_t rb, int64_t c, int64_t C, double x[4]) {
+  const double* __restrict__ a = T.a;
+  const int64_t* __restrict__ ca = T.ca;
+  if (c + 3 < C) {
+    if (T.c4 && (rb & 1) == 0) {
+      const int64_t o = ca[c];
+      const double2 v01 = *reinterpret_cast<const double2*>(a + rb + o);
+      const double2 v23 = *reinterpret_cast<const double2*>(a + rb + o + 2);
       x[0] = v01.x;
       x[1] = v01.y;
       x[2] = v23.x;
@@ -247,42 +244,95 @@ __device__ __forceinline__ void split4_load(const GatherArgs& g, int64_t r, int6
     }
   } else {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) x[j] = c + j < g.C ? a[rb + ca[c + j]] : 0.0;
+    for (int j = 0; j < 4; ++j) x[j] = c + j < C ? a[rb + ca[c + j]] : 0.0;
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 5) gather_split4_kernel(GatherArgs g) {
+// values of K elements c..c+3 of row r (0 outside R x C), NT terms as in gather_value
+template <int NT, bool PROD>
+__device__ __forceinline__ void split4_values(const GatherArgs& g, int64_t r, int64_t c, double v[4]) {
+  if (r >= g.R) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = 0.0;
+    return;
+  }
+  if constexpr (NT == 0) {
+    load4(g.t[0], g.t[0].ra[r], c, g.C, v);
+  } else if constexpr (NT < 0) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = c + j < g.C ? gather_value<NT, PROD>(g, r, c + j) : 0.0;
+  } else {
+    double x[NT][4];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const GatherTerm& T = g.t[t];
+      load4(T, T.ra[r], c, g.C, x[t]);
+      if constexpr (PROD) {
+        if (T.b) {
+          double y[4];
+          GatherTerm U = T;
+          U.a = T.b;
+          U.ca = T.cb;
+          U.c4 = 0;
+          load4(U, T.rb[r], c, g.C, y);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) x[t][j] *= y[j];
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      double val = term_scale(g.t[0], x[0][j]);
+#pragma unroll
+      for (int t = 1; t < NT; ++t) val += term_scale(g.t[t], x[t][j]);
+      v[j] = val;
+    }
+  }
+}
+
+// the 4 values split into BF16 slices, one 8-byte store per slice
+__device__ __forceinline__ void split4_store(const GatherArgs& g, int64_t r, int64_t c, const double v[4]) {
+  unsigned short* orow = reinterpret_cast<unsigned short*>(g.outs) + r * g.ldo;
+  unsigned short b[4][3];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) split_bits(v[j], b[j], g.nslices);
+#pragma unroll
+  for (int s = 0; s < 3; ++s) {
+    if (s >= g.nslices) break;
+    uint2 w;
+    w.x = static_cast<unsigned>(b[0][s]) | (static_cast<unsigned>(b[1][s]) << 16);
+    w.y = static_cast<unsigned>(b[2][s]) | (static_cast<unsigned>(b[3][s]) << 16);
+    *reinterpret_cast<uint2*>(orow + s * g.slice_stride + c) = w;
+  }
+}
+
+template <int NT, bool PROD>
+__device__ __forceinline__ void split4_rows(const GatherArgs& g) {
   const int64_t nq = g.Cpad / 4;
   const int64_t q0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t qstep = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const int64_t r0 = static_cast<int64_t>(blockIdx.y) * blockDim.y + threadIdx.y;
   const int64_t rstep = static_cast<int64_t>(gridDim.y) * blockDim.y;
-  const int ns = g.nslices;
   for (int64_t r = r0; r < g.Rpad; r += kSplitRows * rstep) {
     for (int64_t q = q0; q < nq; q += qstep) {
       const int64_t c = 4 * q;
-      double x[kSplitRows][4];
+      double v[kSplitRows][4];
 #pragma unroll
-      for (int u = 0; u < kSplitRows; ++u) split4_load(g, r + u * rstep, c, x[u]);
+      for (int u = 0; u < kSplitRows; ++u) split4_values<NT, PROD>(g, r + u * rstep, c, v[u]);
 #pragma unroll
       for (int u = 0; u < kSplitRows; ++u) {
         const int64_t ru = r + u * rstep;
         if (ru >= g.Rpad) break;
-        unsigned short* orow = reinterpret_cast<unsigned short*>(g.outs) + ru * g.ldo;
-        unsigned short b[4][3];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) split_bits(x[u][j], b[j], ns);
-#pragma unroll
-        for (int s = 0; s < 3; ++s) {
-          if (s >= ns) break;
-          uint2 w;
-          w.x = static_cast<unsigned>(b[0][s]) | (static_cast<unsigned>(b[1][s]) << 16);
-          w.y = static_cast<unsigned>(b[2][s]) | (static_cast<unsigned>(b[3][s]) << 16);
-          *reinterpret_cast<uint2*>(orow + s * g.slice_stride + c) = w;
-        }
+        split4_store(g, ru, c, v[u]);
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kThreads, 4) gather_split4_kernel(GatherArgs g) {
+#define GBCC_SPLIT4(N, P) split4_rows<N, P>(g)
+  GBCC_GATHER_DISPATCH(g, GBCC_SPLIT4);
+#undef GBCC_SPLIT4
 }
 
 // Same contract as gather_kernel for sources contiguous along R: a 32 x 32
@@ -292,6 +342,10 @@ template <int NT, bool PROD, bool RMW>
 __device__ __forceinline__ void gather_tiles(const GatherArgs& g, double (*tile)[33]) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int64_t nrt = (g.Rpad + 31) / 32, nct = (g.Cpad + 31) / 32;
+  // BF16-slice output with 4-aligned rows: each thread writes 4 consecutive
+  // columns of one row (one 8-byte store per slice) instead of one column
+  const bool wide = g.outs && ((g.Cpad | g.ldo | g.slice_stride) & 3) == 0 &&
+                    (reinterpret_cast<uintptr_t>(g.outs) & 7) == 0;
   for (int64_t t = blockIdx.x; t < nrt * nct; t += gridDim.x) {
     int64_t tr, tc;
     divmod32(t, nct, tr, tc);
@@ -303,6 +357,19 @@ __device__ __forceinline__ void gather_tiles(const GatherArgs& g, double (*tile)
       tile[ty + 8 * k][tx] = (r < g.R && c < g.C) ? gather_value<NT, PROD>(g, r, c) : 0.0;
     }
     __syncthreads();
+    if (wide) {
+      // thread (row rl, columns cg..cg+3); a warp covers 4 rows x 32 columns
+      const int t = ty * 32 + tx, rl = t >> 3, cg = (t & 7) * 4;
+      const int64_t r = r0 + rl, c = c0 + cg;
+      if (r < g.Rpad && c < g.Cpad) {
+        double v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = tile[cg + j][rl];
+        split4_store(g, r, c, v);
+      }
+      __syncthreads();
+      continue;
+    }
     // write: lanes along c
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -900,8 +967,12 @@ void launch_gather(const GatherArgs& g, cudaStream_t st) {
     gather_t_kernel<<<static_cast<unsigned>(grid), dim3(32, 8), 0, st>>>(g);
     return;
   }
-  if (g.outs && g.plain && g.Cpad % 4 == 0 && g.ldo % 4 == 0 && g.slice_stride % 4 == 0 &&
-      reinterpret_cast<uintptr_t>(g.outs) % 8 == 0 && reinterpret_cast<uintptr_t>(g.t[0].ca) % 16 == 0) {
+  bool tables16 = true;
+  for (int t = 0; t < g.nterms; ++t)
+    tables16 = tables16 && reinterpret_cast<uintptr_t>(g.t[t].ca) % 16 == 0 &&
+               (!g.t[t].b || reinterpret_cast<uintptr_t>(g.t[t].cb) % 16 == 0);
+  if (g.outs && tables16 && g.Cpad % 4 == 0 && g.ldo % 4 == 0 && g.slice_stride % 4 == 0 &&
+      reinterpret_cast<uintptr_t>(g.outs) % 8 == 0) {
     const int64_t nq = g.Cpad / 4;
     int bx = 32;
     while (bx < nq && bx < kThreads) bx <<= 1;

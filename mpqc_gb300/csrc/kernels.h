@@ -37,6 +37,9 @@ struct GatherTerm {
   int pow2;
   int pow2_k;
   unsigned long long pow2_sign;
+  // 1: ca runs in contiguous groups of four starting at even offsets and a is
+  // 16-byte aligned (vector loads of 4 K elements; set by gather_set_c4)
+  int c4;
 };
 
 // true when c = (-1)^neg 2^k exactly with |k| <= 64
@@ -73,14 +76,18 @@ struct GatherArgs {
   int transpose;
   // 1: one term, no second factor, coefficient 1 -- a plain load (set by the planner)
   int plain;
-  // 1 (plain packs only): the term's column offsets are 0, 1, 2, ... and its
-  // base is 16-byte aligned, so rows can be read with 16-byte vector loads
-  int cunit;
   // 1: some term has a second factor (b != nullptr)
   int products;
   // 1: some coefficient is not +-2^k (set by gather_finish)
   int general;
 };
+
+inline void gather_set_c4(GatherTerm& T, const int64_t* hca, int64_t n) {
+  bool ok = reinterpret_cast<uintptr_t>(T.a) % 16 == 0;
+  for (int64_t q = 0; ok && q + 3 < n; q += 4)
+    ok = hca[q] % 2 == 0 && hca[q + 1] == hca[q] + 1 && hca[q + 2] == hca[q] + 2 && hca[q + 3] == hca[q] + 3;
+  T.c4 = ok ? 1 : 0;
+}
 
 // derived flags of a filled GatherArgs (call after its terms are set)
 inline void gather_finish(GatherArgs& g) {
