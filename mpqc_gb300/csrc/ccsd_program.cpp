@@ -23,7 +23,9 @@
 //    (tau(c,d,k,i) = tau(d,c,i,k) for pair-symmetric amplitudes), so tmp2 is
 //    evaluated first;
 //  - h_kc(k,c) (2 t2(c,a,k,i) - t2(c,a,i,k) + t1(c,i) t1(a,k)) is not
-//    materialised: the t1 t1 part is t1(a,k) (h_kc(k,c) t1(c,i)).
+//    materialised: the t1 t1 part is t1(a,k) (h_kc(k,c) t1(c,i));
+//  - nor is T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l): the ring
+//    contractions pack its two terms directly.
 #include "ccsd_program.h"
 
 namespace gbcc {
@@ -56,7 +58,6 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v) {
   Y2 = &E.tensor("Y2", {o, o, v, o});
   gki = &E.tensor("gki", {o, o});
   gac = &E.tensor("gac", {v, v});
-  T = &E.tensor("T", {v, v, o, o});
   J = &E.tensor("J", {v, o, o, v});
   K = &E.tensor("K", {o, v, o, v});
   tmp = &E.tensor("tmp", {v, v, o, o});
@@ -146,15 +147,16 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   // reads and adds to it, while an elementwise pass pays little for the read.
   const Tensor& r2u = *S.r2u;
   const Tensor &J = *S.J, &K = *S.K;
-  // j and k intermediates (:229-249), T(d,b,i,l) = 0.5 t2(d,b,i,l) + t1(d,i) t1(b,l)
-  E.assign(ix(*S.T, "dbil"), 0.0, {f1(0.5, ix(t2, "dbil")), f2(1.0, ix(t1, "di"), ix(t1, "bl"))});
-  E.contract(ix(J, "akic"), 0.0, -1.0, {{1.0, ix(Gijab, "klcd")}}, {{1.0, ix(*S.T, "dail")}}, R);
+  // j and k intermediates (:229-249) with T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l),
+  // packed from its two terms where it is used (not stored)
+  const std::vector<Lin> T = {{0.5, ix(t2, "dail")}, lin2(1.0, ix(t1, "di"), ix(t1, "al"))};
+  E.contract(ix(J, "akic"), 0.0, -1.0, {{1.0, ix(Gijab, "klcd")}}, T, R);
   E.contract(ix(J, "akic"), 1.0, 0.5, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "kldc")}},
              {{1.0, ix(t2, "adil")}}, R);
   E.assign(ix(J, "akic"), 1.0, {f1(1.0, ix(Gijab, "ikac"))});
   E.contract(ix(J, "akic"), 1.0, -1.0, {{1.0, ix(Gijka, "lkic")}}, {{1.0, ix(t1, "al")}}, O);
   E.contract(ix(J, "akic"), 1.0, 1.0, {{1.0, ix(Giabc, "kacd")}}, {{1.0, ix(t1, "di")}}, O);
-  E.contract(ix(K, "kaic"), 0.0, -1.0, {{1.0, ix(Gijab, "kldc")}}, {{1.0, ix(*S.T, "dail")}}, R);
+  E.contract(ix(K, "kaic"), 0.0, -1.0, {{1.0, ix(Gijab, "kldc")}}, T, R);
   E.assign(ix(K, "kaic"), 1.0, {f1(1.0, ix(Giajb, "kaic"))});
   E.contract(ix(K, "kaic"), 1.0, -1.0, {{1.0, ix(Gijka, "klic")}}, {{1.0, ix(t1, "al")}}, O);
   E.contract(ix(K, "kaic"), 1.0, 1.0, {{1.0, ix(Giabc, "kadc")}}, {{1.0, ix(t1, "di")}}, O);
@@ -185,7 +187,8 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.contract(ix(r2u, "abij"), 1.0, 1.0, {{1.0, ix(*S.gac, "ac")}}, {{1.0, ix(t2, "cbij")}}, O);
   E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(*S.gki, "ki")}}, {{1.0, ix(t2, "abkj")}}, O);
   // tmp(a,b,i,j) = k(k,a,i,c) t2(c,b,j,k); r2 -= 0.5 tmp(a,b,i,j) + tmp(b,a,i,j)   (:254-256)
-  E.contract(ix(*S.tmp, "abij"), 0.0, 1.0, {{1.0, ix(K, "kaic")}}, {{1.0, ix(t2, "cbjk")}}, R);
+  // (t2(c,b,j,k) read as t2(b,c,k,j): its rows (b,j) then run along j in storage)
+  E.contract(ix(*S.tmp, "abij"), 0.0, 1.0, {{1.0, ix(K, "kaic")}}, {{1.0, ix(t2, "bckj")}}, R);
   E.assign(ix(r2u, "abij"), 1.0, {f1(-0.5, ix(*S.tmp, "abij")), f1(-1.0, ix(*S.tmp, "baij"))});
   // r2(a,b,i,j) = r2(a,b,i,j) + r2(b,a,j,i) + Gijab(i,j,a,b)   (:260-262)
   // (g_abij(a,b,i,j) = Gijab(i,j,a,b), stored in r2's order)

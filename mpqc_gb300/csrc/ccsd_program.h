@@ -13,7 +13,7 @@ struct CcsdTensors {
   // amplitudes and residuals
   Tensor *t1, *t2, *tau, *r1, *r2;
   // intermediates
-  Tensor *tki, *FAB, *FIJ, *hkc, *r2u, *Y1, *Y2, *gki, *gac, *T, *J, *K, *tmp, *W, *tmp2;
+  Tensor *tki, *FAB, *FIJ, *hkc, *r2u, *Y1, *Y2, *gki, *gac, *J, *K, *tmp, *W, *tmp2;
   // particle-particle ladder over pair-(anti)symmetric combinations: G+/G- of
   // Gabcd over (a <= b) x (c <= d) and of Giabc over (k a) x (c <= d)
   // (constants), tau+/tau- over (c <= d) x (i <= j), and the pair products

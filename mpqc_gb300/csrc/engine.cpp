@@ -640,12 +640,18 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     throw Error(GBCC_ERR_STATE, "engine: contract needs 1..4 terms per operand");
   Extents e;
   add_extents(e, c);
-  for (const auto& l : A) add_extents(e, l.x);
-  for (const auto& l : B) add_extents(e, l.x);
+  for (const auto* ops : {&A, &B})
+    for (const auto& l : *ops) {
+      add_extents(e, l.x);
+      if (l.y.t) add_extents(e, l.y);
+    }
+  // the first term of an operand is a single factor carrying all its indices
+  auto term_labels = [](const Lin& l) { return l.y.t ? l.x.lab + l.y.lab : l.x.lab; };
+  if (A[0].y.t || B[0].y.t) throw Error(GBCC_ERR_STATE, "engine: the first operand term must be one factor");
   for (const auto& l : A)
-    if (!same_set(l.x.lab, A[0].x.lab)) throw Error(GBCC_ERR_STATE, "engine: A terms differ in indices");
+    if (!same_set(term_labels(l), A[0].x.lab)) throw Error(GBCC_ERR_STATE, "engine: A terms differ in indices");
   for (const auto& l : B)
-    if (!same_set(l.x.lab, B[0].x.lab)) throw Error(GBCC_ERR_STATE, "engine: B terms differ in indices");
+    if (!same_set(term_labels(l), B[0].x.lab)) throw Error(GBCC_ERR_STATE, "engine: B terms differ in indices");
   const std::string la = A[0].x.lab, lb = B[0].x.lab;
   const std::string kset = set_and(la, lb);
   const std::string aext = set_minus(la, kset), bext = set_minus(lb, kset);
@@ -656,8 +662,8 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     throw Error(GBCC_ERR_STATE, "engine: output indices must be exactly the external ones (" + c.lab + ")");
   const int64_t rowsA = extent_of(e, aext), rowsB = extent_of(e, bext), K = extent_of(e, kset);
   bool constA = true, constB = true;
-  for (const auto& l : A) constA = constA && l.x.t->constant;
-  for (const auto& l : B) constB = constB && l.x.t->constant;
+  for (const auto& l : A) constA = constA && l.x.t->constant && (!l.y.t || l.y.t->constant);
+  for (const auto& l : B) constB = constB && l.x.t->constant && (!l.y.t || l.y.t->constant);
   const double flops = 2.0 * static_cast<double>(rowsA) * rowsB * K;
 
   for (int pm = 0; pm < 2; ++pm) {
@@ -703,8 +709,8 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     const Ix& bigM = Ms[0].x;
     const Ix& bigN = Ns[0].x;
     if (!p.use_tc) {
-      const bool dM = Ms.size() == 1 && storage_is_panel(bigM, mext);
-      const bool dN = Ns.size() == 1 && storage_is_panel(bigN, next);
+      const bool dM = Ms.size() == 1 && !Ms[0].y.t && storage_is_panel(bigM, mext);
+      const bool dN = Ns.size() == 1 && !Ns[0].y.t && storage_is_panel(bigN, next);
       if (dM && (!dN || bigM.t->size() >= bigN.t->size())) {
         PM.direct = true;
         PM.ext = order_by(mext, bigM.lab);
@@ -743,8 +749,8 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       GatherArgs& g = op.gather;
       std::memset(&g, 0, sizeof(g));
       g.nterms = static_cast<int>(op.terms.size());
-      // a single term packs as a plain copy; its coefficient scales alpha
-      const bool single = op.terms.size() == 1;
+      // a single one-factor term packs as a plain copy; its coefficient scales alpha
+      const bool single = op.terms.size() == 1 && !op.terms[0].y.t;
       if (single) coef_direct *= op.terms[0].coef;
       g.plain = single ? 1 : 0;
       for (size_t t = 0; t < op.terms.size(); ++t) {
@@ -755,6 +761,12 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         gather_set_c4(g.t[t], hca.data(), static_cast<int64_t>(hca.size()));
         g.t[t].ra = upload(hra).d;
         g.t[t].ca = upload(hca).d;
+        if (op.terms[t].y.t) {
+          g.products = 1;
+          g.t[t].b = op.terms[t].y.t->d;
+          g.t[t].rb = upload(offsets(op.ext, e, op.terms[t].y)).d;
+          g.t[t].cb = upload(offsets(op.kord, e, op.terms[t].y)).d;
+        }
       }
       gather_finish(g);
       g.R = op.rows;
@@ -833,10 +845,12 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
           bool frozen = true;
           std::string sig;
           for (const auto& l : op.terms) {
-            frozen = frozen && frozen_.count(l.x.t) > 0;
-            // a single term is packed unscaled (plain copy)
-            const double coef = op.terms.size() == 1 ? 1.0 : l.coef;
-            sig += l.x.t->name + "(" + l.x.lab + ")*" + std::to_string(coef) + ";";
+            frozen = frozen && frozen_.count(l.x.t) > 0 && (!l.y.t || frozen_.count(l.y.t) > 0);
+            // a single one-factor term is packed unscaled (plain copy)
+            const double coef = (op.terms.size() == 1 && !l.y.t) ? 1.0 : l.coef;
+            sig += l.x.t->name + "(" + l.x.lab + ")";
+            if (l.y.t) sig += l.y.t->name + "(" + l.y.lab + ")";
+            sig += "*" + std::to_string(coef) + ";";
           }
           if (frozen) {
             op.sig = sig + op.ext + "|" + op.kord + "|" + std::to_string(slices) + "|" +

@@ -83,10 +83,14 @@ struct Factor {
 inline Factor f1(double c, const Ix& a) { return Factor{c, a, Ix{}}; }
 inline Factor f2(double c, const Ix& a, const Ix& b) { return Factor{c, a, b}; }
 
+// coef * x [* y]: a term of a contraction operand; a second factor y (its
+// labels among the operand's) makes an outer-product term such as t1(d,i) t1(a,l)
 struct Lin {
   double coef;
   Ix x;
+  Ix y{};
 };
+inline Lin lin2(double c, const Ix& x, const Ix& y) { return Lin{c, x, y}; }
 
 enum TermClass { kClassLadder = 0, kClassRing = 1, kClassOther = 2 };
 
