@@ -638,13 +638,39 @@ __global__ void __launch_bounds__(kThreads) jacobi_inplace_kernel(int64_t o, int
   }
 }
 
-// out[0] = max |t2(a,b,i,j) - t2(b,a,j,i)|, out[1] = max |t2| (out zeroed by
-// the caller), maxima combined as in maxabs_diff_kernel
+// |x| as its bit pattern: for non-negative doubles the unsigned order of the
+// bits is the order of the values (NaN above infinity), so maxima of |x| are
+// integer maxima and take no FP64 instruction
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// block maxima of two bit patterns, combined into out[0..1] with atomicMax
+__device__ __forceinline__ void block_max2_bits(unsigned long long md, unsigned long long mb,
+                                                unsigned long long* out) {
+  __shared__ unsigned long long sd[kThreads], sb[kThreads];
+  sd[threadIdx.x] = md;
+  sb[threadIdx.x] = mb;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sd[threadIdx.x] = max(sd[threadIdx.x], sd[threadIdx.x + w]);
+      sb[threadIdx.x] = max(sb[threadIdx.x], sb[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    atomicMax(out, sd[0]);
+    atomicMax(out + 1, sb[0]);
+  }
+}
+
+// out[0] = bits of max |t2(a,b,i,j) - t2(b,a,j,i)|, out[1] = bits of max |t2|
+// (out zeroed by the caller); a NaN anywhere makes the maximum a NaN
 __global__ void __launch_bounds__(kThreads) pair_asym_kernel(int64_t o, int64_t v, const double* t2,
                                                              unsigned long long* out) {
-  __shared__ double sd[kThreads], sb[kThreads];
   const int64_t o2 = o * o;
-  double md = 0.0, mb = 0.0;
+  unsigned long long md = 0ull, mb = 0ull;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
     int64_t a, b;
     divmod32(p, v, a, b);
@@ -653,52 +679,27 @@ __global__ void __launch_bounds__(kThreads) pair_asym_kernel(int64_t o, int64_t 
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
       int64_t i, j;
       divmod32(ij, o, i, j);
-      md = fmax(md, fabs(x[ij] - y[j * o + i]));
-      mb = fmax(mb, fabs(x[ij]));
+      const double xv = x[ij];
+      md = max(md, abs_bits(xv - y[j * o + i]));
+      mb = max(mb, abs_bits(xv));
     }
   }
-  sd[threadIdx.x] = md;
-  sb[threadIdx.x] = mb;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      sd[threadIdx.x] = fmax(sd[threadIdx.x], sd[threadIdx.x + w]);
-      sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + w]);
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(sd[0])));
-    atomicMax(out + 1, static_cast<unsigned long long>(__double_as_longlong(sb[0])));
-  }
+  block_max2_bits(md, mb, out);
 }
 
-// out[0] = max |a - b|, out[1] = max |b| (out zeroed by the caller): block
+// out[0] = bits of max |a - b|, out[1] = bits of max |b| (out zeroed by the caller): block
 // maxima combined with atomicMax on the bit patterns, which order like the
 // values for non-negative doubles
 __global__ void __launch_bounds__(kThreads) maxabs_diff_kernel(int64_t n, const double* a, const double* b,
                                                                unsigned long long* out) {
-  __shared__ double sd[kThreads], sb[kThreads];
-  double md = 0.0, mb = 0.0;
+  unsigned long long md = 0ull, mb = 0ull;
   for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
        e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    md = fmax(md, fabs(a[e] - b[e]));
-    mb = fmax(mb, fabs(b[e]));
+    const double bv = b[e];
+    md = max(md, abs_bits(a[e] - bv));
+    mb = max(mb, abs_bits(bv));
   }
-  sd[threadIdx.x] = md;
-  sb[threadIdx.x] = mb;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      sd[threadIdx.x] = fmax(sd[threadIdx.x], sd[threadIdx.x + w]);
-      sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + w]);
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(sd[0])));
-    atomicMax(out + 1, static_cast<unsigned long long>(__double_as_longlong(sb[0])));
-  }
+  block_max2_bits(md, mb, out);
 }
 
 // ---------------------------------------------------------------------------
