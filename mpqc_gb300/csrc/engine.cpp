@@ -395,6 +395,7 @@ void Engine::assign(const Ix& c, double beta, const std::vector<Factor>& terms) 
     T.a = terms[t].a.t->d;
     const std::vector<int64_t> hra = offsets(rlab, e, terms[t].a), hca = offsets(clab, e, terms[t].a);
     if (t == 0) g.transpose = pick_transpose(hra, hca);
+    gather_set_c4(T, hca.data(), static_cast<int64_t>(hca.size()));
     T.ra = upload(hra).d;
     T.ca = upload(hca).d;
     if (terms[t].b.t) {

@@ -306,7 +306,8 @@ __device__ __forceinline__ void split4_store(const GatherArgs& g, int64_t r, int
   }
 }
 
-template <int NT, bool PROD>
+// OUT 0: BF16 slices; 1: FP64 stores; 2: FP64 read-modify-write (beta)
+template <int NT, bool PROD, int OUT>
 __device__ __forceinline__ void split4_rows(const GatherArgs& g) {
   const int64_t nq = g.Cpad / 4;
   const int64_t q0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -317,22 +318,53 @@ __device__ __forceinline__ void split4_rows(const GatherArgs& g) {
     for (int64_t q = q0; q < nq; q += qstep) {
       const int64_t c = 4 * q;
       double v[kSplitRows][4];
+      double2 old[kSplitRows][2];
 #pragma unroll
-      for (int u = 0; u < kSplitRows; ++u) split4_values<NT, PROD>(g, r + u * rstep, c, v[u]);
+      for (int u = 0; u < kSplitRows; ++u) {
+        const int64_t ru = r + u * rstep;
+        split4_values<NT, PROD>(g, ru, c, v[u]);
+        if constexpr (OUT == 2) {
+          if (ru < g.Rpad) {
+            const double2* po = reinterpret_cast<const double2*>(g.out + ru * g.ldo + c);
+            old[u][0] = po[0];
+            old[u][1] = po[1];
+          }
+        }
+      }
 #pragma unroll
       for (int u = 0; u < kSplitRows; ++u) {
         const int64_t ru = r + u * rstep;
         if (ru >= g.Rpad) break;
-        split4_store(g, ru, c, v[u]);
+        if constexpr (OUT == 0) {
+          split4_store(g, ru, c, v[u]);
+        } else {
+          double2* po = reinterpret_cast<double2*>(g.out + ru * g.ldo + c);
+          if constexpr (OUT == 2) {
+            po[0] = make_double2(fma(g.beta, old[u][0].x, v[u][0]), fma(g.beta, old[u][0].y, v[u][1]));
+            po[1] = make_double2(fma(g.beta, old[u][1].x, v[u][2]), fma(g.beta, old[u][1].y, v[u][3]));
+          } else {
+            po[0] = make_double2(v[u][0], v[u][1]);
+            po[1] = make_double2(v[u][2], v[u][3]);
+          }
+        }
       }
     }
   }
 }
 
+// 4 K elements per thread into BF16 slices
 __global__ void __launch_bounds__(kThreads, 4) gather_split4_kernel(GatherArgs g) {
-#define GBCC_SPLIT4(N, P) split4_rows<N, P>(g)
+#define GBCC_SPLIT4(N, P) split4_rows<N, P, 0>(g)
   GBCC_GATHER_DISPATCH(g, GBCC_SPLIT4);
 #undef GBCC_SPLIT4
+}
+
+// 4 columns per thread into 16-byte aligned FP64 rows (assignments, FP64 panels)
+__global__ void __launch_bounds__(kThreads, 3) gather4_f64_kernel(GatherArgs g) {
+  const bool rmw = g.beta != 0.0;
+#define GBCC_F64X4(N, P) (rmw ? split4_rows<N, P, 2>(g) : split4_rows<N, P, 1>(g))
+  GBCC_GATHER_DISPATCH(g, GBCC_F64X4);
+#undef GBCC_F64X4
 }
 
 // Same contract as gather_kernel for sources contiguous along R: a 32 x 32
@@ -972,15 +1004,18 @@ void launch_gather(const GatherArgs& g, cudaStream_t st) {
   for (int t = 0; t < g.nterms; ++t)
     tables16 = tables16 && reinterpret_cast<uintptr_t>(g.t[t].ca) % 16 == 0 &&
                (!g.t[t].b || reinterpret_cast<uintptr_t>(g.t[t].cb) % 16 == 0);
-  if (g.outs && tables16 && g.Cpad % 4 == 0 && g.ldo % 4 == 0 && g.slice_stride % 4 == 0 &&
-      reinterpret_cast<uintptr_t>(g.outs) % 8 == 0) {
+  const bool split_ok = g.outs && g.slice_stride % 4 == 0 && reinterpret_cast<uintptr_t>(g.outs) % 8 == 0;
+  const bool fp64_ok = g.out && reinterpret_cast<uintptr_t>(g.out) % 16 == 0;
+  if ((split_ok || fp64_ok) && tables16 && g.Cpad % 4 == 0 && g.ldo % 4 == 0) {
     const int64_t nq = g.Cpad / 4;
     int bx = 32;
     while (bx < nq && bx < kThreads) bx <<= 1;
     const int by = kThreads / bx;
     const int64_t gx = std::min<int64_t>((nq + bx - 1) / bx, 152LL * 64);
     const int64_t gy = std::min<int64_t>({(g.Rpad + by - 1) / by, std::max<int64_t>(1, 152LL * 64 / gx), 65535LL});
-    gather_split4_kernel<<<dim3(static_cast<unsigned>(gx), static_cast<unsigned>(gy)), dim3(bx, by), 0, st>>>(g);
+    const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy)), block(bx, by);
+    if (g.outs) gather_split4_kernel<<<grid, block, 0, st>>>(g);
+    else gather4_f64_kernel<<<grid, block, 0, st>>>(g);
     return;
   }
   int bx = 1;
