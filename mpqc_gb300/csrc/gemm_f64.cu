@@ -241,6 +241,73 @@ __global__ void __launch_bounds__(256, 2) gemm_smallk_kernel(GemmF64Args g) {
   }
 }
 
+// Short contractions whose C is contiguous along M (every short-K site of the
+// CCSD residual): B (N x K, rounded to FP32, K padded to 32) stays in shared
+// memory, each thread owns one row m of C and keeps that row of A in
+// registers, and walks C eight columns at a time.  The eight C loads of a
+// group are issued before its dot products (which do not need them), and
+// three CTAs per SM keep enough of them in flight to stream C, the dominant
+// traffic (16 bytes per output against 8 per A element).  BETA 0: C = alpha
+// acc, 1: C += alpha acc, 2: C = beta C + alpha acc, one FP64 FMA per output
+// where beta is 0 or 1.
+constexpr int kStreamK = 32;
+constexpr int kStreamCols = 8;
+
+template <int BETA>
+__global__ void __launch_bounds__(256, 3) gemm_smallk_stream_kernel(GemmF64Args g) {
+  extern __shared__ float Bs[];  // [Npad][kStreamK]
+  const int K = static_cast<int>(g.K);
+  const int64_t npad = (g.N + kStreamCols - 1) / kStreamCols * kStreamCols;
+  for (int64_t e = threadIdx.x; e < npad * kStreamK; e += blockDim.x) {
+    const int64_t n = e / kStreamK;
+    const int k = static_cast<int>(e % kStreamK);
+    Bs[e] = (n < g.N && k < K) ? d2f_rn(g.B[n * g.ldb + k]) : 0.f;
+  }
+  __syncthreads();
+  const int64_t mtiles = (g.M + blockDim.x - 1) / blockDim.x;
+  for (int64_t t = blockIdx.x; t < mtiles; t += gridDim.x) {
+    const int64_t m = t * blockDim.x + threadIdx.x;
+    if (m >= g.M) continue;
+    float a[kStreamK];
+#pragma unroll
+    for (int k = 0; k < kStreamK; ++k) a[k] = k < K ? d2f_rn(g.A[m * g.lda + k]) : 0.f;
+    double* crow = g.C + g.cm[m];
+    for (int64_t n0 = 0; n0 < g.N; n0 += kStreamCols) {
+      // (the column offsets are read again at the store, from L1, rather
+      // than held: 8 live 64-bit offsets pushed the kernel into spills)
+      double c[kStreamCols];
+      if constexpr (BETA != 0) {
+#pragma unroll
+        for (int j = 0; j < kStreamCols; ++j) c[j] = n0 + j < g.N ? crow[g.cn[n0 + j]] : 0.0;
+      }
+      float acc[kStreamCols];
+#pragma unroll
+      for (int j = 0; j < kStreamCols; ++j) {
+        const float4* b4 = reinterpret_cast<const float4*>(Bs + (n0 + j) * kStreamK);
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < kStreamK / 4; ++q) {
+          const float4 b = b4[q];
+          s = fmaf(a[4 * q], b.x, s);
+          s = fmaf(a[4 * q + 1], b.y, s);
+          s = fmaf(a[4 * q + 2], b.z, s);
+          s = fmaf(a[4 * q + 3], b.w, s);
+        }
+        acc[j] = s;
+      }
+#pragma unroll
+      for (int j = 0; j < kStreamCols; ++j) {
+        if (n0 + j >= g.N) continue;
+        double* p = crow + g.cn[n0 + j];
+        const double y = f2d_bits(acc[j]);
+        if constexpr (BETA == 0) *p = g.alpha * y;
+        else if constexpr (BETA == 1) *p = fma(g.alpha, y, c[j]);
+        else *p = fma(g.alpha, y, g.beta * c[j]);
+      }
+    }
+  }
+}
+
 template <int TM, int TN>
 void launch_smallk_tiles(const GemmF64Args& g, cudaStream_t st) {
   const int64_t tiles = ((g.M + TM - 1) / TM) * ((g.N + TN - 1) / TN);
@@ -253,6 +320,23 @@ void launch_smallk_tiles(const GemmF64Args& g, cudaStream_t st) {
 
 void launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return;
+  const int64_t npad = (g.N + kStreamCols - 1) / kStreamCols * kStreamCols;
+  const size_t smem = static_cast<size_t>(npad) * kStreamK * sizeof(float);
+  if (g.m_major && g.K <= kStreamK && smem <= 64 * 1024) {
+    const int64_t mtiles = (g.M + 255) / 256;
+    const unsigned grid = static_cast<unsigned>(std::min<int64_t>(mtiles, static_cast<int64_t>(num_sms()) * 3));
+    if (g.beta == 0.0) {
+      cudaFuncSetAttribute(gemm_smallk_stream_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      gemm_smallk_stream_kernel<0><<<grid, 256, smem, st>>>(g);
+    } else if (g.beta == 1.0) {
+      cudaFuncSetAttribute(gemm_smallk_stream_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      gemm_smallk_stream_kernel<1><<<grid, 256, smem, st>>>(g);
+    } else {
+      cudaFuncSetAttribute(gemm_smallk_stream_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      gemm_smallk_stream_kernel<2><<<grid, 256, smem, st>>>(g);
+    }
+    return;
+  }
   if (g.N <= 32)
     launch_smallk_tiles<128, 32>(g, st);
   else
