@@ -114,8 +114,10 @@ def reference_arm(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
+        # the workload of the GPU arm; each step times a bounded sample of it
         "config": {"workload": "synthetic CCSD doubles residual, one R1+R2 evaluation",
-                   "o": o, "v": v, "naux": naux, "note": "bounded CPU sample of the o=32 v=320 workload"},
+                   "o": args.o, "v": args.v, "naux": args.naux, "parallelism": f"{cpu_threads()} host threads",
+                   "sample": {"o": o, "v": v, "naux": naux}},
         "cpu_baseline": {"value": rate, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
                          "sample": f"one FP64 R1+R2 residual at o={o} v={v} naux={naux} per step "
                                    "(numpy/OpenBLAS restatement of the reference's CPU CCSD)"},
