@@ -450,19 +450,19 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
             // the leader's full barrier counts the bytes of both CTAs
             const uint32_t bar = full0 + static_cast<uint32_t>(s) * 8u;
             if (leader) mbar_expect_tx(&full[s], 2 * Cfg::kStageBytes);
-            tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kAStage, kb * BK, m0, g.pa[pr]);
-            tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBStage, kb * BK, nb0, g.pb[pr]);
+            tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kAStage, 0, m0, g.pa[pr] * kblocks + kb);
+            tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBStage, 0, nb0, g.pb[pr] * kblocks + kb);
           } else if constexpr (SPS == 1) {
             mbar_expect_tx(&full[s], Cfg::kStageBytes);
-            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage, kb * BK, m0, g.pa[pr]);
-            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage, kb * BK, nb0, g.pb[pr]);
+            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage, 0, m0, g.pa[pr] * kblocks + kb);
+            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage, 0, nb0, g.pb[pr] * kblocks + kb);
           } else {
             // every slice of A and B of this k-block
             mbar_expect_tx(&full[s], Cfg::kStageBytes);
 #pragma unroll
             for (int j = 0; j < SPS; ++j) {
-              tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage + j * Cfg::kABytes, kb * BK, m0, j);
-              tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage + j * Cfg::kBBytes, kb * BK, nb0, j);
+              tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage + j * Cfg::kABytes, 0, m0, j * kblocks + kb);
+              tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage + j * Cfg::kBBytes, 0, nb0, j * kblocks + kb);
             }
           }
           if (SPS > 1 || ++pr == g.npairs) {
@@ -836,13 +836,17 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
+// Operand panels are k-block major per slice, [Kpad/64][rows][64] BF16, so a
+// box of 64 K elements x box_rows rows is one contiguous run; the slice
+// stride is (Kpad/64) times the k-block stride, so (k-block, slice) fold into
+// the third coordinate: slice * (Kpad/64) + k-block.
 bool make_map(CUtensorMap* map, const void* base, int64_t slices, int64_t rows, int64_t kpad,
               int box_rows) {
   auto fn = encode_fn();
   if (!fn) return false;
-  cuuint64_t dims[3] = {static_cast<cuuint64_t>(kpad), static_cast<cuuint64_t>(rows),
-                        static_cast<cuuint64_t>(slices)};
-  cuuint64_t strides[2] = {static_cast<cuuint64_t>(kpad * 2), static_cast<cuuint64_t>(rows * kpad * 2)};
+  cuuint64_t dims[3] = {static_cast<cuuint64_t>(BK), static_cast<cuuint64_t>(rows),
+                        static_cast<cuuint64_t>(slices * (kpad / BK))};
+  cuuint64_t strides[2] = {static_cast<cuuint64_t>(BK * 2), static_cast<cuuint64_t>(rows * BK * 2)};
   cuuint32_t box[3] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(box_rows), 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,

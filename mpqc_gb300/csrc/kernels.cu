@@ -92,6 +92,13 @@ __device__ __forceinline__ void split_bits(double x, unsigned short* out, int ns
   out[2] = static_cast<unsigned short>(bf16_rne(r));
 }
 
+// Element (r, c) of a BF16 slice panel, k-block major: [Cpad / 64][Rpad][64]
+// per slice, so that a 64-wide k-block of consecutive rows (one TMA box of
+// the tensor-core GEMM) is a contiguous run of memory.  Cpad is a multiple of 64.
+__device__ __forceinline__ int64_t panel_index(const GatherArgs& g, int64_t r, int64_t c) {
+  return (c >> 6) * (g.Rpad << 6) + (r << 6) + (c & 63);
+}
+
 __device__ __forceinline__ void split_store(double x, __nv_bfloat16* out, int nslices,
                                             int64_t slice_stride, int64_t idx) {
   unsigned short b[3];
@@ -197,7 +204,7 @@ __device__ __forceinline__ void gather_rows(const GatherArgs& g) {
           if constexpr (RMW) g.out[ru * g.ldo + c] = fma(g.beta, old[u], val[u]);
           else g.out[ru * g.ldo + c] = val[u];
         } else {
-          split_store(val[u], g.outs, g.nslices, g.slice_stride, ru * g.ldo + c);
+          split_store(val[u], g.outs, g.nslices, g.slice_stride, panel_index(g, ru, c));
         }
       }
     }
@@ -292,7 +299,7 @@ __device__ __forceinline__ void split4_values(const GatherArgs& g, int64_t r, in
 
 // the 4 values split into BF16 slices, one 8-byte store per slice
 __device__ __forceinline__ void split4_store(const GatherArgs& g, int64_t r, int64_t c, const double v[4]) {
-  unsigned short* orow = reinterpret_cast<unsigned short*>(g.outs) + r * g.ldo;
+  unsigned short* o4 = reinterpret_cast<unsigned short*>(g.outs) + panel_index(g, r, c);
   unsigned short b[4][3];
 #pragma unroll
   for (int j = 0; j < 4; ++j) split_bits(v[j], b[j], g.nslices);
@@ -302,7 +309,7 @@ __device__ __forceinline__ void split4_store(const GatherArgs& g, int64_t r, int
     uint2 w;
     w.x = static_cast<unsigned>(b[0][s]) | (static_cast<unsigned>(b[1][s]) << 16);
     w.y = static_cast<unsigned>(b[2][s]) | (static_cast<unsigned>(b[3][s]) << 16);
-    *reinterpret_cast<uint2*>(orow + s * g.slice_stride + c) = w;
+    *reinterpret_cast<uint2*>(o4 + s * g.slice_stride) = w;
   }
 }
 
@@ -413,7 +420,7 @@ __device__ __forceinline__ void gather_tiles(const GatherArgs& g, double (*tile)
           if constexpr (RMW) *p = fma(g.beta, *p, val);
           else *p = val;
         } else {
-          split_store(val, g.outs, g.nslices, g.slice_stride, r * g.ldo + c);
+          split_store(val, g.outs, g.nslices, g.slice_stride, panel_index(g, r, c));
         }
       }
     }

@@ -67,7 +67,9 @@ struct GatherArgs {
   double* out;
   int64_t ldo;
   double beta;
-  // split output (outs != nullptr): nslices BF16 slices, slice s at outs + s*slice_stride
+  // split output (outs != nullptr): nslices BF16 slices, slice s at
+  // outs + s*slice_stride, each k-block major ([Cpad/64][Rpad][64], Cpad a
+  // multiple of 64: the tensor-core GEMM's operand layout; ldo unused)
   __nv_bfloat16* outs;
   int nslices;
   int64_t slice_stride;
