@@ -153,3 +153,50 @@ def test_device_term_scaling_is_the_ieee_product(gbcc_lib, coef):
     bad = np.nonzero((np.isnan(out) != nan) | (~nan & (out.view(np.uint64) != ref.view(np.uint64))))[0]
     assert bad.size == 0, [(hex(x[i:i + 1].view(np.uint64)[0]), hex(out[i:i + 1].view(np.uint64)[0]),
                             hex(ref[i:i + 1].view(np.uint64)[0])) for i in bad[:6]]
+
+
+def scale_pow2_bits(x, k):
+    """Integer transcription of the packing kernels' x * 2^k on the bit
+    pattern (fp_bits.cuh: scale_pow2 / scale_pow2_rare): exponent shift for
+    normal results, round-to-nearest-even into the subnormals, overflow to
+    infinity; zeros, infinities and NaN unchanged."""
+    M52 = (1 << 52) - 1
+    b = int(np.float64(x).view(np.uint64))
+    m, sign = b & ((1 << 63) - 1), b & (1 << 63)
+    e = m >> 52
+    if m == 0 or e == 0x7FF:
+        return np.float64(x)
+    if e != 0 and 1 <= e + k <= 0x7FE:
+        return np.uint64(b + (k << 52)).view(np.float64)
+    s = ((m & M52) | (1 << 52)) if e else m
+    q = (e - 1 if e else 0) + k
+    lz = (64 - s.bit_length()) - 11
+    s <<= lz
+    q -= lz
+    if q >= 0x7FE:
+        r = 0x7FF << 52
+    elif q >= 0:
+        r = ((q + 1) << 52) | (s & M52)
+    else:
+        sh = -q
+        if sh > 54:
+            r = 0
+        else:
+            lo, rem, half = s >> sh, s & ((1 << sh) - 1), 1 << (sh - 1)
+            r = lo + (1 if (rem > half or (rem == half and (lo & 1))) else 0)
+    return np.uint64(sign | r).view(np.float64)
+
+
+@pytest.mark.parametrize("k", [0, 1, -1, 2, -2, 5, -60, 60])
+def test_integer_power_of_two_scaling_is_the_ieee_product(k):
+    """The algorithm the packing kernels use for power-of-two coefficients
+    (checked on the device by test_device_term_scaling_is_the_ieee_product)
+    rounds exactly as the IEEE product, across the normal range, into and out
+    of the subnormals and up to overflow."""
+    x = scale_sample(seed=abs(k) + (k < 0))
+    with np.errstate(over="ignore", under="ignore", invalid="ignore"):
+        ref = x * np.float64(2.0) ** k
+    got = np.array([scale_pow2_bits(v, k) for v in x])
+    nan = np.isnan(ref)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got[~nan].view(np.uint64), ref[~nan].view(np.uint64))
