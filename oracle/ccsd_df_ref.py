@@ -87,7 +87,7 @@ def compute_cs_ccsd_r2_df(t1, t2, tau, ints: Integrals, Xai, Xab, Xij):
     r2 = r2 + 0.5 * _es("akic,cbkj->abij", u, w)
     tmp = _es("kaic,cbjk->abij", k_kaic, t2)
     r2 = r2 - (0.5 * tmp + _es("baij->abij", tmp))
-    # symmetrise and add the driver, :368-369
+    # symmetrise and add Gijab(i,j,a,b), :368-369
     r2 = r2 + _es("baji->abij", r2)
     r2 = r2 + _es("ijab->abij", ints.Gijab)
     # hole-hole ladder, :371-377

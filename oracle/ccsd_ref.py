@@ -176,7 +176,7 @@ def compute_cs_ccsd_r2(t1, t2, tau, ints: Integrals):
     r2 = r2 + 0.5 * _es("akic,cbkj->abij", u, w)
     tmp = _es("kaic,cbjk->abij", k_kaic, t2)
     r2 = r2 - (0.5 * tmp + _es("baij->abij", tmp))
-    # symmetrise and add the driver, :259-262
+    # symmetrise and add Gijab(i,j,a,b), :259-262
     r2 = r2 + _es("baji->abij", r2)
     r2 = r2 + _es("ijab->abij", ints.Gijab)
     # hole-hole ladder, :264-270

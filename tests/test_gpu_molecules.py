@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 CASES = [("h2o_631g", False), ("h2o_ccpvdz", False), ("h2o_ccpvdz", True)]
 
-# BASELINE configuration 0 geometry: O (0, 0, 0.1173), H (0, +-0.7572, -0.4692) Angstrom
+# single-water benchmark geometry: O (0, 0, 0.1173), H (0, +-0.7572, -0.4692) Angstrom
 WATER_C0_XYZ = "3\n\nO 0 0 0.1173\nH 0 0.7572 -0.4692\nH 0 -0.7572 -0.4692\n"
 
 
