@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 CASES = [("h2o_631g", False), ("h2o_ccpvdz", False), ("h2o_ccpvdz", True)]
 
 # single-water benchmark geometry: O (0, 0, 0.1173), H (0, +-0.7572, -0.4692) Angstrom
-WATER_C0_XYZ = "3\n\nO 0 0 0.1173\nH 0 0.7572 -0.4692\nH 0 -0.7572 -0.4692\n"
+WATER_BENCH_XYZ = "3\n\nO 0 0 0.1173\nH 0 0.7572 -0.4692\nH 0 -0.7572 -0.4692\n"
 
 
 def _case(name, frozen):
@@ -73,7 +73,7 @@ def test_residual_at_converged_amplitudes(name):
 def test_water_config0_geometry_against_oracle():
     """cc-pVDZ water at the configuration-0 geometry, no frozen core (o=5, v=19):
     converge to 1e-10 and compare E_corr and T2 with the oracle."""
-    scf, blocks, eo, ev, nfz = M.molecular_inputs(WATER_C0_XYZ, "cc-pVDZ", frozen_core=False)
+    scf, blocks, eo, ev, nfz = M.molecular_inputs(WATER_BENCH_XYZ, "cc-pVDZ", frozen_core=False)
     assert (len(eo), len(ev), scf.C.shape[0]) == (5, 19, 24)
     ora = R.solve_ccsd(R.Integrals(**blocks), eo, ev, target_precision=1e-10, max_iter=60)
     with Solver(5, 19, target_precision=1e-10, max_iter=60) as s:
