@@ -70,8 +70,8 @@ def test_residual_at_converged_amplitudes(name):
     assert abs(e - float(g["oracle_e_ccsd"])) < 1e-10 and err < 1e-10
 
 
-def test_water_config0_geometry_against_oracle():
-    """cc-pVDZ water at the configuration-0 geometry, no frozen core (o=5, v=19):
+def test_water_benchmark_geometry_against_oracle():
+    """cc-pVDZ water at the single-water benchmark geometry, no frozen core (o=5, v=19):
     converge to 1e-10 and compare E_corr and T2 with the oracle."""
     scf, blocks, eo, ev, nfz = M.molecular_inputs(WATER_BENCH_XYZ, "cc-pVDZ", frozen_core=False)
     assert (len(eo), len(ev), scf.C.shape[0]) == (5, 19, 24)
