@@ -133,7 +133,7 @@ def test_golden_solve():
 
 
 def test_flop_count_matches_contraction_list():
-    # C1 synthetic residual o=32, v=320: 3.53e13 FLOP (61 % ladder)
+    # the synthetic o=32, v=320 residual: 3.53e13 FLOP (61 % ladder)
     f = R.flop_count(32, 320)
     assert abs(f - 3.53e13) / 3.53e13 < 0.01
     assert abs(2 * 32**2 * 320**4 / f - 0.61) < 0.01
