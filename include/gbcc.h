@@ -162,17 +162,21 @@ gbcc_status gbcc_energy(gbcc_handle* h, const double* t1_ai, const double* t2_ab
                         double* error);
 
 /* Allocation-free form of gbcc_energy, for callers that cannot allocate GPU
- * memory when they test convergence (a host framework that owns a fixed
- * device pool, or code running while a stream is captured into a CUDA
- * graph).  It needs no handle: every argument is device memory owned by the
+ * memory when they test convergence: a host framework that owns one fixed
+ * device pool and forbids later allocation, or a caller that cannot accept
+ * the device-wide synchronisation a cudaMalloc may cause.  It needs no
+ * handle: every argument is device memory of the stream's device owned by the
  * caller -- f_ai [v][o], g_abij [v][v][o][o], t1 [v][o], tau [v][v][o][o],
  * r1 [v][o], r2 [v][v][o][o] in, out[0] = energy and out[1] = residual error
- * (as gbcc_energy) written -- and the kernels are enqueued on `stream` (a
+ * (as gbcc_energy) written; any other pointer (host memory, another device)
+ * gives GBCC_ERR_INVALID_ARG -- and the kernels are enqueued on `stream` (a
  * cudaStream_t; NULL = the legacy default stream) without synchronising.
  * Partial sums go to a fixed 8 MiB __device__ array, so v <= 512 (larger v is
  * rejected with GBCC_ERR_INVALID_ARG).  Calls that overlap on the GPU share
- * that array and race; the first call on a device must precede any stream
- * capture.  No counterpart in the reference. */
+ * that array and race.  The first call on a device (and again in a new CUDA
+ * context of it, e.g. after cudaDeviceReset) looks up the array's address;
+ * make that first call before any stream capture begins.  No counterpart in
+ * the reference. */
 gbcc_status gbcc_energy_noalloc(int64_t o, int64_t v, const double* f_ai, const double* g_abij,
                                 const double* t1_ai, const double* tau_abij, const double* r1_ai,
                                 const double* r2_abij, double* out, void* stream);

@@ -1,12 +1,14 @@
 // Allocation-free evaluation of the CCSD energy functional and residual norm.
 //
 // Some callers cannot call cudaMalloc at the point where they need the
-// convergence test: a host framework that hands the GPU a fixed memory pool
-// and forbids further allocation, or code running while a stream is being
-// captured into a CUDA graph, where a cudaMalloc would break the capture.
-// gbcc_energy_noalloc serves them: the caller passes every input and the
-// output in its own device memory, and the per-pair partial sums live in a
-// file-scope __device__ array instead of allocated scratch.
+// convergence test.  A host framework may hand the GPU one fixed memory pool
+// at start-up and forbid any later allocation (MPQC-style drivers that size
+// the device pool to the integrals they keep resident), and cudaMalloc may
+// synchronise the whole device, which a caller overlapping the test with work
+// on other streams cannot afford.  gbcc_energy_noalloc serves them: the caller
+// passes every input and the output in its own device memory, and the
+// per-pair partial sums live in a file-scope __device__ array instead of
+// allocated scratch.
 //
 // The array holds one partial-sum record per virtual pair (a,b), so it bounds
 // the problem size: v * v <= kMaxVirtualPairs (v <= 512), 8 MiB in total, reserved on
@@ -14,11 +16,16 @@
 // it, and it keeps the last call's contents; every record a call reads is
 // written earlier in the same call, so nothing needs clearing, but calls that
 // overlap on the GPU (concurrent streams) race on it.  The first call on a
-// device looks up the array's device address (cudaGetSymbolAddress), so make
-// that first call before any stream capture begins.
+// device (in each CUDA context of that device, e.g. again after a
+// cudaDeviceReset) looks up the array's device address with
+// cudaGetSymbolAddress, with the stream's device current; make that first call
+// before any stream capture begins.
 #include <cmath>
 #include <mutex>
 #include <string>
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include "../../include/gbcc.h"
 #include "engine.h"
@@ -34,10 +41,25 @@ static __device__ __align__(256) double g_pair_partials[kMaxVirtualPairs * 4];
 
 struct ScratchAddr {
   double* partials = nullptr;
-  bool ready = false;
+  CUcontext ctx = nullptr;  // context the address belongs to
 };
 ScratchAddr g_addr[kMaxDevices];
 std::mutex g_addr_mu;
+
+// cuCtxGetCurrent through the runtime's driver entry point (no libcuda link)
+PFN_cuCtxGetCurrent_v4000 ctx_get_current_fn() {
+  static PFN_cuCtxGetCurrent_v4000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+  }();
+  return fn;
+}
 
 __device__ __forceinline__ double block_sum_na(double v, double* sh) {
   const int tid = threadIdx.x;
@@ -110,17 +132,22 @@ __global__ void __launch_bounds__(kNoAllocThreads)
   }
 }
 
-// Device address of the scratch array on the current device (looked up once).
-double* scratch_for_current_device(std::string& why) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    cudaGetLastError();
-    why = "no usable current CUDA device";
+// Device address of the scratch array on device `dev`, which the caller has
+// made current.  Looked up once per device and context: a new primary
+// context (after cudaDeviceReset) reloads the module, so the address is
+// looked up again when the current context is not the one it came from.
+double* scratch_for_device(int dev, std::string& why) {
+  if (dev < 0 || dev >= kMaxDevices) {
+    why = "device ordinal out of range";
     return nullptr;
+  }
+  CUcontext ctx = nullptr;
+  if (auto fn = ctx_get_current_fn()) {
+    if (fn(&ctx) != CUDA_SUCCESS) ctx = nullptr;
   }
   std::lock_guard<std::mutex> lock(g_addr_mu);
   ScratchAddr& s = g_addr[dev];
-  if (!s.ready) {
+  if (!s.partials || ctx == nullptr || s.ctx != ctx) {
     void* ptr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&ptr, g_pair_partials);
     if (e != cudaSuccess || ptr == nullptr) {
@@ -129,10 +156,36 @@ double* scratch_for_current_device(std::string& why) {
       return nullptr;
     }
     s.partials = static_cast<double*>(ptr);
-    s.ready = true;
+    s.ctx = ctx;
   }
   return s.partials;
 }
+
+// Device memory of device `dev` (or managed memory): anything else, such as a
+// host pointer, would reach the kernels as a bad address.
+bool device_pointer_on(const void* p, int dev) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
+// Makes `dev` current for its lifetime and restores the caller's device.
+struct DeviceScope {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceScope(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    ok = cudaSetDevice(dev) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
 
 }  // namespace
 }  // namespace gbcc
@@ -156,13 +209,32 @@ extern "C" gbcc_status gbcc_energy_noalloc(int64_t o, int64_t v, const double* f
     gbcc_set_thread_error("gbcc_energy_noalloc: NULL argument");
     return GBCC_ERR_INVALID_ARG;
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int dev = -1;
+  if (cudaStreamGetDevice(st, &dev) != cudaSuccess || dev < 0) {
+    cudaGetLastError();
+    gbcc_set_thread_error("gbcc_energy_noalloc: cannot determine the stream's device");
+    return GBCC_ERR_INVALID_ARG;
+  }
+  const void* ptrs[] = {f_ai, g_abij, t1_ai, tau_abij, r1_ai, r2_abij, out};
+  const char* names[] = {"f_ai", "g_abij", "t1", "tau", "r1", "r2", "out"};
+  for (int k = 0; k < 7; ++k)
+    if (!device_pointer_on(ptrs[k], dev)) {
+      gbcc_set_thread_error(std::string("gbcc_energy_noalloc: ") + names[k] +
+                            " is not device memory of the stream's device " + std::to_string(dev));
+      return GBCC_ERR_INVALID_ARG;
+    }
+  DeviceScope scope(dev);
+  if (!scope.ok) {
+    gbcc_set_thread_error("gbcc_energy_noalloc: cannot make the stream's device current");
+    return GBCC_ERR_CUDA;
+  }
   std::string why;
-  double* partials = scratch_for_current_device(why);
+  double* partials = scratch_for_device(dev, why);
   if (!partials) {
     gbcc_set_thread_error("gbcc_energy_noalloc: " + why);
     return GBCC_ERR_CUDA;
   }
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int64_t npairs = v * v;
   pair_partials_kernel<<<static_cast<unsigned>(npairs), kNoAllocThreads, 0, st>>>(
       o, v, f_ai, g_abij, t1_ai, tau_abij, r1_ai, r2_abij, partials);

@@ -51,7 +51,9 @@ def recorded(path, pattern, line_no):
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_molecules.py <MPQC source tree>")
+    ref = Path(sys.argv[1])
     out = ref / VALIDATION / "outputs"
     xyz = (ref / VALIDATION / "inputs" / "h2o.xyz").read_text()
     num = r"(-?\d+\.\d+(?:e-?\d+)?)"
