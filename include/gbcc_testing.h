@@ -61,6 +61,10 @@ int gbcc_testing_gemm_ex3(int64_t M, int64_t N, int64_t K, const double* A, cons
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);
 
+/* Symmetric eigensolver of the RHF driver (host code, no GPU needed):
+ * eigenvalues w[n] ascending, eigenvectors V[n][n] by column. */
+int gbcc_testing_eigh(int32_t n, const double* A, double* w, double* V);
+
 /* One residual on the device-resident amplitudes of handle h (t1/t2 as left
  * by the previous gbcc_residual / gbcc_solve call) with CUDA events around
  * every operation of the residual program.  For each of the first

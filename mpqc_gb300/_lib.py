@@ -27,11 +27,16 @@ EXPORTS = (
     "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error",
 )
+# every symbol include/gbcc_scf.h declares
+SCF_EXPORTS = (
+    "gbcc_scf_config_default", "gbcc_scf_create", "gbcc_scf_run", "gbcc_scf_ao", "gbcc_scf_orbitals",
+    "gbcc_scf_ccsd_inputs", "gbcc_scf_destroy", "gbcc_last_scf_error",
+)
 # test hooks of include/gbcc_testing.h
 TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_gemm_ex3", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims",
-                   "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total")
+                   "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total", "gbcc_testing_eigh")
 
 
 class Config(C.Structure):
@@ -60,6 +65,26 @@ class Report(C.Structure):
         ("seconds_total", C.c_double), ("seconds_residual_mixed", C.c_double),
         ("seconds_residual_fp64", C.c_double),
     ]
+
+
+class Molecule(C.Structure):
+    _fields_ = [("natom", C.c_int32), ("charge", C.c_void_p), ("xyz", C.c_void_p), ("mol_charge", C.c_int32)]
+
+
+class Basis(C.Structure):
+    _fields_ = [("nshell", C.c_int32), ("atom", C.c_void_p), ("l", C.c_void_p), ("nprim", C.c_void_p),
+                ("exps", C.c_void_p), ("coefs", C.c_void_p), ("pure", C.c_int32)]
+
+
+class ScfConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_iter", C.c_int32), ("threshold", C.c_double),
+                ("n_diis", C.c_int32), ("verbose", C.c_int32)]
+
+
+class ScfReport(C.Structure):
+    _fields_ = [("nbf", C.c_int32), ("nocc", C.c_int32), ("iters", C.c_int32), ("converged", C.c_int32),
+                ("energy", C.c_double), ("e_nuc", C.c_double), ("seconds_one_body", C.c_double),
+                ("seconds_eri", C.c_double), ("seconds_scf", C.c_double), ("seconds_transform", C.c_double)]
 
 
 _lib = None
@@ -143,6 +168,24 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_slice_policy.argtypes = [vp, vp, vp]
     lib.gbcc_last_error.restype = C.c_char_p
     lib.gbcc_last_error.argtypes = [vp]
+    lib.gbcc_scf_config_default.restype = None
+    lib.gbcc_scf_config_default.argtypes = [C.POINTER(ScfConfig)]
+    lib.gbcc_scf_create.restype = C.c_int
+    lib.gbcc_scf_create.argtypes = [C.POINTER(vp), C.POINTER(Molecule), C.POINTER(Basis), C.POINTER(ScfConfig)]
+    lib.gbcc_scf_run.restype = C.c_int
+    lib.gbcc_scf_run.argtypes = [vp, C.POINTER(ScfReport)]
+    lib.gbcc_scf_ao.restype = C.c_int
+    lib.gbcc_scf_ao.argtypes = [vp, vp, vp, vp]
+    lib.gbcc_scf_orbitals.restype = C.c_int
+    lib.gbcc_scf_orbitals.argtypes = [vp, vp, vp]
+    lib.gbcc_scf_ccsd_inputs.restype = C.c_int
+    lib.gbcc_scf_ccsd_inputs.argtypes = [vp, i32, vp]
+    lib.gbcc_scf_destroy.restype = C.c_int
+    lib.gbcc_scf_destroy.argtypes = [vp]
+    lib.gbcc_last_scf_error.restype = C.c_char_p
+    lib.gbcc_last_scf_error.argtypes = [vp]
+    lib.gbcc_testing_eigh.restype = C.c_int
+    lib.gbcc_testing_eigh.argtypes = [i32, vp, vp, vp]
     del i64
     if path is None:
         _lib = lib

@@ -379,6 +379,15 @@ void commit_inputs(gbcc_handle* h) {
 // Thread-local message read by gbcc_last_error(NULL) (handle-free entry points).
 void gbcc_set_thread_error(const std::string& msg) { g_create_error = msg; }
 
+// Dimensions and device of a handle, for the SCF input producer (scf.cpp).
+bool gbcc_internal_dims(const gbcc_handle* h, int64_t* o, int64_t* v, int* device) {
+  if (!h) return false;
+  *o = h->cfg.o;
+  *v = h->cfg.v;
+  *device = h->cfg.device;
+  return true;
+}
+
 extern "C" {
 
 int gbcc_abi_version(void) { return GBCC_ABI_VERSION; }

@@ -504,3 +504,63 @@ def molecular_inputs(xyz_text, basis, frozen_core=True, charge=0):
     nfz = mol.n_frozen_core() if frozen_core else 0
     blocks, eo, ev = mo_blocks(scf, G, nfz)
     return scf, blocks, eo, ev, nfz
+
+
+# ---------------------------------------------------------------------------
+# The same integrals from the C restatement (oracle/ints_ref.c), for systems
+# too large for the Python shell loops above
+# ---------------------------------------------------------------------------
+
+def _ints_lib():
+    import ctypes as C
+    from . import build_ref
+    lib = C.CDLL(str(build_ref.build()))
+    ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    lib.oneint_sph.restype = C.c_int
+    lib.oneint_sph.argtypes = [C.c_int, ip, dp, ip, dp, dp, C.c_int, C.c_int, dp, dp, dp, dp, dp]
+    lib.eri_sph.restype = C.c_int
+    lib.eri_sph.argtypes = [C.c_int, ip, dp, ip, dp, dp, C.c_int, dp]
+    return lib
+
+
+def _flat_shells(shells):
+    import ctypes as C
+    l = np.array([s.l for s in shells], dtype=np.int32)
+    center = np.ascontiguousarray(np.array([s.center for s in shells], dtype=float))
+    nprim = np.array([len(s.exps) for s in shells], dtype=np.int32)
+    exps = np.ascontiguousarray(np.concatenate([s.exps for s in shells]))
+    coefs = np.ascontiguousarray(np.concatenate([s.coefs for s in shells]))
+    pure = int(any(s.pure for s in shells))
+    ptr = lambda a, t: a.ctypes.data_as(C.POINTER(t))  # noqa: E731
+    return (len(shells), ptr(l, C.c_int), ptr(center, C.c_double), ptr(nprim, C.c_int),
+            ptr(exps, C.c_double), ptr(coefs, C.c_double), pure), (l, center, nprim, exps, coefs)
+
+
+def ao_integrals_c(mol: Molecule, basis: str, eri=True):
+    """``ao_integrals`` computed by the C restatement: S, H = T + V and (if
+    ``eri``) (mu nu|la si) in the spherical AO basis, each function scaled to
+    unit self-overlap.  The ERI array is filled and rescaled in place."""
+    import ctypes as C
+    lib = _ints_lib()
+    shells = build_shells(mol, basis)
+    args, keep = _flat_shells(shells)
+    nf = sum(s.nfunc for s in shells)
+    Zn = np.array([float(Z_OF[s]) for s in mol.symbols])
+    xyz = np.ascontiguousarray(mol.coords, dtype=float)
+    S = np.zeros((nf, nf))
+    Tk = np.zeros((nf, nf))
+    V = np.zeros((nf, nf))
+    dp = C.POINTER(C.c_double)
+    lib.oneint_sph(*args, len(mol.symbols), Zn.ctypes.data_as(dp), xyz.ctypes.data_as(dp),
+                   S.ctypes.data_as(dp), Tk.ctypes.data_as(dp), V.ctypes.data_as(dp))
+    d = 1.0 / np.sqrt(np.diag(S))
+    S = S * d[:, None] * d[None, :]
+    H = (Tk + V) * d[:, None] * d[None, :]
+    if not eri:
+        return S, H, None
+    G = np.empty((nf, nf, nf, nf))
+    lib.eri_sph(*args, G.ctypes.data_as(dp))
+    for p in range(nf):   # rescale in place, one slab at a time
+        G[p] *= d[p] * (d[:, None, None] * d[None, :, None] * d[None, None, :])
+    del keep
+    return S, H, G

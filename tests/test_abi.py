@@ -17,20 +17,23 @@ def lib():
     return _lib.load()
 
 
-def declared_symbols():
-    text = (ROOT / "include" / "gbcc.h").read_text()
+def declared_symbols(header="gbcc.h"):
+    text = (ROOT / "include" / header).read_text()
     body = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(gbcc_[a-z_]+)\s*\(", body)))
+    return sorted(set(re.findall(r"\b(gbcc_[a-z0-9_]+)\s*\(", body)))
 
 
 def test_header_and_binding_agree():
     from mpqc_gb300 import _lib
     assert declared_symbols() == sorted(_lib.EXPORTS)
+    assert declared_symbols("gbcc_scf.h") == sorted(_lib.SCF_EXPORTS)
+    assert declared_symbols("gbcc_testing.h") == sorted(_lib.TESTING_EXPORTS)
 
 
 def test_library_exports_every_declared_symbol(lib):
-    for name in declared_symbols():
-        assert hasattr(lib, name), name
+    for header in ("gbcc.h", "gbcc_scf.h", "gbcc_testing.h"):
+        for name in declared_symbols(header):
+            assert hasattr(lib, name), name
     assert lib.gbcc_abi_version() == 3
 
 
