@@ -458,6 +458,92 @@ def solve_report(args):
     return 0
 
 
+def molecule_report(args):
+    """The (H2O)10 / cc-pVDZ target on the GPU, from the geometry: AO integrals,
+    RHF and the AO -> MO transform on the device, then a mixed-precision solve
+    (split-BF16 bulk contractions, FP64 denominators, DIIS, energy, then FP64
+    refinement iterations) and a plain-FP64 solve on the same MO integrals.
+    Reports |dE_corr| of both against the FP64 oracle's energy
+    (tests/golden/h2o10_ccpvdz.json, computed on the CPU by
+    tests/golden/make_h2o10.py), max|dT2| mixed vs FP64, s/iter and TFLOP/s of
+    each path, and the ladder GEMM's fraction of the BF16 tensor peak."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    from mpqc_gb300 import build as gb
+    gb.build()
+    from mpqc_gb300 import RHF, Solver, molecules
+    nw = args.waters
+    sym, xyz = molecules.water_cluster(nw, seed=0)
+    fixture = ROOT / "tests" / "golden" / ("h2o10_ccpvdz.json" if nw == 10 else f"h2o{nw}_ccpvdz.json")
+    ref = json.loads(fixture.read_text()) if fixture.exists() else None
+    t0 = time.perf_counter()
+    scf = RHF(sym, xyz, "cc-pVDZ", threshold=1e-11, max_iter=60)
+    e_scf = scf.run()
+    srep = scf.report
+    nocc = scf.nocc()
+    o, v = nocc, scf.nbf - nocc
+    F = flop_count(o, v)
+    log(f"[h2o{nw}] N={scf.nbf} o={o} v={v}: E_RHF {e_scf:.10f} ({srep.iters} it., ERI {srep.seconds_eri:.2f} s, "
+        f"SCF {srep.seconds_scf:.2f} s, wall {time.perf_counter() - t0:.1f} s)")
+    runs, amps = {}, {}
+    for prec in ("mixed", "fp64"):
+        s = Solver(o, v, precision=prec, target_precision=args.solve_precision, max_iter=args.max_iter,
+                   refine_iters=2)
+        t1 = time.perf_counter()
+        scf.ccsd_inputs(s)
+        t_in = time.perf_counter() - t1
+        t2_ = time.perf_counter()
+        e, a1, a2, rep = s.solve()
+        wall = time.perf_counter() - t2_
+        # inputs_s: the MO transform on the device and the input commit (slice
+        # calibration and autotuning in mixed precision)
+        run = {"e_corr": e, "converged": rep.converged, "iters": rep.iters, "mixed_iters": rep.mixed_iters,
+               "fp64_iters": rep.fp64_iters, "solve_s": wall, "inputs_s": t_in,
+               "s_per_iter_mixed": rep.seconds_residual_mixed or None,
+               "s_per_iter_fp64": rep.seconds_residual_fp64 or None}
+        if prec == "mixed":
+            sl, se = s.slice_policy()
+            run["slices"], run["slice_rel_change_vs_3"] = list(sl), list(se)
+            prof = s.profile_residual(precision="mixed")
+            lad = [p for p in prof if p["cls"] == 0 and p["gemm_ms"] > 0]
+            if lad:
+                lp = max(lad, key=lambda p: p["flops"])
+                ach = lp["pairs"] * lp["flops"] / (lp["gemm_ms"] * 1e-3) / 1e12
+                pk = peaks().get("bf16_tflops") or 1953.9
+                run["ladder"] = {"M": lp["M"], "N": lp["N"], "K": lp["K"], "launch_ms": lp["gemm_ms"],
+                                 "executed_tflops": ach, "frac_of_bf16_burst_peak": ach / pk}
+            run["term_ms"] = {}
+            for p in prof:
+                key = {0: "ladder", 1: "ring", 2: "other", -1: "elementwise"}[p["cls"]]
+                run["term_ms"][key] = run["term_ms"].get(key, 0.0) + p["ms"]
+        s.close()
+        runs[prec] = run
+        amps[prec] = a2
+        log(f"[h2o{nw}] {prec}: E_corr {e:.12f}, {rep.iters} it. ({rep.mixed_iters} mixed), {wall:.1f} s")
+    scf.close()
+    m, f = runs["mixed"], runs["fp64"]
+    line = {"molecule": f"(H2O){nw}", "basis": "cc-pVDZ", "nbf": srep.nbf, "o": o, "v": v, "frozen_core": False,
+            "geometry": f"mpqc_gb300.molecules.water_cluster({nw}, seed=0)", "flops_per_iter": F,
+            "e_rhf": e_scf, "scf": {"iters": srep.iters, "eri_s": srep.seconds_eri, "scf_s": srep.seconds_scf,
+                                    "one_body_s": srep.seconds_one_body},
+            "target_precision": args.solve_precision, "runs": runs,
+            "abs_dE_mixed_vs_fp64_gpu": abs(m["e_corr"] - f["e_corr"]),
+            "max_abs_dT2_mixed_vs_fp64_gpu": float(np.max(np.abs(amps["mixed"] - amps["fp64"])))}
+    if m["s_per_iter_mixed"] and f["s_per_iter_fp64"]:
+        line["tflops_mixed"] = F / m["s_per_iter_mixed"] / 1e12
+        line["tflops_fp64"] = F / f["s_per_iter_fp64"] / 1e12
+        line["per_iteration_speedup"] = f["s_per_iter_fp64"] / m["s_per_iter_mixed"]
+    line["solve_speedup"] = f["solve_s"] / m["solve_s"]
+    if ref:
+        line["oracle"] = {"e_rhf": ref["e_rhf"], "e_ccsd_corr": ref["e_ccsd_corr"], "source": fixture.name}
+        line["abs_dE_rhf_vs_oracle"] = abs(e_scf - ref["e_rhf"])
+        line["abs_dE_corr_mixed_vs_oracle"] = abs(m["e_corr"] - ref["e_ccsd_corr"])
+        line["abs_dE_corr_fp64_vs_oracle"] = abs(f["e_corr"] - ref["e_ccsd_corr"])
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def gemm_probe(args):
     """One GEMM shape C = A B^T on the library's kernels (profiling aid): seeded
     normal FP64 inputs through gbcc_testing_gemm_ex3 (split-BF16 tensor-core
@@ -534,9 +620,17 @@ def main():
     ap.add_argument("--gemm-repeat", type=int, default=5)
     ap.add_argument("--gemm-check", action="store_true",
                     help="also report max |C - A B^T| / max |A B^T| against numpy FP64")
+    ap.add_argument("--config", default="residual", choices=["residual", "h2o10"],
+                    help="residual: the synthetic o=32 v=320 residual (default); h2o10: (H2O)10 / cc-pVDZ "
+                         "from the geometry, mixed and plain-FP64 solves against the oracle's energy")
+    ap.add_argument("--waters", type=int, default=10, help="--config h2o10: cluster size (default 10)")
     args = ap.parse_args()
     if args.gemm:
         return gemm_probe(args)
+    if args.config == "h2o10":
+        if args.max_iter == 40 and args.solve_precision == 1e-8:
+            args.solve_precision = 1e-9
+        return molecule_report(args)
     if args.impl == "reference":
         return reference_arm(args)
     if args.solve:

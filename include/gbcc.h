@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define GBCC_ABI_VERSION 3
+#define GBCC_ABI_VERSION 4
 
 typedef enum gbcc_status {
   GBCC_OK = 0,
@@ -84,6 +84,10 @@ typedef struct gbcc_config {
                                /* may add against 3 slices at the probe amplitudes; 1e-5     */
   int32_t autotune;            /* 1 (default): mixed handles time each tensor-core contraction's */
                                /* candidate tile widths and K splits once and keep the fastest */
+  int32_t refine_reset_diis;   /* 1 (default): the DIIS subspace restarts after the update at  */
+                               /* the switch to FP64, so the refinement extrapolates with FP64 */
+                               /* residuals only (DIISSolver::reset, cc/solvers.h:154-157,     */
+                               /* "used when switching to a new solver subspace"); 0: keep it   */
 } gbcc_config;
 
 typedef struct gbcc_inputs {
@@ -190,6 +194,25 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
 
 /* Release the handle and all its device memory.  NULL is accepted. */
 gbcc_status gbcc_destroy(gbcc_handle* h);
+
+/* Amplitudes the next gbcc_solve starts from instead of t = 0 (host or
+ * device pointers, t1[a][i], t2[a][b][i][j], t2 pair-symmetric): a restart.
+ * Counterpart of CCSD::set_t1 / set_t2 (ccsd.h:183-185), which store
+ * amplitudes in the wavefunction; here they seed one solve and are then
+ * consumed. */
+gbcc_status gbcc_set_amplitudes(gbcc_handle* h, const double* t1_ai, const double* t2_abij);
+
+/* Checkpoint of the amplitudes of the last gbcc_solve on this handle: a file
+ * of the 8 bytes "GBCCAMP1", int64 o, int64 v, double E_corr, then t1 and t2
+ * as FP64 in host byte order.  GBCC_ERR_STATE if no solve has completed since
+ * the inputs were set (or a residual / energy call has replaced the
+ * amplitudes).  No reference counterpart (MPQC keeps T1/T2 in memory only). */
+gbcc_status gbcc_save_amplitudes(gbcc_handle* h, const char* path);
+
+/* Read a checkpoint written by gbcc_save_amplitudes (same o and v) and seed
+ * the next gbcc_solve with it, as gbcc_set_amplitudes does; *e_corr (may be
+ * NULL) receives the energy stored with it. */
+gbcc_status gbcc_load_amplitudes(gbcc_handle* h, const char* path, double* e_corr);
 
 /* Slice counts in use per contraction class {ladder, ring, other} once inputs
  * are set, and for classes configured as 0 the measured max|dr|/max|r| of the

@@ -25,7 +25,8 @@ EXPORTS = (
     "gbcc_abi_version", "gbcc_status_string", "gbcc_config_default", "gbcc_create",
     "gbcc_set_inputs", "gbcc_device_inputs", "gbcc_commit_inputs", "gbcc_residual",
     "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
-    "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error",
+    "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error", "gbcc_set_amplitudes",
+    "gbcc_save_amplitudes", "gbcc_load_amplitudes",
 )
 # every symbol include/gbcc_scf.h declares
 SCF_EXPORTS = (
@@ -49,7 +50,7 @@ class Config(C.Structure):
         ("diis_start", C.c_int32), ("n_diis", C.c_int32), ("diis_damp", C.c_double),
         ("diis_ngroup", C.c_int32), ("diis_group_nstart", C.c_int32),
         ("verbose", C.c_int32), ("device", C.c_int32), ("use_graphs", C.c_int32),
-        ("slice_tolerance", C.c_double), ("autotune", C.c_int32),
+        ("slice_tolerance", C.c_double), ("autotune", C.c_int32), ("refine_reset_diis", C.c_int32),
     ]
 
 
@@ -168,6 +169,12 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_slice_policy.argtypes = [vp, vp, vp]
     lib.gbcc_last_error.restype = C.c_char_p
     lib.gbcc_last_error.argtypes = [vp]
+    lib.gbcc_set_amplitudes.restype = C.c_int
+    lib.gbcc_set_amplitudes.argtypes = [vp, vp, vp]
+    lib.gbcc_save_amplitudes.restype = C.c_int
+    lib.gbcc_save_amplitudes.argtypes = [vp, C.c_char_p]
+    lib.gbcc_load_amplitudes.restype = C.c_int
+    lib.gbcc_load_amplitudes.argtypes = [vp, C.c_char_p, dp]
     lib.gbcc_scf_config_default.restype = None
     lib.gbcc_scf_config_default.argtypes = [C.POINTER(ScfConfig)]
     lib.gbcc_scf_create.restype = C.c_int

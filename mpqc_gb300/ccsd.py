@@ -76,7 +76,8 @@ class Solver:
     def __init__(self, o, v, precision="fp64", slices=(0, 0, 0), refine_iters=2,
                  mixed_switch_precision=0.0, max_iter=30, target_precision=1e-9,
                  diis_start=1, n_diis=8, diis_damp=0.0, diis_ngroup=1, diis_group_nstart=1,
-                 verbose=False, device=0, use_graphs=True, slice_tolerance=1e-5, autotune=True):
+                 verbose=False, device=0, use_graphs=True, slice_tolerance=1e-5, autotune=True,
+                 refine_reset_diis=True):
         self.lib = L.load()
         cfg = L.Config()
         self.lib.gbcc_config_default(C.byref(cfg))
@@ -95,6 +96,7 @@ class Solver:
         cfg.use_graphs = int(bool(use_graphs))
         cfg.slice_tolerance = float(slice_tolerance)
         cfg.autotune = int(bool(autotune))
+        cfg.refine_reset_diis = int(bool(refine_reset_diis))
         self.cfg = cfg
         self.o, self.v = int(o), int(v)
         h = C.c_void_p()
@@ -210,6 +212,22 @@ class Solver:
         _check(self.lib, self.h, self.lib.gbcc_energy(self.h, _ptr(t1), _ptr(t2), _ptr(r1), _ptr(r2),
                                                       C.byref(e), C.byref(err)))
         return e.value, err.value
+
+    def set_amplitudes(self, t1, t2):
+        """Seed the next ``solve()`` with these amplitudes (a restart; host or device arrays)."""
+        self._keep = (t1, t2)
+        _check(self.lib, self.h, self.lib.gbcc_set_amplitudes(self.h, _ptr(t1), _ptr(t2)))
+        self._keep = None
+
+    def save_amplitudes(self, path):
+        """Write the last solve's t1/t2 and energy to a checkpoint file."""
+        _check(self.lib, self.h, self.lib.gbcc_save_amplitudes(self.h, str(path).encode()))
+
+    def load_amplitudes(self, path):
+        """Seed the next ``solve()`` from a checkpoint; returns its stored energy."""
+        e = C.c_double()
+        _check(self.lib, self.h, self.lib.gbcc_load_amplitudes(self.h, str(path).encode(), C.byref(e)))
+        return e.value
 
     def solve(self, want_amplitudes=True):
         o, v = self.o, self.v

@@ -57,6 +57,12 @@ struct gbcc_handle {
   // calibration chose, the measured relative residual change; -1 when not measured
   int slices_used[3] = {3, 3, 3};
   double slice_err[3] = {-1.0, -1.0, -1.0};
+  // amplitudes seeding the next solve (gbcc_set_amplitudes / load), and
+  // whether t1/t2 hold the result of the last solve (gbcc_save_amplitudes)
+  double *seed1 = nullptr, *seed2 = nullptr;
+  bool seeded = false;
+  bool have_solution = false;
+  double last_e = 0.0;
 };
 
 namespace {
@@ -124,6 +130,7 @@ bool check_config(const gbcc_config* c, std::string& why) {
   if (!(c->target_precision > 0.0)) { why = "target_precision must be > 0"; return false; }
   if (c->refine_iters < 0) { why = "refine_iters must be >= 0"; return false; }
   if (!(c->mixed_switch_precision >= 0.0)) { why = "mixed_switch_precision must be >= 0"; return false; }
+  if (c->refine_reset_diis != 0 && c->refine_reset_diis != 1) { why = "refine_reset_diis must be 0 or 1"; return false; }
   return true;
 }
 
@@ -427,6 +434,7 @@ void gbcc_config_default(gbcc_config* c) {
   c->use_graphs = 1;
   c->slice_tolerance = 1e-5;
   c->autotune = 1;
+  c->refine_reset_diis = 1;
 }
 
 gbcc_status gbcc_create(gbcc_handle** out, const gbcc_config* cfg) {
@@ -489,6 +497,8 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
     if (!h->S.t1) h->S.create(*h->eng, o, v);
     gbcc::CcsdTensors& S = h->S;
     h->inputs_set = false;
+    h->have_solution = false;
+    h->seeded = false;
     copy_in(S.eps_o->d, in->eps_o, o, h->stream);
     copy_in(S.eps_v->d, in->eps_v, v, h->stream);
     copy_in(S.Fia->d, in->Fia, o * v, h->stream);
@@ -523,6 +533,8 @@ gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out) {
     out->Giabc = S.Giabc->d;
     out->Gabcd = S.Gabcd->d;
     h->inputs_set = false;
+    h->have_solution = false;
+    h->seeded = false;
     return GBCC_OK;
   });
 }
@@ -545,6 +557,7 @@ gbcc_status gbcc_residual_ex(gbcc_handle* h, int32_t precision, const double* t1
       throw Error(GBCC_ERR_INVALID_ARG, "gbcc_residual: bad precision");
     if (!t1_ai || !t2_abij || !r1_ai || !r2_abij)
       throw Error(GBCC_ERR_INVALID_ARG, "gbcc_residual: NULL argument");
+    h->have_solution = false;
     copy_in(h->S.t1->d, t1_ai, n1_of(h), h->stream);
     copy_in(h->S.t2->d, t2_abij, n2_of(h), h->stream);
     check_pair_symmetric(h);
@@ -568,6 +581,7 @@ gbcc_status gbcc_energy(gbcc_handle* h, const double* t1_ai, const double* t2_ab
     if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "gbcc_energy: inputs not set");
     if (!t1_ai || !t2_abij || !r1_ai || !r2_abij)
       throw Error(GBCC_ERR_INVALID_ARG, "gbcc_energy: NULL argument");
+    h->have_solution = false;
     copy_in(h->S.t1->d, t1_ai, n1_of(h), h->stream);
     copy_in(h->S.t2->d, t2_abij, n2_of(h), h->stream);
     copy_in(h->S.r1->d, r1_ai, n1_of(h), h->stream);
@@ -589,17 +603,40 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
     const int64_t n1 = n1_of(h), n2 = n2_of(h);
     ensure_diis(h);
     gbcc_report rep{};
-    // t = 0, tau = 0, r1 = f_ai, r2 = g_abij   (ccsd.h:331-350)
-    GBCC_CK(cudaMemsetAsync(S.t1->d, 0, n1 * sizeof(double), h->stream));
-    GBCC_CK(cudaMemsetAsync(S.t2->d, 0, n2 * sizeof(double), h->stream));
-    GBCC_CK(cudaMemsetAsync(S.tau->d, 0, n2 * sizeof(double), h->stream));
-    GBCC_CK(cudaMemcpyAsync(S.r1->d, S.f_ai->d, n1 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-    GBCC_CK(cudaMemcpyAsync(S.r2->d, S.g_abij->d, n2 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-    GBCC_CK(cudaMemsetAsync(h->Bmat, 0, c.n_diis * c.n_diis * sizeof(double), h->stream));
+    h->have_solution = false;
     bool mixed_phase = c.precision == GBCC_PREC_MIXED;
     const bool used_mixed = mixed_phase;
     int fp64_resid = 0, mixed_resid = 0;
     double t_mixed = 0.0, t_fp64 = 0.0;
+    GBCC_CK(cudaMemsetAsync(h->Bmat, 0, c.n_diis * c.n_diis * sizeof(double), h->stream));
+    if (h->seeded) {
+      // restart: the residual of the seeded amplitudes in the starting precision
+      GBCC_CK(cudaMemcpyAsync(S.t1->d, h->seed1, n1 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+      GBCC_CK(cudaMemcpyAsync(S.t2->d, h->seed2, n2 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+      h->seeded = false;
+      const int prec = mixed_phase ? GBCC_PREC_MIXED : GBCC_PREC_FP64;
+      GBCC_CK(cudaEventRecord(h->ev0, h->stream));
+      run_residual(h, prec);
+      GBCC_CK(cudaEventRecord(h->ev1, h->stream));
+      sync_check(h);
+      float ms = 0.f;
+      GBCC_CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+      if (prec == GBCC_PREC_MIXED) {
+        ++mixed_resid;
+        t_mixed += ms * 1e-3;
+      } else {
+        ++fp64_resid;
+        t_fp64 += ms * 1e-3;
+      }
+    } else {
+      // t = 0, tau = 0, r1 = f_ai, r2 = g_abij   (ccsd.h:331-350)
+      GBCC_CK(cudaMemsetAsync(S.t1->d, 0, n1 * sizeof(double), h->stream));
+      GBCC_CK(cudaMemsetAsync(S.t2->d, 0, n2 * sizeof(double), h->stream));
+      GBCC_CK(cudaMemsetAsync(S.tau->d, 0, n2 * sizeof(double), h->stream));
+      GBCC_CK(cudaMemcpyAsync(S.r1->d, S.f_ai->d, n1 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+      GBCC_CK(cudaMemcpyAsync(S.r2->d, S.g_abij->d, n2 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    }
+    bool reset_after_update = false;
     double E1 = 0.0, E0 = 0.0, dE = 0.0, error = 1.0;
     double best_error = std::numeric_limits<double>::infinity();
     double best_dE = std::numeric_limits<double>::infinity();
@@ -639,7 +676,10 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
             progress = true;
           }
           stalled = progress ? 0 : stalled + 1;
-          if ((error <= sw && dE <= 0.1 * sw) || stalled >= 4) mixed_phase = false;
+          if ((error <= sw && dE <= 0.1 * sw) || stalled >= 4) {
+            mixed_phase = false;
+            reset_after_update = c.refine_reset_diis != 0;
+          }
         }
         conv = false;
       } else if (used_mixed && fp64_resid < c.refine_iters) {
@@ -684,6 +724,15 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
       gbcc::launch_diis_step(d, h->stream);
       gbcc::launch_diis_extrapolate(c.o, c.v, h->x1, h->x2, h->coef, c.n_diis, slots.data(), nvec,
                                     S.t1->d, S.t2->d, S.tau->d, h->stream);
+      if (reset_after_update) {
+        // a new subspace for the FP64 refinement: only FP64 residuals from here on
+        reset_after_update = false;
+        diis_iter = 0;
+        nvec = 0;
+        head = -1;
+        slots.clear();
+        GBCC_CK(cudaMemsetAsync(h->Bmat, 0, c.n_diis * c.n_diis * sizeof(double), h->stream));
+      }
       // residual of the new amplitudes
       const int prec = mixed_phase ? GBCC_PREC_MIXED : GBCC_PREC_FP64;
       GBCC_CK(cudaEventRecord(h->ev0, h->stream));
@@ -706,6 +755,8 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
     if (t2_abij) copy_out(t2_abij, S.t2->d, n2, h->stream);
     sync_check(h);
     if (e_corr) *e_corr = E1;
+    h->have_solution = true;
+    h->last_e = E1;
     rep.iters = iter;
     rep.converged = converged ? 1 : 0;
     rep.mixed_iters = mixed_resid;
@@ -730,7 +781,8 @@ gbcc_status gbcc_destroy(gbcc_handle* h) {
   h->eng.reset();
   h->aux.reset();
   for (void* p : {(void*)h->x1, (void*)h->x2, (void*)h->e1, (void*)h->e2, (void*)h->Bmat, (void*)h->coef,
-                  (void*)h->d_nskip, (void*)h->d_err, (void*)h->d_partial, (void*)h->d_out})
+                  (void*)h->d_nskip, (void*)h->d_err, (void*)h->d_partial, (void*)h->d_out,
+                  (void*)h->seed1, (void*)h->seed2})
     gbcc::dev_free(p);
   if (h->h_out) cudaFreeHost(h->h_out);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -742,12 +794,93 @@ gbcc_status gbcc_destroy(gbcc_handle* h) {
   return GBCC_OK;
 }
 
+gbcc_status gbcc_set_amplitudes(gbcc_handle* h, const double* t1_ai, const double* t2_abij) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "gbcc_set_amplitudes: inputs not set");
+    if (!t1_ai || !t2_abij) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_amplitudes: NULL amplitudes");
+    const int64_t n1 = n1_of(h), n2 = n2_of(h);
+    if (!h->seed1) h->seed1 = static_cast<double*>(gbcc::dev_alloc(n1 * sizeof(double)));
+    if (!h->seed2) h->seed2 = static_cast<double*>(gbcc::dev_alloc(n2 * sizeof(double)));
+    copy_in(h->seed1, t1_ai, n1, h->stream);
+    copy_in(h->seed2, t2_abij, n2, h->stream);
+    // the pair-symmetry check reads S.t2: stage the seed there
+    GBCC_CK(cudaMemcpyAsync(h->S.t2->d, h->seed2, n2 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    h->have_solution = false;
+    check_pair_symmetric(h);
+    h->seeded = true;
+    return GBCC_OK;
+  });
+}
+
+namespace {
+constexpr char kAmpMagic[8] = {'G', 'B', 'C', 'C', 'A', 'M', 'P', '1'};
+struct FileCloser {
+  FILE* f;
+  ~FileCloser() {
+    if (f) std::fclose(f);
+  }
+};
+}  // namespace
+
+gbcc_status gbcc_save_amplitudes(gbcc_handle* h, const char* path) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!path) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_save_amplitudes: NULL path");
+    if (!h->have_solution) throw Error(GBCC_ERR_STATE, "gbcc_save_amplitudes: no solve has completed");
+    const int64_t n1 = n1_of(h), n2 = n2_of(h);
+    std::vector<double> t1(n1), t2(n2);
+    GBCC_CK(cudaMemcpyAsync(t1.data(), h->S.t1->d, n1 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    GBCC_CK(cudaMemcpyAsync(t2.data(), h->S.t2->d, n2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    GBCC_CK(cudaStreamSynchronize(h->stream));
+    FileCloser fc{std::fopen(path, "wb")};
+    if (!fc.f) throw Error(GBCC_ERR_INVALID_ARG, std::string("gbcc_save_amplitudes: cannot open ") + path);
+    const int64_t dims[2] = {h->cfg.o, h->cfg.v};
+    const bool ok = std::fwrite(kAmpMagic, 1, 8, fc.f) == 8 && std::fwrite(dims, sizeof(int64_t), 2, fc.f) == 2 &&
+                    std::fwrite(&h->last_e, sizeof(double), 1, fc.f) == 1 &&
+                    std::fwrite(t1.data(), sizeof(double), n1, fc.f) == static_cast<size_t>(n1) &&
+                    std::fwrite(t2.data(), sizeof(double), n2, fc.f) == static_cast<size_t>(n2);
+    if (!ok || std::fflush(fc.f) != 0) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_save_amplitudes: write failed");
+    return GBCC_OK;
+  });
+}
+
+gbcc_status gbcc_load_amplitudes(gbcc_handle* h, const char* path, double* e_corr) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!path) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_load_amplitudes: NULL path");
+    FileCloser fc{std::fopen(path, "rb")};
+    if (!fc.f) throw Error(GBCC_ERR_INVALID_ARG, std::string("gbcc_load_amplitudes: cannot open ") + path);
+    char magic[8];
+    int64_t dims[2];
+    double e = 0.0;
+    if (std::fread(magic, 1, 8, fc.f) != 8 || std::memcmp(magic, kAmpMagic, 8) != 0 ||
+        std::fread(dims, sizeof(int64_t), 2, fc.f) != 2 || std::fread(&e, sizeof(double), 1, fc.f) != 1)
+      throw Error(GBCC_ERR_INVALID_ARG, "gbcc_load_amplitudes: not an amplitude checkpoint");
+    if (dims[0] != h->cfg.o || dims[1] != h->cfg.v)
+      throw Error(GBCC_ERR_INVALID_ARG, "gbcc_load_amplitudes: checkpoint has o = " + std::to_string(dims[0]) +
+                                            ", v = " + std::to_string(dims[1]));
+    const int64_t n1 = n1_of(h), n2 = n2_of(h);
+    std::vector<double> t1(n1), t2(n2);
+    if (std::fread(t1.data(), sizeof(double), n1, fc.f) != static_cast<size_t>(n1) ||
+        std::fread(t2.data(), sizeof(double), n2, fc.f) != static_cast<size_t>(n2))
+      throw Error(GBCC_ERR_INVALID_ARG, "gbcc_load_amplitudes: truncated checkpoint");
+    for (double x : t1)
+      if (!std::isfinite(x)) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_load_amplitudes: non-finite amplitude");
+    std::fclose(fc.f);
+    fc.f = nullptr;
+    const gbcc_status st = gbcc_set_amplitudes(h, t1.data(), t2.data());
+    if (st != GBCC_OK) throw Error(st, h->last_error);
+    if (e_corr) *e_corr = e;
+    return GBCC_OK;
+  });
+}
+
 gbcc_status gbcc_calibrate_slices(gbcc_handle* h, const double* t1_ai, const double* t2_abij) {
   return guarded(h, [&]() -> gbcc_status {
     if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "gbcc_calibrate_slices: inputs not set");
     if (h->cfg.precision != GBCC_PREC_MIXED) throw Error(GBCC_ERR_STATE, "gbcc_calibrate_slices: not a mixed-precision handle");
     if (!t1_ai || !t2_abij) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_calibrate_slices: NULL amplitudes");
     h->inputs_set = false;
+    h->have_solution = false;
+    h->seeded = false;
     calibrate_slices(h, t1_ai, t2_abij);
     h->inputs_set = true;
     return GBCC_OK;

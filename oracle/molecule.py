@@ -564,3 +564,98 @@ def ao_integrals_c(mol: Molecule, basis: str, eri=True):
         G[p] *= d[p] * (d[:, None, None] * d[None, :, None] * d[None, None, :])
     del keep
     return S, H, G
+
+
+# ---------------------------------------------------------------------------
+# Memory-lean variants for a few hundred basis functions (the same arithmetic)
+# ---------------------------------------------------------------------------
+
+def rhf_lean(S, H, G, nocc, e_nuc, conv=1e-13, max_iter=200, n_diis=8):
+    """``rhf`` with the exchange matrix built one AO slab at a time, so that no
+    N^4 temporary is made (G alone is 26.5 GB at N = 240)."""
+    n = S.shape[0]
+
+    def jk(D):
+        J = (G.reshape(n * n, n * n) @ D.ravel()).reshape(n, n)
+        K = np.empty((n, n))
+        for p in range(n):
+            K[p] = np.einsum("rqs,rs->q", G[p], D, optimize=True)
+        return J, K
+
+    w, U = np.linalg.eigh(S)
+    X = U @ np.diag(w ** -0.5) @ U.T
+    e, Cp = np.linalg.eigh(X.T @ H @ X)
+    C = X @ Cp
+    D = C[:, :nocc] @ C[:, :nocc].T
+    Eold = 0.0
+    fs, es = [], []
+    for it in range(1, max_iter + 1):
+        J, K = jk(D)
+        F = H + 2 * J - K
+        E = float(np.sum(D * (H + F))) + e_nuc
+        err = F @ D @ S - S @ D @ F
+        fs.append(F)
+        es.append(err)
+        if len(fs) > n_diis:
+            fs.pop(0)
+            es.pop(0)
+        if abs(E - Eold) < conv and np.max(np.abs(err)) < 1e-10:
+            break
+        Eold = E
+        m = len(fs)
+        B = -np.ones((m + 1, m + 1))
+        B[m, m] = 0.0
+        for i in range(m):
+            for j in range(m):
+                B[i, j] = float(np.vdot(es[i], es[j]))
+        rhs = np.zeros(m + 1)
+        rhs[m] = -1.0
+        c = np.linalg.solve(B, rhs)[:m]
+        Fd = sum(ci * fi for ci, fi in zip(c, fs))
+        e, Cp = np.linalg.eigh(X.T @ Fd @ X)
+        C = X @ Cp
+        D = C[:, :nocc] @ C[:, :nocc].T
+    e, Cp = np.linalg.eigh(X.T @ F @ X)
+    C = X @ Cp
+    return RHFResult(E, e_nuc, C, e, F, nocc, it)
+
+
+def mo_blocks_inplace(scf: RHFResult, G, n_frozen, chunk=8):
+    """``mo_blocks`` for large N: the last three indices of G are transformed
+    to the MO basis in place, one AO slab at a time (G is overwritten with
+    (mu q|r s)); each block then takes the first index in chunks of its second
+    index.  Needs all orbitals (number of MOs = N)."""
+    C = scf.C
+    n = C.shape[0]
+    if C.shape[1] != n:
+        raise ValueError("mo_blocks_inplace needs as many orbitals as basis functions")
+    for mu in range(n):
+        Y = G[mu] @ C                                  # (nu, la, s)
+        Y = np.tensordot(C, Y, axes=([0], [1]))        # (r, nu, s)
+        Y = np.tensordot(C, Y, axes=([0], [1]))        # (q, r, s)
+        G[mu] = Y
+    nocc = scf.nocc
+    Ca = C[:, n_frozen:]
+    o = nocc - n_frozen
+    O, V = slice(n_frozen, nocc), slice(nocc, n)
+
+    def block(P, Q, R, Sl):
+        """<p r|q s> = (pq|rs) laid out [p][r][q][s] (MPQC annotation order)."""
+        Cp = C[:, P]
+        nq = Q.stop - Q.start
+        out = np.empty((Cp.shape[1], R.stop - R.start, nq, Sl.stop - Sl.start))
+        for q0 in range(0, nq, chunk):
+            q1 = min(nq, q0 + chunk)
+            Y = np.tensordot(Cp, G[:, Q.start + q0:Q.start + q1, R, Sl], axes=([0], [0]))  # (p, q, r, s)
+            out[:, :, q0:q1, :] = Y.transpose(0, 2, 1, 3)
+        return out
+
+    Fmo = Ca.T @ scf.F @ Ca
+    Oa, Va = slice(0, o), slice(o, Ca.shape[1])
+    blocks = dict(
+        Fia=Fmo[Oa, Va].copy(), Fij=Fmo[Oa, Oa].copy(), Fab=Fmo[Va, Va].copy(),
+        Gijab=block(O, V, O, V), Gijkl=block(O, O, O, O), Giajb=block(O, O, V, V),
+        Gijka=block(O, O, O, V), Giabc=block(O, V, V, V), Gabcd=block(V, V, V, V),
+    )
+    eps = np.diag(Fmo)
+    return blocks, eps[:o].copy(), eps[o:].copy()

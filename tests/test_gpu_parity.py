@@ -5,6 +5,7 @@ import pytest
 
 from conftest import ints_dict, load_golden, oracle_ints, rel_err
 from mpqc_gb300 import Solver, synth
+from mpqc_gb300 import _lib as L
 from mpqc_gb300._lib import GbccError
 from oracle import ccsd_ref as R
 
@@ -229,3 +230,49 @@ def test_residual_rejects_amplitudes_without_pair_symmetry():
         assert e.value.status == 1 and "pair-symmetric" in str(e.value)
         r1, r2 = s.residual(inp.t1, inp.t2)   # the handle stays usable
     assert np.all(np.isfinite(r2))
+
+
+def test_restart_from_checkpoint_converges_at_once(tmp_path):
+    """gbcc_save_amplitudes / gbcc_load_amplitudes: a solve seeded with converged
+    amplitudes stops after its first convergence test with the same energy."""
+    inp = synth.make_inputs(5, 19, 30, seed=22)
+    kw = dict(target_precision=1e-10, max_iter=40)
+    with _solver(inp, **kw) as s:
+        e0, t1, t2, rep0 = s.solve()
+        path = tmp_path / "amps.bin"
+        s.save_amplitudes(path)
+    with _solver(inp, **kw) as s:
+        assert abs(s.load_amplitudes(path) - e0) == 0.0
+        e1, u1, u2, rep1 = s.solve()
+    assert rep1.converged and rep1.iters <= 2 < rep0.iters
+    assert abs(e1 - e0) < 1e-10 and np.max(np.abs(u2 - t2)) < 1e-9
+    with _solver(inp, **kw) as s:
+        with pytest.raises(L.GbccError) as ex:
+            s.save_amplitudes(tmp_path / "none.bin")   # no solve yet
+        assert ex.value.status == L.GBCC_ERR_STATE
+        bad = t2.copy()
+        bad[0, 1, 0, 0] += 1e-3                         # not pair-symmetric
+        with pytest.raises(L.GbccError) as ex:
+            s.set_amplitudes(t1, bad)
+        assert ex.value.status == L.GBCC_ERR_INVALID_ARG
+    with pytest.raises(L.GbccError) as ex:
+        with Solver(4, 19) as s2:
+            s2.set_inputs(inp.eps_o[:4], inp.eps_v, **{k: np.ascontiguousarray(v) for k, v in dict(
+                Fia=inp.Fia[:4], Fij=inp.Fij[:4, :4], Fab=inp.Fab, Gijab=inp.Gijab[:4, :4], Gijkl=inp.Gijkl[:4, :4, :4, :4],
+                Giajb=inp.Giajb[:4, :, :4], Gijka=inp.Gijka[:4, :4, :4], Giabc=inp.Giabc[:4], Gabcd=inp.Gabcd).items()})
+            s2.load_amplitudes(path)                    # checkpoint of o = 5
+    assert ex.value.status == L.GBCC_ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("reset", [True, False])
+def test_mixed_solve_refinement_with_and_without_diis_restart(reset):
+    """The switch to FP64 refinement restarts the DIIS subspace (default) or keeps
+    the split-precision vectors; both reach the oracle's energy within 1e-6 Eh."""
+    inp = synth.make_inputs(6, 30, 40, seed=23)
+    ref = R.solve_ccsd(oracle_ints(inp), inp.eps_o, inp.eps_v, target_precision=1e-9, max_iter=60)
+    with _solver(inp, precision="mixed", slices=(2, 2, 2), target_precision=1e-9, max_iter=60,
+                 refine_iters=2, refine_reset_diis=reset) as s:
+        e, t1, t2, rep = s.solve()
+    assert rep.converged and rep.fp64_iters >= 2
+    assert abs(e - ref.e_corr) < 1e-6
+    print(f"refine_reset_diis={reset}: {rep.mixed_iters} mixed + {rep.fp64_iters} FP64 iterations")
