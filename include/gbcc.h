@@ -78,8 +78,13 @@ typedef struct gbcc_config {
   int32_t diis_group_nstart;   /* "diis_group_nstart", default 1                               */
   int32_t verbose;             /* print the iteration table (ccsd.h:28-46)                     */
   int32_t device;              /* CUDA device ordinal                                          */
-  int32_t use_graphs;          /* 1 (default): each residual evaluation replays a CUDA graph    */
-                               /* captured on first use per precision; 0: direct launches     */
+  int32_t use_graphs;          /* 2 (default): gbcc_solve runs the whole loop as one CUDA     */
+                               /* graph -- a WHILE node whose body is one iteration, the      */
+                               /* convergence test and DIIS bookkeeping decided on the device,*/
+                               /* no host synchronisation per iteration; residual calls       */
+                               /* replay a graph captured on first use per precision.  1: the */
+                               /* same residual graphs with the loop driven from the host     */
+                               /* (same decisions and results); 0: direct launches            */
   double slice_tolerance;      /* automatic slices: largest max|dr|/max|r| (r1 and r2) a class */
                                /* may add against 3 slices at the probe amplitudes; 1e-5     */
   int32_t autotune;            /* 1 (default): mixed handles time each tensor-core contraction's */

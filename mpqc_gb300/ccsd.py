@@ -76,7 +76,7 @@ class Solver:
     def __init__(self, o, v, precision="fp64", slices=(0, 0, 0), refine_iters=2,
                  mixed_switch_precision=0.0, max_iter=30, target_precision=1e-9,
                  diis_start=1, n_diis=8, diis_damp=0.0, diis_ngroup=1, diis_group_nstart=1,
-                 verbose=False, device=0, use_graphs=True, slice_tolerance=1e-5, autotune=True,
+                 verbose=False, device=0, use_graphs=2, slice_tolerance=1e-5, autotune=True,
                  refine_reset_diis=True):
         self.lib = L.load()
         cfg = L.Config()
@@ -93,7 +93,7 @@ class Solver:
         cfg.diis_ngroup, cfg.diis_group_nstart = int(diis_ngroup), int(diis_group_nstart)
         cfg.verbose = int(bool(verbose))
         cfg.device = int(device)
-        cfg.use_graphs = int(bool(use_graphs))
+        cfg.use_graphs = int(use_graphs)  # False 0, True 1, or 2 (whole solve as one graph)
         cfg.slice_tolerance = float(slice_tolerance)
         cfg.autotune = int(bool(autotune))
         cfg.refine_reset_diis = int(bool(refine_reset_diis))

@@ -63,6 +63,13 @@ struct gbcc_handle {
   bool seeded = false;
   bool have_solution = false;
   double last_e = 0.0;
+  // whole-solve graph (use_graphs = 2): the residual programs as graphs (FP64,
+  // mixed), the instantiated loop, its device state, history and timestamps
+  cudaGraph_t rgraph[2] = {nullptr, nullptr};
+  cudaGraphExec_t solve_exec = nullptr;
+  gbcc::SolveState* d_state = nullptr;
+  double* d_history = nullptr;
+  unsigned long long* d_stamps = nullptr;
 };
 
 namespace {
@@ -131,6 +138,7 @@ bool check_config(const gbcc_config* c, std::string& why) {
   if (c->refine_iters < 0) { why = "refine_iters must be >= 0"; return false; }
   if (!(c->mixed_switch_precision >= 0.0)) { why = "mixed_switch_precision must be >= 0"; return false; }
   if (c->refine_reset_diis != 0 && c->refine_reset_diis != 1) { why = "refine_reset_diis must be 0 or 1"; return false; }
+  if (c->use_graphs < 0 || c->use_graphs > 2) { why = "use_graphs must be 0, 1 or 2"; return false; }
   return true;
 }
 
@@ -139,6 +147,12 @@ void drop_graphs(gbcc_handle* h) {
     if (g) cudaGraphExecDestroy(g);
     g = nullptr;
   }
+  for (auto& g : h->rgraph) {
+    if (g) cudaGraphDestroy(g);
+    g = nullptr;
+  }
+  if (h->solve_exec) cudaGraphExecDestroy(h->solve_exec);
+  h->solve_exec = nullptr;
   h->graph_launches[0] = h->graph_launches[1] = 0;
 }
 
@@ -215,6 +229,181 @@ void ensure_diis(gbcc_handle* h) {
   h->coef = static_cast<double*>(gbcc::dev_alloc(nd * sizeof(double)));
   h->d_nskip = static_cast<int*>(gbcc::dev_alloc(sizeof(int)));
   h->ndiis_alloc = nd;
+}
+
+// The residual program of one precision as a (not instantiated) graph.
+cudaGraph_t capture_residual_graph(gbcc_handle* h, int precision) {
+  if (precision == GBCC_PREC_MIXED && !h->prepacked) {
+    h->eng->finalize(true);
+    h->prepacked = true;
+  }
+  cudaGraph_t g = nullptr;
+  GBCC_CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    h->eng->begin(gbcc::Mode::kExec, precision);
+    gbcc::residual_program(*h->eng, h->S);
+    h->eng->end();
+  } catch (...) {
+    cudaStreamEndCapture(h->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    throw;
+  }
+  GBCC_CK(cudaStreamEndCapture(h->stream, &g));
+  return g;
+}
+
+// Capture what fn enqueues on the handle's stream into the (empty) graph g.
+template <class F>
+void capture_into(gbcc_handle* h, cudaGraph_t g, F&& fn) {
+  GBCC_CK(cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  cudaGraph_t out = nullptr;
+  try {
+    fn();
+  } catch (...) {
+    cudaStreamEndCapture(h->stream, &out);
+    cudaGetLastError();
+    throw;
+  }
+  GBCC_CK(cudaStreamEndCapture(h->stream, &out));
+}
+
+// the node of g that no other node depends on (g has exactly one)
+cudaGraphNode_t sink_node(cudaGraph_t g) {
+  size_t n = 0;
+  GBCC_CK(cudaGraphGetNodes(g, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  GBCC_CK(cudaGraphGetNodes(g, nodes.data(), &n));
+  cudaGraphNode_t sink = nullptr;
+  for (cudaGraphNode_t nd : nodes) {
+    size_t k = 0;
+    GBCC_CK(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &k));
+    if (k == 0) {
+      if (sink) throw Error(GBCC_ERR_CUDA, "solve graph: captured segment has more than one sink");
+      sink = nd;
+    }
+  }
+  if (!sink) throw Error(GBCC_ERR_CUDA, "solve graph: empty captured segment");
+  return sink;
+}
+
+// A conditional node of type `type` after `dep` in graph g; returns its body.
+cudaGraph_t add_conditional(cudaGraph_t g, const cudaGraphNode_t* dep, cudaGraphConditionalHandle hc,
+                            cudaGraphConditionalNodeType type, cudaGraphNode_t* node) {
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = hc;
+  p.conditional.type = type;
+  p.conditional.size = 1;
+  GBCC_CK(cudaGraphAddNode(node, g, dep, nullptr, dep ? 1 : 0, &p));
+  return p.conditional.phGraph_out[0];
+}
+
+// The whole solve loop as one graph (use_graphs = 2): a WHILE node whose body
+// is one iteration -- energy terms, the decision kernel (solve_graph.cu), the
+// Jacobi + DIIS update and the residual of the precision it chose -- so the
+// host launches the graph once per solve and synchronises once.
+void build_solve_graph(gbcc_handle* h) {
+  const gbcc_config& c = h->cfg;
+  const bool mixed = c.precision == GBCC_PREC_MIXED;
+  cudaStream_t st = h->stream;
+  if (!h->rgraph[0]) h->rgraph[0] = capture_residual_graph(h, GBCC_PREC_FP64);
+  if (mixed && !h->rgraph[1]) h->rgraph[1] = capture_residual_graph(h, GBCC_PREC_MIXED);
+  if (!h->d_state) h->d_state = static_cast<gbcc::SolveState*>(gbcc::dev_alloc(sizeof(gbcc::SolveState)));
+  if (!h->d_history) h->d_history = static_cast<double*>(gbcc::dev_alloc((c.max_iter + 1) * 3 * sizeof(double)));
+  if (!h->d_stamps)
+    h->d_stamps = static_cast<unsigned long long*>(gbcc::dev_alloc((c.max_iter + 1) * 2 * sizeof(unsigned long long)));
+  cudaGraph_t G = nullptr;
+  GBCC_CK(cudaGraphCreate(&G, 0));
+  struct GraphGuard {
+    cudaGraph_t g;
+    ~GraphGuard() {
+      if (g) cudaGraphDestroy(g);
+    }
+  } guard{G};
+  cudaGraphConditionalHandle hloop, hup, hmix, hf64;
+  GBCC_CK(cudaGraphConditionalHandleCreate(&hloop, G, 1, cudaGraphCondAssignDefault));
+  cudaGraphNode_t wnode;
+  cudaGraph_t body = add_conditional(G, nullptr, hloop, cudaGraphCondTypeWhile, &wnode);
+  GBCC_CK(cudaGraphConditionalHandleCreate(&hup, body, 0, cudaGraphCondAssignDefault));
+  GBCC_CK(cudaGraphConditionalHandleCreate(&hmix, body, 0, cudaGraphCondAssignDefault));
+  GBCC_CK(cudaGraphConditionalHandleCreate(&hf64, body, 0, cudaGraphCondAssignDefault));
+  gbcc::CcsdTensors& S = h->S;
+  gbcc::SolveParams p{};
+  p.n1 = n1_of(h);
+  p.n2 = n2_of(h);
+  p.max_iter = c.max_iter;
+  p.n_diis = c.n_diis;
+  p.diis_start = c.diis_start;
+  p.diis_ngroup = c.diis_ngroup;
+  p.diis_group_nstart = c.diis_group_nstart;
+  p.refine_iters = c.refine_iters;
+  p.reset_diis = c.refine_reset_diis;
+  p.target = c.target_precision;
+  p.switch_precision = c.mixed_switch_precision;
+  p.Bmat = h->Bmat;
+  p.sums = h->d_out;
+  p.state = h->d_state;
+  p.history = h->d_history;
+  p.cond_loop = hloop;
+  p.cond_update = hup;
+  p.cond_mixed = hmix;
+  p.cond_fp64 = hf64;
+  capture_into(h, body, [&] {
+    gbcc::launch_energy_terms(c.o, c.v, S.r1->d, S.r2->d, S.f_ai->d, S.g_abij->d, S.t1->d, S.tau->d, h->d_partial,
+                              h->d_out, st);
+    gbcc::launch_solve_decide(p, st);
+  });
+  cudaGraphNode_t decide = sink_node(body);
+  cudaGraphNode_t nup;
+  cudaGraph_t ub = add_conditional(body, &decide, hup, cudaGraphCondTypeIf, &nup);
+  gbcc::DiisArgs d{};
+  d.dyn = &h->d_state->diis;
+  d.o = c.o;
+  d.v = c.v;
+  d.eps_o = S.eps_o->d;
+  d.eps_v = S.eps_v->d;
+  d.t1 = S.t1->d;
+  d.t2 = S.t2->d;
+  d.r1 = S.r1->d;
+  d.r2 = S.r2->d;
+  d.x1 = h->x1;
+  d.x2 = h->x2;
+  d.e1 = h->e1;
+  d.e2 = h->e2;
+  d.ndiis = c.n_diis;
+  d.partial = h->d_partial;
+  d.Bmat = h->Bmat;
+  d.coef = h->coef;
+  d.damping = c.diis_damp;
+  d.nskip_out = h->d_nskip;
+  capture_into(h, ub, [&] {
+    gbcc::launch_diis_step(d, st);
+    gbcc::launch_diis_extrapolate(c.o, c.v, h->x1, h->x2, h->coef, c.n_diis, nullptr, 0, S.t1->d, S.t2->d,
+                                  S.tau->d, st, &h->d_state->diis);
+  });
+  // residual of the chosen precision, timestamped on the device
+  auto add_residual = [&](cudaGraphConditionalHandle hc, cudaGraphNode_t dep, cudaGraph_t rg) {
+    cudaGraphNode_t n, s0, child, s1;
+    cudaGraph_t rb = add_conditional(body, &dep, hc, cudaGraphCondTypeIf, &n);
+    if (!rg) {
+      GBCC_CK(cudaGraphAddEmptyNode(&s0, rb, nullptr, 0));
+      return n;
+    }
+    GBCC_CK(gbcc::add_stamp_node(rb, nullptr, 0, h->d_stamps, h->d_state, 0, &s0));
+    GBCC_CK(cudaGraphAddChildGraphNode(&child, rb, &s0, 1, rg));
+    GBCC_CK(gbcc::add_stamp_node(rb, &child, 1, h->d_stamps, h->d_state, 1, &s1));
+    return n;
+  };
+  cudaGraphNode_t last = add_residual(hf64, nup, h->rgraph[0]);
+  add_residual(hmix, last, mixed ? h->rgraph[1] : nullptr);
+  cudaGraphExec_t ge = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&ge, G, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(GBCC_ERR_CUDA, std::string("solve graph instantiation: ") + cudaGetErrorString(e));
+  }
+  h->solve_exec = ge;
 }
 
 void print_iter(int iter, double dE, double error, double E, double t) {
@@ -431,7 +620,7 @@ void gbcc_config_default(gbcc_config* c) {
   c->diis_group_nstart = 1;
   c->verbose = 0;
   c->device = 0;
-  c->use_graphs = 1;
+  c->use_graphs = 2;
   c->slice_tolerance = 1e-5;
   c->autotune = 1;
   c->refine_reset_diis = 1;
@@ -646,7 +835,42 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
     int diis_iter = 0, nvec = 0, head = -1;
     std::vector<int> slots;  // age order
     auto wall0 = std::chrono::steady_clock::now();
-    while (iter < c.max_iter) {
+    const bool graph_solve = c.use_graphs == 2 && !h->profiling && !h->calibrating;
+    if (graph_solve) {
+      // the whole loop below, decided on the device: one launch, one synchronisation
+      if (!h->solve_exec) build_solve_graph(h);
+      gbcc::launch_solve_init(h->d_state, mixed_phase ? 1 : 0, h->stream);
+      GBCC_CK(cudaGraphLaunch(h->solve_exec, h->stream));
+      sync_check(h);
+      gbcc::SolveState ss{};
+      GBCC_CK(cudaMemcpy(&ss, h->d_state, sizeof(ss), cudaMemcpyDeviceToHost));
+      const int ntest = ss.iter + (ss.stop ? 1 : 0);
+      std::vector<double> hist(3 * static_cast<size_t>(std::max(ntest, 1)));
+      std::vector<unsigned long long> stamps(2 * static_cast<size_t>(std::max(ss.iter, 1)));
+      if (ntest > 0)
+        GBCC_CK(cudaMemcpy(hist.data(), h->d_history, 3 * ntest * sizeof(double), cudaMemcpyDeviceToHost));
+      if (ss.iter > 0)
+        GBCC_CK(cudaMemcpy(stamps.data(), h->d_stamps, 2 * ss.iter * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost));
+      if (ss.status) throw Error(GBCC_ERR_NUMERIC, "non-finite energy or residual at iteration " + std::to_string(ss.iter));
+      for (int k = 0; k < ss.iter; ++k) {
+        const double secs_k = static_cast<double>(stamps[2 * k + 1] - stamps[2 * k]) * 1e-9;
+        if (k < ss.mixed_resid)
+          t_mixed += secs_k;
+        else
+          t_fp64 += secs_k;
+      }
+      mixed_resid += ss.mixed_resid;
+      fp64_resid += ss.fp64_resid;
+      iter = ss.iter;
+      converged = ss.converged != 0;
+      E1 = ss.E1;
+      dE = ss.dE;
+      error = ss.error;
+      if (c.verbose)
+        for (int k = 1; k < ntest; ++k) print_iter(k, hist[3 * k + 1], hist[3 * k + 2], hist[3 * k], 0.0);
+    }
+    while (!graph_solve && iter < c.max_iter) {
       auto ee = energy_error(h);
       error = ee.second;
       E0 = E1;
@@ -782,7 +1006,7 @@ gbcc_status gbcc_destroy(gbcc_handle* h) {
   h->aux.reset();
   for (void* p : {(void*)h->x1, (void*)h->x2, (void*)h->e1, (void*)h->e2, (void*)h->Bmat, (void*)h->coef,
                   (void*)h->d_nskip, (void*)h->d_err, (void*)h->d_partial, (void*)h->d_out,
-                  (void*)h->seed1, (void*)h->seed2})
+                  (void*)h->seed1, (void*)h->seed2, (void*)h->d_state, (void*)h->d_history, (void*)h->d_stamps})
     gbcc::dev_free(p);
   if (h->h_out) cudaFreeHost(h->h_out);
   if (h->ev0) cudaEventDestroy(h->ev0);

@@ -746,14 +746,35 @@ __global__ void __launch_bounds__(kThreads) maxabs_diff_kernel(int64_t n, const 
 
 constexpr int kDiisMax = 16;
 
+// slot, nvec, slots and the extrapolation flag of this DIIS step, from the
+// launch arguments or (graph solve) from device memory, into shared memory
+struct DiisMeta {
+  int slot, nvec, extrapolate;
+  int slots[kDiisMax];
+};
+
+__device__ __forceinline__ void load_diis_meta(const DiisArgs& d, DiisMeta* m) {
+  const DiisDyn* y = d.dyn;
+  if (threadIdx.x < kDiisMax) m->slots[threadIdx.x] = y ? y->slots[threadIdx.x] : d.slots[threadIdx.x];
+  if (threadIdx.x == 0) {
+    m->slot = y ? y->slot : d.slot;
+    m->nvec = y ? y->nvec : d.nvec;
+    m->extrapolate = y ? y->extrapolate : d.extrapolate;
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) {
   __shared__ double sh[kThreads];
+  __shared__ DiisMeta meta;
+  load_diis_meta(d, &meta);
+  const int slot = meta.slot, nvec = meta.nvec;
   const int64_t o = d.o, v = d.v, o2 = o * o, n2 = v * v * o2, n1 = v * o;
   double acc[kDiisMax];
 #pragma unroll
   for (int q = 0; q < kDiisMax; ++q) acc[q] = 0.0;
-  double* x2n = d.x2 + static_cast<int64_t>(d.slot) * n2;
-  double* e2n = d.e2 + static_cast<int64_t>(d.slot) * n2;
+  double* x2n = d.x2 + static_cast<int64_t>(slot) * n2;
+  double* e2n = d.e2 + static_cast<int64_t>(slot) * n2;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
     int64_t a, b;
     divmod32(p, v, a, b);
@@ -768,15 +789,16 @@ __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) 
       e2n[e] = r;
 #pragma unroll
       for (int q = 0; q < kDiisMax; ++q) {
-        if (q < d.nvec) {
-          const double eq = (d.slots[q] == d.slot) ? r : d.e2[static_cast<int64_t>(d.slots[q]) * n2 + e];
+        if (q < nvec) {
+          const int sq = meta.slots[q];
+          const double eq = (sq == slot) ? r : d.e2[static_cast<int64_t>(sq) * n2 + e];
           acc[q] = fma(r, eq, acc[q]);
         }
       }
     }
   }
-  double* x1n = d.x1 + static_cast<int64_t>(d.slot) * n1;
-  double* e1n = d.e1 + static_cast<int64_t>(d.slot) * n1;
+  double* x1n = d.x1 + static_cast<int64_t>(slot) * n1;
+  double* e1n = d.e1 + static_cast<int64_t>(slot) * n1;
   for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n1;
        e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     int64_t a, i;
@@ -786,13 +808,14 @@ __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) 
     e1n[e] = r;
 #pragma unroll
     for (int q = 0; q < kDiisMax; ++q) {
-      if (q < d.nvec) {
-        const double eq = (d.slots[q] == d.slot) ? r : d.e1[static_cast<int64_t>(d.slots[q]) * n1 + e];
+      if (q < nvec) {
+        const int sq = meta.slots[q];
+        const double eq = (sq == slot) ? r : d.e1[static_cast<int64_t>(sq) * n1 + e];
         acc[q] = fma(r, eq, acc[q]);
       }
     }
   }
-  for (int q = 0; q < d.nvec; ++q) {
+  for (int q = 0; q < nvec; ++q) {
     const double s = block_sum(acc[q], sh);
     if (threadIdx.x == 0) d.partial[blockIdx.x * kDiisMax + q] = s;
   }
@@ -836,7 +859,10 @@ __device__ double gepp(double* A, double* b, double* x, int n) {
 __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
   __shared__ double sh[kThreads];
   __shared__ double dots[kDiisMax];
-  for (int q = 0; q < d.nvec; ++q) {
+  __shared__ DiisMeta meta;
+  load_diis_meta(d, &meta);
+  const int slot = meta.slot;
+  for (int q = 0; q < meta.nvec; ++q) {
     double s = 0.0;
     for (int b = threadIdx.x; b < kReduceBlocks; b += blockDim.x) s += d.partial[b * kDiisMax + q];
     s = block_sum(s, sh);
@@ -845,14 +871,15 @@ __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
   __syncthreads();
   if (threadIdx.x != 0) return;
   const int nd = d.ndiis;
-  for (int q = 0; q < d.nvec; ++q) {
-    d.Bmat[d.slot * nd + d.slots[q]] = dots[q];
-    d.Bmat[d.slots[q] * nd + d.slot] = dots[q];
+  const int* slots = meta.slots;
+  for (int q = 0; q < meta.nvec; ++q) {
+    d.Bmat[slot * nd + slots[q]] = dots[q];
+    d.Bmat[slots[q] * nd + slot] = dots[q];
   }
   for (int s = 0; s < nd; ++s) d.coef[s] = 0.0;
-  const int n = d.nvec;
-  if (!d.extrapolate) {
-    d.coef[d.slot] = 1.0;
+  const int n = meta.nvec;
+  if (!meta.extrapolate) {
+    d.coef[slot] = 1.0;
     *d.nskip_out = -1;
     return;
   }
@@ -863,7 +890,7 @@ __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
     const int m = n - nskip;
     const int w = m + 1;
     // normalise by the oldest kept vector's <e, e>
-    const double b0 = fabs(d.Bmat[d.slots[nskip] * nd + d.slots[nskip]]);
+    const double b0 = fabs(d.Bmat[slots[nskip] * nd + slots[nskip]]);
     const double norm = b0 > 0.0 ? 1.0 / b0 : 1.0;
     for (int r = 0; r < w; ++r) {
       rhs[r] = (r == 0) ? -1.0 : 0.0;
@@ -871,19 +898,19 @@ __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
         double val;
         if (r == 0 && c == 0) val = 0.0;
         else if (r == 0 || c == 0) val = -1.0;
-        else val = d.Bmat[d.slots[nskip + r - 1] * nd + d.slots[nskip + c - 1]] * norm;
+        else val = d.Bmat[slots[nskip + r - 1] * nd + slots[nskip + c - 1]] * norm;
         if (r > 0 && r == c) val *= 1.0 + d.damping;
         A[r * w + c] = val;
       }
     }
     const double det = gepp(A, rhs, sol, w);
     if (det > 0.0 && (det >= kDiisDetMin || nskip == n - 1)) {
-      for (int q = 0; q < m; ++q) d.coef[d.slots[nskip + q]] = sol[q + 1];
+      for (int q = 0; q < m; ++q) d.coef[slots[nskip + q]] = sol[q + 1];
       *d.nskip_out = nskip;
       return;
     }
   }
-  d.coef[d.slot] = 1.0;
+  d.coef[slot] = 1.0;
   *d.nskip_out = n - 1;
 }
 
@@ -897,22 +924,36 @@ struct ExtrapArgs {
   double* t1;
   double* t2;
   double* tau;
+  const DiisDyn* dyn;  // non-NULL: nvec and slots from device memory
 };
 
+__device__ __forceinline__ void load_extrap_meta(const ExtrapArgs& x, int* s_slots, int* s_nvec) {
+  if (threadIdx.x < kDiisMax) s_slots[threadIdx.x] = x.dyn ? x.dyn->slots[threadIdx.x] : x.slots[threadIdx.x];
+  if (threadIdx.x == 0) *s_nvec = x.dyn ? x.dyn->nvec : x.nvec;
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kThreads) extrapolate_t1_kernel(ExtrapArgs x) {
+  __shared__ int slots[kDiisMax];
+  __shared__ int nvec;
+  load_extrap_meta(x, slots, &nvec);
   const int64_t n1 = x.v * x.o;
   for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n1;
        e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     double acc = 0.0;
-    for (int q = 0; q < x.nvec; ++q) acc = fma(x.coef[x.slots[q]], x.x1[x.slots[q] * n1 + e], acc);
+    for (int q = 0; q < nvec; ++q) acc = fma(x.coef[slots[q]], x.x1[slots[q] * n1 + e], acc);
     x.t1[e] = acc;
   }
 }
 
 __global__ void __launch_bounds__(kThreads) extrapolate_t2_tau_kernel(ExtrapArgs x) {
+  __shared__ int slots[kDiisMax];
+  __shared__ int s_nvec;
+  load_extrap_meta(x, slots, &s_nvec);
+  const int nvec = s_nvec;
   const int64_t o = x.o, v = x.v, o2 = o * o, n2 = v * v * o2;
   double c[kDiisMax];
-  for (int q = 0; q < kDiisMax; ++q) c[q] = (q < x.nvec) ? x.coef[x.slots[q]] : 0.0;
+  for (int q = 0; q < kDiisMax; ++q) c[q] = (q < nvec) ? x.coef[slots[q]] : 0.0;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
     int64_t a, b;
     divmod32(p, v, a, b);
@@ -921,7 +962,7 @@ __global__ void __launch_bounds__(kThreads) extrapolate_t2_tau_kernel(ExtrapArgs
       divmod32(ij, o, i, j);
       const int64_t e = p * o2 + ij;
       double acc = 0.0;
-      for (int q = 0; q < x.nvec; ++q) acc = fma(c[q], x.x2[x.slots[q] * n2 + e], acc);
+      for (int q = 0; q < nvec; ++q) acc = fma(c[q], x.x2[slots[q] * n2 + e], acc);
       x.t2[e] = acc;
       x.tau[e] = fma(x.t1[a * o + i], x.t1[b * o + j], acc);
     }
@@ -1097,7 +1138,7 @@ void launch_diis_step(const DiisArgs& d, cudaStream_t st) {
 
 void launch_diis_extrapolate(int64_t o, int64_t v, const double* x1, const double* x2,
                              const double* coef, int ndiis, const int* slots, int nvec,
-                             double* t1, double* t2, double* tau, cudaStream_t st) {
+                             double* t1, double* t2, double* tau, cudaStream_t st, const DiisDyn* dyn) {
   (void)ndiis;
   ExtrapArgs x;
   x.o = o;
@@ -1106,10 +1147,11 @@ void launch_diis_extrapolate(int64_t o, int64_t v, const double* x1, const doubl
   x.x2 = x2;
   x.coef = coef;
   x.nvec = nvec;
-  for (int q = 0; q < kDiisMax; ++q) x.slots[q] = (q < nvec) ? slots[q] : 0;
+  for (int q = 0; q < kDiisMax; ++q) x.slots[q] = (slots && q < nvec) ? slots[q] : 0;
   x.t1 = t1;
   x.t2 = t2;
   x.tau = tau;
+  x.dyn = dyn;
   extrapolate_t1_kernel<<<grid_for(v * o, kThreads), kThreads, 0, st>>>(x);
   extrapolate_t2_tau_kernel<<<grid_for(v * v, 1), kThreads, 0, st>>>(x);
 }

@@ -240,7 +240,17 @@ void launch_make_tau(int64_t o, int64_t v, const double* t1, const double* t2, d
 //   dots[j] = <e_new, e_j> for the nvec slots listed in `slots` (partials in
 //   scratch, reduced into Bmat row/column `slot`).
 // ---------------------------------------------------------------------------
+// DIIS bookkeeping kept in device memory when the solve loop runs as one CUDA
+// graph (the decision kernel of solve_graph.cu writes it each iteration)
+struct DiisDyn {
+  int slot;
+  int nvec;
+  int slots[16];
+  int extrapolate;
+};
+
 struct DiisArgs {
+  const DiisDyn* dyn;  // non-NULL: slot, nvec, slots and extrapolate are read from here
   int64_t o, v;
   const double* eps_o;
   const double* eps_v;
@@ -266,8 +276,46 @@ struct DiisArgs {
 void launch_diis_step(const DiisArgs& d, cudaStream_t st);
 
 // t1 = sum_j coef[j] x1_j, t2 = sum_j coef[j] x2_j, tau = t2 + t1 t1
+// (dyn non-NULL: nvec and slots read from device memory)
 void launch_diis_extrapolate(int64_t o, int64_t v, const double* x1, const double* x2,
                              const double* coef, int ndiis, const int* slots, int nvec,
-                             double* t1, double* t2, double* tau, cudaStream_t st);
+                             double* t1, double* t2, double* tau, cudaStream_t st,
+                             const DiisDyn* dyn = nullptr);
+
+// ---------------------------------------------------------------------------
+// Whole-solve CUDA graph (solve_graph.cu): the convergence test of each
+// iteration runs on the device and drives the graph's conditional nodes.
+// ---------------------------------------------------------------------------
+struct SolveState {
+  // loop
+  int iter, converged, stop, status;  // status: 0 ok, 1 non-finite energy or residual
+  int mixed_phase, used_mixed, stalled, pending_reset;
+  int fp64_resid, mixed_resid;
+  double E0, E1, dE, error, best_error, best_dE;
+  // DIIS bookkeeping (read by the DIIS kernels)
+  int diis_iter, head;
+  DiisDyn diis;
+};
+struct SolveParams {
+  int64_t n1, n2;
+  int max_iter, n_diis, diis_start, diis_ngroup, diis_group_nstart, refine_iters, reset_diis;
+  double target, switch_precision;
+  double* Bmat;                 // [n_diis][n_diis], cleared at a DIIS restart
+  const double* sums;           // the energy reduction's four sums
+  SolveState* state;
+  double* history;              // [max_iter + 1][3]: E, dE, error per convergence test
+  unsigned long long cond_loop, cond_update, cond_mixed, cond_fp64;  // cudaGraphConditionalHandle
+};
+// zero the state for a solve (mixed: start in the mixed phase)
+void launch_solve_init(SolveState* s, int mixed, cudaStream_t st);
+// one thread: E, error, convergence test, phase switch, DIIS bookkeeping,
+// and the conditions of the loop, the update and the residual precision
+void launch_solve_decide(const SolveParams& p, cudaStream_t st);
+// nanosecond timestamp (globaltimer) of the current iteration's residual:
+// base[2 (iter - 1) + which]
+void launch_stamp(unsigned long long* base, const SolveState* s, int which, cudaStream_t st);
+// the same as an explicit kernel node of graph g
+cudaError_t add_stamp_node(cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps, unsigned long long* base,
+                           const SolveState* s, int which, cudaGraphNode_t* out);
 
 }  // namespace gbcc

@@ -44,7 +44,7 @@ def test_defaults_follow_the_reference(lib):
     # ccsd.h:104 max_iter 30; cc/solvers.h:93-95 DIIS; energy.h:45 precision 1e-9
     assert c.max_iter == 30 and c.n_diis == 8 and c.diis_start == 1
     assert c.diis_damp == 0.0 and c.diis_ngroup == 1 and c.diis_group_nstart == 1
-    assert c.target_precision == 1e-9 and c.precision == 0 and c.use_graphs == 1
+    assert c.target_precision == 1e-9 and c.precision == 0 and c.use_graphs == 2
     assert (c.slices_ladder, c.slices_ring, c.slices_other) == (0, 0, 0) and c.slice_tolerance == 1e-5
     assert c.mixed_switch_precision == 0.0 and c.autotune == 1 and c.refine_reset_diis == 1
 

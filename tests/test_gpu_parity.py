@@ -165,6 +165,40 @@ def test_graph_solve_matches_direct_solve():
     assert rg.iters == rd.iters and eg == ed and np.array_equal(t2g, t2d)
 
 
+@pytest.mark.parametrize("precision,max_iter", [("fp64", 60), ("mixed", 60), ("mixed", 7), ("fp64", 3)])
+def test_whole_solve_graph_makes_the_host_loops_decisions(precision, max_iter):
+    """use_graphs = 2 (the loop as one graph, convergence decided on the device)
+    gives the host-driven loop's iterations, phase switch, energy and
+    amplitudes bit for bit, converged or stopped at max_iter."""
+    inp = synth.make_inputs(5, 24, 20, seed=43, b_scale=0.03)
+    kw = dict(precision=precision, target_precision=1e-10, max_iter=max_iter)
+    if precision == "mixed":
+        kw["slices"] = (2, 2, 2)
+    runs = []
+    for ug in (1, 2):
+        with _solver(inp, use_graphs=ug, **kw) as s:
+            e, t1, t2, rep = s.solve()
+            e2, u1, u2, rep2 = s.solve()   # the graph is replayed
+        runs.append((e, t1, t2, rep, e2, u2, rep2))
+    (e1, a1, b1, r1, f1, c1, q1), (eg, ag, bg, rg, fg, cg, qg) = runs
+    assert (rg.iters, rg.mixed_iters, rg.fp64_iters, rg.converged) == (r1.iters, r1.mixed_iters, r1.fp64_iters,
+                                                                     r1.converged)
+    assert eg == e1 and np.array_equal(bg, b1) and np.array_equal(ag, a1)
+    assert fg == eg and np.array_equal(cg, bg) and qg.iters == rg.iters
+    assert rg.converged == (max_iter == 60)
+    if precision == "mixed" and max_iter == 60:
+        assert rg.mixed_iters > 0 and rg.fp64_iters >= 2 and rg.seconds_residual_mixed > 0.0
+
+
+def test_whole_solve_graph_restart():
+    inp = synth.make_inputs(5, 19, 30, seed=22)
+    with _solver(inp, use_graphs=2, target_precision=1e-10, max_iter=40) as s:
+        e0, t1, t2, rep0 = s.solve()
+        s.set_amplitudes(t1, t2)
+        e1, _, u2, rep1 = s.solve()
+    assert rep1.converged and rep1.iters <= 2 and abs(e1 - e0) < 1e-10
+
+
 def test_automatic_slices_follow_measured_error():
     """Slice counts 0 are chosen at set_inputs from the measured residual change
     against 3 slices; the residual stays within the tolerance of the 3-slice one."""
