@@ -15,10 +15,14 @@ Reported (one JSON line):
   e2e        the same through the C ABI with host (pinned) t1/t2 in and r1/r2 out
   fp64       the plain-FP64 residual on the same inputs (s/iter, TFLOP/s)
   roofline   the particle-particle ladder GEMM (dominant kernel) against the BF16 tensor peak
-  cpu_baseline  the FP64 oracle on the host cores on a bounded sample (o=32, v=96)
+  cpu_baseline  the FP64 oracle on the host cores at the same o, v: each of the
+             residual's contractions timed on a slab of its first output index
+             and scaled back (oracle/ccsd_sample.py)
 
 --impl reference times the FP64 CPU oracle (the restatement of the reference's
-CPU path; the reference itself cannot be built here) on that bounded sample.
+CPU path; the reference itself cannot be built here) the same way, on the
+same workload and config as this arm.
+--config h2o10 runs (H2O)10 / cc-pVDZ from the geometry (mixed and FP64 solves).
 Multi-GPU (torchrun): every rank runs an independent replica ("replicas only",
 weak scaling); value = sum of all ranks' FLOPs / max rank time.
 """
@@ -38,7 +42,6 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "CCSD s/iter and residual TFLOP/s, mixed vs plain-FP64 on 1 GB300 at |ΔE|≤1e-6 Eh"
-CPU_SAMPLE = (32, 96, 200)   # o, v, naux of the bounded CPU sample
 
 
 def flop_count(o, v):
@@ -76,22 +79,6 @@ def log(*a):
 # ---------------------------------------------------------------------------
 # CPU baseline / reference arm: the FP64 oracle on a bounded sample
 
-def cpu_residual_rate(steps, warmup, sample=CPU_SAMPLE):
-    from mpqc_gb300 import synth
-    from oracle import ccsd_ref as R
-    o, v, naux = sample
-    inp = synth.make_inputs(o, v, naux, seed=1, t1_scale=1e-3)
-    ints = R.Integrals(inp.Fia, inp.Fij, inp.Fab, inp.Gijab, inp.Gijkl, inp.Giajb, inp.Gijka,
-                       inp.Giabc, inp.Gabcd)
-    for _ in range(warmup):
-        R.residual(inp.t1, inp.t2, ints)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        R.residual(inp.t1, inp.t2, ints)
-    dt = (time.perf_counter() - t0) / steps
-    return flop_count(o, v) / dt / 1e12, dt
-
-
 def cpu_threads():
     try:
         from threadpoolctl import threadpool_info
@@ -103,24 +90,46 @@ def cpu_threads():
     return os.cpu_count() or 1
 
 
+def bench_config(args, ws):
+    """The workload both arms report (identical dicts)."""
+    return {"workload": "synthetic CCSD doubles residual, one R1+R2 evaluation",
+            "o": args.o, "v": args.v, "naux": args.naux, "parallelism": f"replicas{ws}",
+            "flops_per_step": flop_count(args.o, args.v), "l2": "inputs larger than L2 (no flush)"}
+
+
+def cpu_sampled_rate(o, v, frac, steps, warmup):
+    """TFLOP/s of the FP64 oracle's residual at (o, v), each step a bounded
+    sample: every contraction of the residual at its full shapes with the
+    first output index cut to a slab of `frac` (oracle/ccsd_sample.py),
+    scaled back by the slab fraction."""
+    from oracle import ccsd_sample as S
+    tr = S.trace()
+    for _ in range(warmup):
+        S.sampled_seconds(o, v, frac, tr)
+    est = [S.sampled_seconds(o, v, frac, tr)[0] for _ in range(max(1, steps))]
+    sec = float(np.median(est))
+    return flop_count(o, v) / sec / 1e12, sec
+
+
+def cpu_sample_text(o, v, frac):
+    return (f"FP64 oracle residual (numpy/OpenBLAS restatement of the reference's R1+R2) at o={o} v={v}: "
+            f"each of its 55 contractions timed at full shapes with the first output index cut to "
+            f"1/{round(1 / frac)} of its range, scaled back; array additions between contractions not timed")
+
+
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if ws > 1 and rank != 0:
         return 0
-    o, v, naux = args.cpu_sample
-    rate, dt = cpu_residual_rate(max(1, args.steps), max(0, args.warmup), args.cpu_sample)
+    rate, sec = cpu_sampled_rate(args.o, args.v, args.cpu_frac, max(1, args.steps), max(0, args.warmup))
     line = {
         "metric": METRIC, "value": rate, "unit": "TFLOP/s", "impl": "reference",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        # the workload of the GPU arm; each step times a bounded sample of it
-        "config": {"workload": "synthetic CCSD doubles residual, one R1+R2 evaluation",
-                   "o": args.o, "v": args.v, "naux": args.naux, "parallelism": f"{cpu_threads()} host threads",
-                   "sample": {"o": o, "v": v, "naux": naux}},
+        "config": bench_config(args, ws),
         "cpu_baseline": {"value": rate, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
-                         "sample": f"one FP64 R1+R2 residual at o={o} v={v} naux={naux} per step "
-                                   "(numpy/OpenBLAS restatement of the reference's CPU CCSD)"},
+                         "sample": cpu_sample_text(args.o, args.v, args.cpu_frac)},
         "e2e": {"value": rate, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -375,22 +384,21 @@ def ours(args):
         return 0
     cpu = None
     if not args.no_cpu:
-        rate, dt = cpu_residual_rate(1, 1, args.cpu_sample)
-        o_, v_, n_ = args.cpu_sample
+        rate, sec = cpu_sampled_rate(o, v, args.cpu_frac, 1, 1)
         cpu = {"value": rate, "unit": "TFLOP/s", "cores": cpu_threads(), "kind": "port",
-               "sample": f"one FP64 R1+R2 residual of the oracle at o={o_} v={v_} naux={n_} ({dt:.2f} s)"}
+               "sample": cpu_sample_text(o, v, args.cpu_frac) + f" ({sec:.1f} s per residual estimated)"}
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "s_per_iter": ms_step * 1e-3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        # the arithmetic of the contractions: FP64 operands split into BF16
+        # slices, FP32 tensor-core accumulation, FP64 in and out
+        "dtype": f"split-bf16x{max(slices_used)} (f64 I/O)",
         "data": "synthetic",
-        "config": {"workload": "synthetic CCSD doubles residual, one R1+R2 evaluation",
-                   "o": o, "v": v, "naux": naux, "parallelism": f"replicas{ws}",
-                   "precision": "split-BF16 slices per class (ladder, ring, other) = "
-                                f"{slices_used}, FP32/float-float chunk accumulation",
-                   "slices": list(slices_used),
-                   "slice_rel_change_vs_3": list(slice_err),
-                   "flops_per_step": F, "l2": "inputs larger than L2 (no flush)"},
+        "config": bench_config(args, ws),
+        "precision_policy": {"slices_ladder_ring_other": list(slices_used),
+                             "slice_rel_change_vs_3": list(slice_err),
+                             "accumulation": "FP32 TMEM chunks, float-float or FP32 register fold, FP64 epilogue"},
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io, "ms_per_step": e2e_ms},
         "fp64": fp64,
@@ -584,8 +592,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--o", type=int, default=32)
-    ap.add_argument("--v", type=int, default=320)
+    ap.add_argument("--o", "--nocc", dest="o", type=int, default=32)
+    ap.add_argument("--v", "--nvirt", dest="v", type=int, default=320)
     ap.add_argument("--naux", type=int, default=1200)
     ap.add_argument("--slices", type=int, default=0,
                     help="BF16 slices per operand for every class; 0 (default): chosen per class "
@@ -604,8 +612,8 @@ def main():
     ap.add_argument("--solve-precision", type=float, default=1e-8)
     ap.add_argument("--max-iter", type=int, default=40)
     ap.add_argument("--no-solve-fp64", action="store_true")
-    ap.add_argument("--cpu-sample", type=lambda s: tuple(int(x) for x in s.split(",")), default=CPU_SAMPLE,
-                    help="o,v,naux of the CPU oracle sample timed by --impl reference")
+    ap.add_argument("--cpu-frac", type=float, default=1.0 / 16,
+                    help="slab of each contraction's first output index timed by the CPU oracle sample")
     ap.add_argument("--gemm", type=lambda s: tuple(int(x) for x in s.split(",")), default=None,
                     metavar="M,N,K", help="profiling aid: time one GEMM shape on the library's kernels")
     ap.add_argument("--gemm-slices", type=int, default=2, help="BF16 slices (0: plain FP64 kernel)")

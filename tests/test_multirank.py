@@ -52,7 +52,7 @@ def test_reference_arm_under_torchrun_prints_once():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-sample", "3,8,6"]
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--nocc", "6", "--nvirt", "16", "--cpu-frac", "0.5"]
     p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
     assert p.returncode == 0, p.stderr[-2000:]
     lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]

@@ -138,3 +138,28 @@ def test_flop_count_matches_contraction_list():
     assert abs(f - 3.53e13) / 3.53e13 < 0.01
     assert abs(2 * 32**2 * 320**4 / f - 0.61) < 0.01
     assert synth.flop_count(5, 19) == R.flop_count(5, 19)
+
+
+def test_sampled_residual_time_tracks_the_full_residual():
+    """The CPU baseline's bounded sample (every contraction of the oracle's
+    residual on a slab of its first output index, scaled back) estimates the
+    time of the full residual to within a factor of two."""
+    import time
+    from mpqc_gb300 import synth
+    from oracle import ccsd_sample as S
+    tr = S.trace()
+    assert len(tr) > 40 and any(spec == "cdij,abcd->abij" for spec, _ in tr)
+    o, v = 12, 48
+    inp = synth.make_inputs(o, v, 40, seed=1, t1_scale=1e-3)
+    ints = R.Integrals(inp.Fia, inp.Fij, inp.Fab, inp.Gijab, inp.Gijkl, inp.Giajb, inp.Gijka, inp.Giabc,
+                       inp.Gabcd)
+    R.residual(inp.t1, inp.t2, ints)
+    full = min(_timed(lambda: R.residual(inp.t1, inp.t2, ints), time) for _ in range(3))
+    est = min(S.sampled_seconds(o, v, 0.5, tr)[0] for _ in range(3))
+    assert 0.5 * full < est < 2.0 * full, (full, est)
+
+
+def _timed(fn, time):
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
