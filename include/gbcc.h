@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define GBCC_ABI_VERSION 4
+#define GBCC_ABI_VERSION 5
 
 typedef enum gbcc_status {
   GBCC_OK = 0,
@@ -109,6 +109,27 @@ typedef struct gbcc_inputs {
   const double* Gabcd;   /* [v][v][v][v] */
 } gbcc_inputs;
 
+/* Density-fitted inputs (the reference's method "df" with the lazy (ab|cd)
+ * ladder, ccsd_r1_r2.h:136-184, 309-520): the four-index blocks the DF
+ * residual reads plus three-index factors with (pq|rs) = sum_K (K|pq)(K|rs).
+ * The (ab|cd) block is never stored: the ladder builds its rows block by
+ * block from Xab on the tensor cores every residual, and <ia|bc> is built
+ * once from Xai and Xab. */
+typedef struct gbcc_df_inputs {
+  const double* eps_o;   /* [o] */
+  const double* eps_v;   /* [v] */
+  const double* Fia;     /* [o][v] */
+  const double* Fij;     /* [o][o] */
+  const double* Fab;     /* [v][v] */
+  const double* Gijab;   /* [o][o][v][v] */
+  const double* Gijkl;   /* [o][o][o][o] */
+  const double* Giajb;   /* [o][v][o][v] */
+  const double* Gijka;   /* [o][o][o][v] */
+  int64_t naux;          /* auxiliary (fitting) functions                */
+  const double* Xai;     /* [naux][v][o] = (K|ai)  (MPQC's Xai("K,a,i")) */
+  const double* Xab;     /* [naux][v][v] = (K|ab)  (MPQC's Xab("K,a,b")) */
+} gbcc_df_inputs;
+
 typedef struct gbcc_report {
   int32_t iters;            /* residual evaluations performed                     */
   int32_t converged;        /* 1 if the convergence test of cc/solvers.h:150 held */
@@ -140,6 +161,14 @@ gbcc_status gbcc_create(gbcc_handle** out, const gbcc_config* cfg);
  * prepare every contraction (split copies of the constant integrals in the
  * mixed mode).  May be called again to replace the inputs. */
 gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in);
+
+/* Density-fitted alternative to gbcc_set_inputs (host or device pointers):
+ * the handle then evaluates the residual of compute_cs_ccsd_r1_df /
+ * compute_cs_ccsd_r2_df (ccsd_r1_r2.h:136-184, 309-520) without a v^4
+ * array.  The first set call fixes a handle's kind: a handle set up with
+ * gbcc_set_inputs rejects this call (GBCC_ERR_STATE) and vice versa, as does
+ * a later call with another naux. */
+gbcc_status gbcc_set_df_inputs(gbcc_handle* h, const gbcc_df_inputs* in);
 
 /* Zero-copy alternative to gbcc_set_inputs for integrals too large to hold
  * twice in device memory (the v^4 (ab|cd) block is 84 GB at v = 320):

@@ -61,6 +61,10 @@ int gbcc_testing_gemm_ex3(int64_t M, int64_t N, int64_t K, const double* A, cons
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);
 
+/* Rows a per block of the density-fitted ladder for handles whose inputs are
+ * set from now on (0: the default size, a block of (ab|cd) of at most 4 GB). */
+int gbcc_testing_df_block_rows(int64_t rows);
+
 /* Symmetric eigensolver of the RHF driver (host code, no GPU needed):
  * eigenvalues w[n] ascending, eigenvectors V[n][n] by column. */
 int gbcc_testing_eigh(int32_t n, const double* A, double* w, double* V);

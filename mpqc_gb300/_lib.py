@@ -26,7 +26,7 @@ EXPORTS = (
     "gbcc_set_inputs", "gbcc_device_inputs", "gbcc_commit_inputs", "gbcc_residual",
     "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error", "gbcc_set_amplitudes",
-    "gbcc_save_amplitudes", "gbcc_load_amplitudes",
+    "gbcc_save_amplitudes", "gbcc_load_amplitudes", "gbcc_set_df_inputs",
 )
 # every symbol include/gbcc_scf.h declares
 SCF_EXPORTS = (
@@ -37,7 +37,8 @@ SCF_EXPORTS = (
 TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_gemm_ex3", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims",
-                   "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total", "gbcc_testing_eigh")
+                   "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total", "gbcc_testing_eigh",
+                   "gbcc_testing_df_block_rows")
 
 
 class Config(C.Structure):
@@ -57,6 +58,11 @@ class Config(C.Structure):
 class Inputs(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in
                 ("eps_o", "eps_v", "Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc", "Gabcd")]
+
+
+class DfInputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("eps_o", "eps_v", "Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka")] + \
+        [("naux", C.c_int64), ("Xai", C.c_void_p), ("Xab", C.c_void_p)]
 
 
 class Report(C.Structure):
@@ -169,6 +175,10 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_slice_policy.argtypes = [vp, vp, vp]
     lib.gbcc_last_error.restype = C.c_char_p
     lib.gbcc_last_error.argtypes = [vp]
+    lib.gbcc_set_df_inputs.restype = C.c_int
+    lib.gbcc_set_df_inputs.argtypes = [vp, C.POINTER(DfInputs)]
+    lib.gbcc_testing_df_block_rows.restype = C.c_int
+    lib.gbcc_testing_df_block_rows.argtypes = [C.c_int64]
     lib.gbcc_set_amplitudes.restype = C.c_int
     lib.gbcc_set_amplitudes.argtypes = [vp, vp, vp]
     lib.gbcc_save_amplitudes.restype = C.c_int

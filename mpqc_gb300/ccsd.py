@@ -133,6 +133,24 @@ class Solver:
         _check(self.lib, self.h, self.lib.gbcc_set_inputs(self.h, C.byref(inp)))
         self._keep = None
 
+    def set_df_inputs(self, eps_o, eps_v, Xai, Xab, **ints):
+        """Density-fitted inputs (the reference's method "df"): Fia, Fij, Fab,
+        Gijab, Gijkl, Giajb, Gijka as for ``set_inputs`` plus the factors
+        Xai[K,a,i] = (K|ai) and Xab[K,a,b] = (K|ab); no (ab|cd) array."""
+        names = ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka")
+        missing = [n for n in names if n not in ints]
+        if missing:
+            raise InputError(f"missing integrals: {missing}")
+        inp = L.DfInputs()
+        inp.eps_o, inp.eps_v = _ptr(eps_o), _ptr(eps_v)
+        for n in names:
+            setattr(inp, n, _ptr(ints[n]))
+        inp.naux = int(Xai.shape[0])
+        inp.Xai, inp.Xab = _ptr(Xai), _ptr(Xab)
+        self._keep = (eps_o, eps_v, Xai, Xab, ints)
+        _check(self.lib, self.h, self.lib.gbcc_set_df_inputs(self.h, C.byref(inp)))
+        self._keep = None
+
     def device_inputs(self):
         """Device pointers (ints) of the handle's own input arrays, to be filled
         on the device before ``commit_inputs()`` (zero-copy set-up)."""

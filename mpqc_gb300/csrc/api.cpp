@@ -684,6 +684,7 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
     const int64_t o = h->cfg.o, v = h->cfg.v;
     validate_eps(in->eps_o, in->eps_v, o, v);
     if (!h->S.t1) h->S.create(*h->eng, o, v);
+    if (h->S.naux > 0) throw Error(GBCC_ERR_STATE, "gbcc_set_inputs: the handle holds density-fitted inputs");
     gbcc::CcsdTensors& S = h->S;
     h->inputs_set = false;
     h->have_solution = false;
@@ -704,10 +705,46 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
   });
 }
 
+gbcc_status gbcc_set_df_inputs(gbcc_handle* h, const gbcc_df_inputs* in) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!in) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_df_inputs: NULL inputs");
+    const double* ptrs[] = {in->eps_o, in->eps_v, in->Fia, in->Fij, in->Fab, in->Gijab,
+                            in->Gijkl, in->Giajb, in->Gijka, in->Xai, in->Xab};
+    for (const double* p : ptrs)
+      if (!p) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_df_inputs: NULL input array");
+    if (in->naux < 1 || in->naux > (int64_t{1} << 20))
+      throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_df_inputs: naux out of range");
+    const int64_t o = h->cfg.o, v = h->cfg.v, nq = in->naux;
+    validate_eps(in->eps_o, in->eps_v, o, v);
+    if (!h->S.t1) h->S.create(*h->eng, o, v, nq);
+    if (h->S.naux != nq)
+      throw Error(GBCC_ERR_STATE, h->S.naux == 0 ? "gbcc_set_df_inputs: the handle holds standard inputs"
+                                                 : "gbcc_set_df_inputs: the handle was set up for another naux");
+    gbcc::CcsdTensors& S = h->S;
+    h->inputs_set = false;
+    h->have_solution = false;
+    h->seeded = false;
+    copy_in(S.eps_o->d, in->eps_o, o, h->stream);
+    copy_in(S.eps_v->d, in->eps_v, v, h->stream);
+    copy_in(S.Fia->d, in->Fia, o * v, h->stream);
+    copy_in(S.Fij->d, in->Fij, o * o, h->stream);
+    copy_in(S.Fab->d, in->Fab, v * v, h->stream);
+    copy_in(S.Gijab->d, in->Gijab, o * o * v * v, h->stream);
+    copy_in(S.Gijkl->d, in->Gijkl, o * o * o * o, h->stream);
+    copy_in(S.Giajb->d, in->Giajb, o * v * o * v, h->stream);
+    copy_in(S.Gijka->d, in->Gijka, o * o * o * v, h->stream);
+    copy_in(S.Xai->d, in->Xai, nq * v * o, h->stream);
+    copy_in(S.Xab->d, in->Xab, nq * v * v, h->stream);
+    commit_inputs(h);
+    return GBCC_OK;
+  });
+}
+
 gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out) {
   return guarded(h, [&]() -> gbcc_status {
     if (!out) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_device_inputs: NULL output");
     if (!h->S.t1) h->S.create(*h->eng, h->cfg.o, h->cfg.v);
+    if (h->S.naux > 0) throw Error(GBCC_ERR_STATE, "gbcc_device_inputs: the handle holds density-fitted inputs");
     GBCC_CK(cudaStreamSynchronize(h->stream));  // zero-initialisation done
     const gbcc::CcsdTensors& S = h->S;
     out->eps_o = S.eps_o->d;

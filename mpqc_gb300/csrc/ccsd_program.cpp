@@ -30,7 +30,30 @@
 
 namespace gbcc {
 
-void CcsdTensors::create(Engine& E, int64_t o, int64_t v) {
+namespace {
+
+// a tensor whose storage lies inside another allocation
+Tensor view(const std::string& name, double* d, std::initializer_list<int64_t> dims) {
+  Tensor t;
+  t.name = name;
+  t.d = d;
+  t.rank = static_cast<int>(dims.size());
+  int k = 0;
+  for (int64_t x : dims) t.dim[k++] = x;
+  return t;
+}
+
+int64_t pairs_before(int64_t a, int64_t v) { return a * v - a * (a - 1) / 2; }     // sym pairs with first < a
+int64_t anti_before(int64_t a, int64_t v) { return a * (v - 1) - a * (a - 1) / 2; }  // anti pairs with first < a
+
+}  // namespace
+
+// rows a per block of the density-fitted ladder for handles set up from now
+// on (0: the default, Gblk of at most 4 GB); a test hook
+int64_t g_df_block_rows = 0;
+
+void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df) {
+  naux = naux_df;
   Fia = &E.tensor("Fia", {o, v}, true);
   Fij = &E.tensor("Fij", {o, o}, true);
   Fab = &E.tensor("Fab", {v, v}, true);
@@ -39,7 +62,7 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v) {
   Giajb = &E.tensor("Giajb", {o, v, o, v}, true);
   Gijka = &E.tensor("Gijka", {o, o, o, v}, true);
   Giabc = &E.tensor("Giabc", {o, v, v, v}, true);
-  Gabcd = &E.tensor("Gabcd", {v, v, v, v}, true);
+  Gabcd = naux > 0 ? nullptr : &E.tensor("Gabcd", {v, v, v, v}, true);
   eps_o = &E.tensor("eps_o", {o}, true);
   eps_v = &E.tensor("eps_v", {v}, true);
   f_ai = &E.tensor("f_ai", {v, o}, true);
@@ -64,16 +87,47 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v) {
   W = &E.tensor("W", {o, o, o, o});
   tmp2 = &E.tensor("tmp2", {o, v, o, o});
   const int64_t np = v * (v + 1) / 2, nm = v * (v - 1) / 2, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
-  Gp = &E.tensor("Gp", {np, np}, true);
-  Gm = &E.tensor("Gm", {nm, nm}, true);
+  Gp = naux > 0 ? nullptr : &E.tensor("Gp", {np, np}, true);
+  Gm = naux > 0 ? nullptr : &E.tensor("Gm", {nm, nm}, true);
   Gip = &E.tensor("Gip", {o * v, np}, true);
   Gim = &E.tensor("Gim", {o * v, nm}, true);
   taup = &E.tensor("taup", {np, sp});
   taum = &E.tensor("taum", {nm, sm});
   Bp = &E.tensor("Bp", {np, sp});
-  Bm = &E.tensor("Bm", {nm, sm});
+  Bm = &E.tensor("Bm", {nm, std::max<int64_t>(sm, 1)});
   Xp = &E.tensor("Xp", {o * v, sp});
   Xm = &E.tensor("Xm", {o * v, sm});
+  if (naux > 0) {
+    Xai = &E.tensor("Xai", {naux, v, o}, true);
+    Xab = &E.tensor("Xab", {naux, v, v}, true);
+    Xac = &E.tensor("Xac", {v, v, naux});
+    // blocks of a: Gblk[a - a0][b][c][d] of at most ~4 GB
+    int64_t blk = std::max<int64_t>(1, std::min<int64_t>(v, (int64_t{1} << 29) / std::max<int64_t>(1, v * v * v)));
+    if (g_df_block_rows > 0) blk = std::min(v, g_df_block_rows);
+    const int64_t rows_p_max = pairs_before(blk, v), rows_m_max = std::max<int64_t>(1, anti_before(blk, v));
+    Tensor& gblk = E.tensor("df_gblk", {blk, v, v, v});
+    Tensor& gpb = E.tensor("df_gp", {rows_p_max, np});
+    Tensor& gmb = E.tensor("df_gm", {rows_m_max, std::max<int64_t>(nm, 1)});
+    df_blocks.clear();
+    for (int64_t a0 = 0; a0 < v; a0 += blk) {
+      auto b = std::make_unique<DfBlock>();
+      const int64_t a1 = std::min(v, a0 + blk), n = a1 - a0;
+      b->a0 = a0;
+      b->a1 = a1;
+      b->rows_p = pairs_before(a1, v) - pairs_before(a0, v);
+      b->rows_m = anti_before(a1, v) - anti_before(a0, v);
+      const std::string tag = "@" + std::to_string(a0);
+      b->xa = view("Xac" + tag, Xac->d + a0 * v * naux, {n, v, naux});
+      b->xb = view("Xac>" + tag, Xac->d + a0 * v * naux, {v - a0, v, naux});
+      b->g = view("df_gblk" + tag, gblk.d, {n, v - a0, v, v});
+      b->gp = view("df_gp" + tag, gpb.d, {b->rows_p, np});
+      b->gm = view("df_gm" + tag, gmb.d, {std::max<int64_t>(b->rows_m, 1), std::max<int64_t>(nm, 1)});
+      b->bp = view("Bp" + tag, Bp->d + pairs_before(a0, v) * sp, {b->rows_p, sp});
+      b->bm = view("Bm" + tag, Bm->d + anti_before(a0, v) * std::max<int64_t>(sm, 1),
+                   {std::max<int64_t>(b->rows_m, 1), std::max<int64_t>(sm, 1)});
+      df_blocks.push_back(std::move(b));
+    }
+  }
 }
 
 // f_ai(a,i) = Fia(i,a), g_abij(a,b,i,j) = Gijab(i,j,a,b)  (ccsd.h:325-330);
@@ -82,15 +136,23 @@ void setup_program(Engine& E, const CcsdTensors& S) {
   E.assign(ix(*S.f_ai, "ai"), 0.0, {f1(1.0, ix(*S.Fia, "ia"))});
   E.assign(ix(*S.g_abij, "abij"), 0.0, {f1(1.0, ix(*S.Gijab, "ijab"))});
   const int64_t v = S.t1->dim[0], o = S.t1->dim[1];
-  const double *Gabcd = S.Gabcd->d, *Giabc = S.Giabc->d;
-  double *Gp = S.Gp->d, *Gm = S.Gm->d, *Gip = S.Gip->d, *Gim = S.Gim->d;
-  E.custom([=](cudaStream_t st) { launch_build_gpm(v, v, true, Gabcd, Gp, Gm, st); }, 1);
+  if (S.naux > 0) {
+    // density fitting: Xac(a,c,K) = Xab(K,a,c); <ia|bc> = (ib|ac) = sum_K Xai(K,b,i) Xab(K,a,c)
+    E.assign(ix(*S.Xac, "acK"), 0.0, {f1(1.0, ix(*S.Xab, "Kac"))});
+    E.contract(ix(*S.Giabc, "iabc"), 0.0, 1.0, {{1.0, ix(*S.Xai, "Kbi")}}, {{1.0, ix(*S.Xab, "Kac")}}, kClassOther);
+  } else {
+    const double* Gabcd = S.Gabcd->d;
+    double *Gp = S.Gp->d, *Gm = S.Gm->d;
+    E.custom([=](cudaStream_t st) { launch_build_gpm(v, v, true, Gabcd, Gp, Gm, st); }, 1);
+  }
+  const double* Giabc = S.Giabc->d;
+  double *Gip = S.Gip->d, *Gim = S.Gim->d;
   E.custom([=](cudaStream_t st) { launch_build_gpm(o, v, false, Giabc, Gip, Gim, st); }, 1);
 }
 
 void residual_program(Engine& E, const CcsdTensors& S) {
   const Tensor &Fia = *S.Fia, &Fij = *S.Fij, &Fab = *S.Fab, &Gijab = *S.Gijab, &Gijkl = *S.Gijkl,
-               &Giajb = *S.Giajb, &Gijka = *S.Gijka, &Giabc = *S.Giabc, &Gabcd = *S.Gabcd;
+               &Giajb = *S.Giajb, &Gijka = *S.Gijka, &Giabc = *S.Giabc;
   const Tensor &t1 = *S.t1, &t2 = *S.t2, &tau = *S.tau;
   const Tensor &r1 = *S.r1, &r2 = *S.r2;
   const TermClass O = kClassOther, R = kClassRing, L = kClassLadder;
@@ -203,9 +265,32 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(W, "klij")}}, {{1.0, ix(tau, "abkl")}}, O);
   // particle-particle ladder (:275, :289): r2 += tau(c,d,i,j) Gabcd(a,b,c,d) as sums
   // over c <= d of the pair-(anti)symmetric combinations (taup / taum from above)
-  E.contract(ix(*S.Bp, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
-  if (minus) E.contract(ix(*S.Bm, "XZ"), 0.0, 1.0, {{1.0, ix(*S.Gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);
+  if (S.naux == 0) {
+    E.contract(ix(*S.Bp, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
+    if (minus) E.contract(ix(*S.Bm, "XZ"), 0.0, 1.0, {{1.0, ix(*S.Gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);
+  } else {
+    // density fitting, lazy (ab|cd) (the reference's direct-DF ladder,
+    // ccsd_r1_r2.h:497-508): per block of a, <ab|cd> = sum_K (K|ac)(K|bd) on
+    // the tensor cores, its G+- rows, and those rows of the pair products
+    for (const auto& bp : S.df_blocks) {
+      const CcsdTensors::DfBlock& B = *bp;
+      E.contract(ix(B.g, "abcd"), 0.0, 1.0, {{1.0, ix(B.xa, "acK")}}, {{1.0, ix(B.xb, "bdK")}}, L);
+      const int64_t a0 = B.a0, a1 = B.a1;
+      const double* gd = B.g.d;
+      double *gp = B.gp.d, *gm = B.gm.d;
+      E.custom([=](cudaStream_t st) { launch_build_gpm_rows(a0, a1, v, gd, gp, gm, st); }, 1);
+      E.contract(ix(B.bp, "PS"), 0.0, 1.0, {{1.0, ix(B.gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
+      if (minus && B.rows_m > 0)
+        E.contract(ix(B.bm, "XZ"), 0.0, 1.0, {{1.0, ix(B.gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);
+    }
+  }
   E.custom([=](cudaStream_t st) { launch_pair_unpack(v, v, o, true, Bp, minus ? Bm : nullptr, 1.0, r2d, st); }, 1);
 }
 
 }  // namespace gbcc
+
+extern "C" int gbcc_testing_df_block_rows(int64_t rows) {
+  if (rows < 0) return GBCC_ERR_INVALID_ARG;
+  gbcc::g_df_block_rows = rows;
+  return GBCC_OK;
+}

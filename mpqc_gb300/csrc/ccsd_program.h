@@ -1,6 +1,9 @@
 // The CCSD residual program and the device tensors it works on.
 #pragma once
 
+#include <memory>
+#include <vector>
+
 #include "engine.h"
 #include "kernels.h"
 
@@ -18,7 +21,20 @@ struct CcsdTensors {
   // Gabcd over (a <= b) x (c <= d) and of Giabc over (k a) x (c <= d)
   // (constants), tau+/tau- over (c <= d) x (i <= j), and the pair products
   Tensor *Gp, *Gm, *Gip, *Gim, *taup, *taum, *Bp, *Bm, *Xp, *Xm;
-  void create(Engine& E, int64_t o, int64_t v);
+  // density-fitted inputs (naux > 0): three-index factors in MPQC order
+  // Xai[K][a][i] = (K|ai), Xab[K][a][b] = (K|ab) instead of Giabc / Gabcd;
+  // Giabc is built from them on the device, (ab|cd) never exists whole: the
+  // ladder builds G+- rows one block of a at a time from Xac[a][c][K]
+  int64_t naux = 0;
+  Tensor *Xai = nullptr, *Xab = nullptr, *Xac = nullptr;
+  struct DfBlock {
+    int64_t a0, a1, rows_p, rows_m;
+    // views: Xac rows a of the block, Xac rows b >= a0, Gblk[a - a0][b - a0][c][d],
+    // its G+- rows and the B+- rows of the block
+    Tensor xa, xb, g, gp, gm, bp, bm;
+  };
+  std::vector<std::unique_ptr<DfBlock>> df_blocks;
+  void create(Engine& E, int64_t o, int64_t v, int64_t naux_df = 0);
 };
 
 void setup_program(Engine& E, const CcsdTensors& S);

@@ -569,6 +569,32 @@ __global__ void __launch_bounds__(kThreads) build_gpm_kernel(int64_t rows_v, int
   }
 }
 
+// The rows a in [a0, a1) of G+ / G- (pairs a <= b / a < b), from the block
+// Gblk[a - a0][b - a0][c][d] = <ab|cd> (b >= a0 only); output rows counted
+// from the block's first pair: sym(a,b) - sym(a0,a0) and anti(a,b) - anti(a0,a0+1).
+__global__ void __launch_bounds__(kThreads) build_gpm_rows_kernel(int64_t a0, int64_t a1, int64_t v,
+                                                                  const double* __restrict__ Gblk,
+                                                                  double* __restrict__ Gp, double* __restrict__ Gm) {
+  const int64_t np = v * (v + 1) / 2, nm = v * (v - 1) / 2, w = v - a0;
+  const int64_t p0 = pair_sym(a0, a0, v), m0 = a0 * (v - 1) - a0 * (a0 - 1) / 2;
+  for (int64_t row = blockIdx.x; row < (a1 - a0) * w; row += gridDim.x) {
+    int64_t al, bl;
+    divmod32(row, w, al, bl);
+    const int64_t a = a0 + al, b = a0 + bl;
+    if (a > b) continue;
+    double* gp = Gp + (pair_sym(a, b, v) - p0) * np;
+    double* gm = a < b ? Gm + (pair_anti(a, b, v) - m0) * nm : nullptr;
+    const double* g = Gblk + row * v * v;
+    for (int64_t c = 0; c < v; ++c) {
+      for (int64_t d = c + threadIdx.x; d < v; d += blockDim.x) {
+        const double x = g[c * v + d], y = g[d * v + c];
+        gp[pair_sym(c, d, v)] = c < d ? x + y : x;
+        if (gm && c < d) gm[pair_anti(c, d, v)] = x - y;
+      }
+    }
+  }
+}
+
 // One block per (c <= d): taup[sym(c,d)][sym(i,j)], taum[anti(c,d)][anti(i,j)].
 __global__ void __launch_bounds__(kThreads) tau_pm_kernel(int64_t o, int64_t v, const double* __restrict__ tau,
                                                           double* __restrict__ taup, double* __restrict__ taum) {
@@ -1099,6 +1125,12 @@ void launch_make_tau(int64_t o, int64_t v, const double* t1, const double* t2, d
 void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G, double* Gp, double* Gm,
                       cudaStream_t st) {
   build_gpm_kernel<<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, ab_pairs, G, Gp, Gm);
+}
+
+void launch_build_gpm_rows(int64_t a0, int64_t a1, int64_t v, const double* Gblk, double* Gp, double* Gm,
+                           cudaStream_t st) {
+  if (a1 <= a0) return;
+  build_gpm_rows_kernel<<<grid_for((a1 - a0) * (v - a0), 1), kThreads, 0, st>>>(a0, a1, v, Gblk, Gp, Gm);
 }
 
 void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double* taum, cudaStream_t st) {

@@ -213,6 +213,10 @@ void launch_energy_terms(int64_t o, int64_t v, const double* r1, const double* r
 // out(row, i, j) = beta out + B+ +- B- unpacked from the pair products (beta 0 or 1).
 void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G, double* Gp, double* Gm,
                       cudaStream_t st);
+// rows a in [a0, a1) of G+ / G- from Gblk[a - a0][b][c][d], rows counted from
+// the block's first pair (the density-fitted ladder builds G+- block by block)
+void launch_build_gpm_rows(int64_t a0, int64_t a1, int64_t v, const double* Gblk, double* Gp, double* Gm,
+                           cudaStream_t st);
 void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double* taum, cudaStream_t st);
 void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, const double* Bp, const double* Bm,
                         double beta, double* out, cudaStream_t st);

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
     for header in ("gbcc.h", "gbcc_scf.h", "gbcc_testing.h"):
         for name in declared_symbols(header):
             assert hasattr(lib, name), name
-    assert lib.gbcc_abi_version() == 4
+    assert lib.gbcc_abi_version() == 5
 
 
 def test_defaults_follow_the_reference(lib):
