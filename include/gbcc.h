@@ -130,6 +130,28 @@ typedef struct gbcc_df_inputs {
   const double* Xab;     /* [naux][v][v] = (K|ab)  (MPQC's Xab("K,a,b")) */
 } gbcc_df_inputs;
 
+/* Integral-direct inputs (the reference's method "direct",
+ * ccsd.h:581-603 and ccsd_r1_r2.h:116-118, 282-286): the MO blocks without
+ * Gabcd, plus the AO integrals and the MO coefficients.  The ladder then runs
+ * in the AO basis, u(p,r,i,j) = sum_qs (pq|rs) tau_AO(q,s,i,j) with
+ * tau_AO = Ca tau Ca^T, and u replaces the (ab|cd) and the Giabc-tau terms. */
+typedef struct gbcc_direct_inputs {
+  const double* eps_o;   /* [o] */
+  const double* eps_v;   /* [v] */
+  const double* Fia;     /* [o][v] */
+  const double* Fij;     /* [o][o] */
+  const double* Fab;     /* [v][v] */
+  const double* Gijab;   /* [o][o][v][v] */
+  const double* Gijkl;   /* [o][o][o][o] */
+  const double* Giajb;   /* [o][v][o][v] */
+  const double* Gijka;   /* [o][o][o][v] */
+  const double* Giabc;   /* [o][v][v][v] (the ring and T1 terms still read it) */
+  int64_t nao;           /* atomic orbitals                                   */
+  const double* Gao;     /* [nao][nao][nao][nao] = (pq|rs), chemists' order   */
+  const double* Ca;      /* [nao][v] virtual MO coefficients                  */
+  const double* Ci;      /* [nao][o] active occupied MO coefficients          */
+} gbcc_direct_inputs;
+
 typedef struct gbcc_report {
   int32_t iters;            /* residual evaluations performed                     */
   int32_t converged;        /* 1 if the convergence test of cc/solvers.h:150 held */
@@ -169,6 +191,12 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in);
  * gbcc_set_inputs rejects this call (GBCC_ERR_STATE) and vice versa, as does
  * a later call with another naux. */
 gbcc_status gbcc_set_df_inputs(gbcc_handle* h, const gbcc_df_inputs* in);
+
+/* Integral-direct alternative to gbcc_set_inputs (host or device pointers):
+ * the handle evaluates the residual with the U intermediate of the
+ * reference's direct method and never holds an MO (ab|cd) array.  The same
+ * rule fixes the handle's kind as for gbcc_set_df_inputs. */
+gbcc_status gbcc_set_direct_inputs(gbcc_handle* h, const gbcc_direct_inputs* in);
 
 /* Zero-copy alternative to gbcc_set_inputs for integrals too large to hold
  * twice in device memory (the v^4 (ab|cd) block is 84 GB at v = 320):

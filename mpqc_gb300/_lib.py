@@ -26,7 +26,7 @@ EXPORTS = (
     "gbcc_set_inputs", "gbcc_device_inputs", "gbcc_commit_inputs", "gbcc_residual",
     "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error", "gbcc_set_amplitudes",
-    "gbcc_save_amplitudes", "gbcc_load_amplitudes", "gbcc_set_df_inputs",
+    "gbcc_save_amplitudes", "gbcc_load_amplitudes", "gbcc_set_df_inputs", "gbcc_set_direct_inputs",
 )
 # every symbol include/gbcc_scf.h declares
 SCF_EXPORTS = (
@@ -63,6 +63,12 @@ class Inputs(C.Structure):
 class DfInputs(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("eps_o", "eps_v", "Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka")] + \
         [("naux", C.c_int64), ("Xai", C.c_void_p), ("Xab", C.c_void_p)]
+
+
+class DirectInputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("eps_o", "eps_v", "Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka",
+                                         "Giabc")] + \
+        [("nao", C.c_int64), ("Gao", C.c_void_p), ("Ca", C.c_void_p), ("Ci", C.c_void_p)]
 
 
 class Report(C.Structure):
@@ -175,6 +181,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_slice_policy.argtypes = [vp, vp, vp]
     lib.gbcc_last_error.restype = C.c_char_p
     lib.gbcc_last_error.argtypes = [vp]
+    lib.gbcc_set_direct_inputs.restype = C.c_int
+    lib.gbcc_set_direct_inputs.argtypes = [vp, C.POINTER(DirectInputs)]
     lib.gbcc_set_df_inputs.restype = C.c_int
     lib.gbcc_set_df_inputs.argtypes = [vp, C.POINTER(DfInputs)]
     lib.gbcc_testing_df_block_rows.restype = C.c_int

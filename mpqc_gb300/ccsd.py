@@ -151,6 +151,25 @@ class Solver:
         _check(self.lib, self.h, self.lib.gbcc_set_df_inputs(self.h, C.byref(inp)))
         self._keep = None
 
+    def set_direct_inputs(self, eps_o, eps_v, Gao, Ca, Ci, **ints):
+        """Integral-direct inputs (the reference's method "direct"): Fia, Fij,
+        Fab, Gijab, Gijkl, Giajb, Gijka, Giabc plus the AO integrals
+        Gao[p,q,r,s] = (pq|rs) and the MO coefficients Ca[p,a], Ci[p,k]; no
+        (ab|cd) array."""
+        names = ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc")
+        missing = [n for n in names if n not in ints]
+        if missing:
+            raise InputError(f"missing integrals: {missing}")
+        inp = L.DirectInputs()
+        inp.eps_o, inp.eps_v = _ptr(eps_o), _ptr(eps_v)
+        for n in names:
+            setattr(inp, n, _ptr(ints[n]))
+        inp.nao = int(Gao.shape[0])
+        inp.Gao, inp.Ca, inp.Ci = _ptr(Gao), _ptr(Ca), _ptr(Ci)
+        self._keep = (eps_o, eps_v, Gao, Ca, Ci, ints)
+        _check(self.lib, self.h, self.lib.gbcc_set_direct_inputs(self.h, C.byref(inp)))
+        self._keep = None
+
     def device_inputs(self):
         """Device pointers (ints) of the handle's own input arrays, to be filled
         on the device before ``commit_inputs()`` (zero-copy set-up)."""

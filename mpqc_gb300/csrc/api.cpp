@@ -684,7 +684,8 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
     const int64_t o = h->cfg.o, v = h->cfg.v;
     validate_eps(in->eps_o, in->eps_v, o, v);
     if (!h->S.t1) h->S.create(*h->eng, o, v);
-    if (h->S.naux > 0) throw Error(GBCC_ERR_STATE, "gbcc_set_inputs: the handle holds density-fitted inputs");
+    if (h->S.naux > 0 || h->S.nao > 0)
+      throw Error(GBCC_ERR_STATE, "gbcc_set_inputs: the handle holds density-fitted or integral-direct inputs");
     gbcc::CcsdTensors& S = h->S;
     h->inputs_set = false;
     h->have_solution = false;
@@ -717,6 +718,7 @@ gbcc_status gbcc_set_df_inputs(gbcc_handle* h, const gbcc_df_inputs* in) {
     const int64_t o = h->cfg.o, v = h->cfg.v, nq = in->naux;
     validate_eps(in->eps_o, in->eps_v, o, v);
     if (!h->S.t1) h->S.create(*h->eng, o, v, nq);
+    if (h->S.nao > 0) throw Error(GBCC_ERR_STATE, "gbcc_set_df_inputs: the handle holds integral-direct inputs");
     if (h->S.naux != nq)
       throw Error(GBCC_ERR_STATE, h->S.naux == 0 ? "gbcc_set_df_inputs: the handle holds standard inputs"
                                                  : "gbcc_set_df_inputs: the handle was set up for another naux");
@@ -740,11 +742,49 @@ gbcc_status gbcc_set_df_inputs(gbcc_handle* h, const gbcc_df_inputs* in) {
   });
 }
 
+gbcc_status gbcc_set_direct_inputs(gbcc_handle* h, const gbcc_direct_inputs* in) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!in) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_direct_inputs: NULL inputs");
+    const double* ptrs[] = {in->eps_o, in->eps_v, in->Fia, in->Fij, in->Fab, in->Gijab, in->Gijkl,
+                            in->Giajb, in->Gijka, in->Giabc, in->Gao, in->Ca, in->Ci};
+    for (const double* p : ptrs)
+      if (!p) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_direct_inputs: NULL input array");
+    const int64_t o = h->cfg.o, v = h->cfg.v, n = in->nao;
+    if (n < 1 || n > 1024) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_direct_inputs: nao must be 1..1024");
+    validate_eps(in->eps_o, in->eps_v, o, v);
+    if (!h->S.t1) h->S.create(*h->eng, o, v, 0, n);
+    if (h->S.naux > 0) throw Error(GBCC_ERR_STATE, "gbcc_set_direct_inputs: the handle holds density-fitted inputs");
+    if (h->S.nao != n)
+      throw Error(GBCC_ERR_STATE, h->S.nao == 0 ? "gbcc_set_direct_inputs: the handle holds standard inputs"
+                                                : "gbcc_set_direct_inputs: the handle was set up for another nao");
+    gbcc::CcsdTensors& S = h->S;
+    h->inputs_set = false;
+    h->have_solution = false;
+    h->seeded = false;
+    copy_in(S.eps_o->d, in->eps_o, o, h->stream);
+    copy_in(S.eps_v->d, in->eps_v, v, h->stream);
+    copy_in(S.Fia->d, in->Fia, o * v, h->stream);
+    copy_in(S.Fij->d, in->Fij, o * o, h->stream);
+    copy_in(S.Fab->d, in->Fab, v * v, h->stream);
+    copy_in(S.Gijab->d, in->Gijab, o * o * v * v, h->stream);
+    copy_in(S.Gijkl->d, in->Gijkl, o * o * o * o, h->stream);
+    copy_in(S.Giajb->d, in->Giajb, o * v * o * v, h->stream);
+    copy_in(S.Gijka->d, in->Gijka, o * o * o * v, h->stream);
+    copy_in(S.Giabc->d, in->Giabc, o * v * v * v, h->stream);
+    copy_in(S.Gao->d, in->Gao, n * n * n * n, h->stream);
+    copy_in(S.Ca->d, in->Ca, n * v, h->stream);
+    copy_in(S.Ci->d, in->Ci, n * o, h->stream);
+    commit_inputs(h);
+    return GBCC_OK;
+  });
+}
+
 gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out) {
   return guarded(h, [&]() -> gbcc_status {
     if (!out) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_device_inputs: NULL output");
     if (!h->S.t1) h->S.create(*h->eng, h->cfg.o, h->cfg.v);
-    if (h->S.naux > 0) throw Error(GBCC_ERR_STATE, "gbcc_device_inputs: the handle holds density-fitted inputs");
+    if (h->S.naux > 0 || h->S.nao > 0)
+      throw Error(GBCC_ERR_STATE, "gbcc_device_inputs: the handle holds density-fitted or integral-direct inputs");
     GBCC_CK(cudaStreamSynchronize(h->stream));  // zero-initialisation done
     const gbcc::CcsdTensors& S = h->S;
     out->eps_o = S.eps_o->d;

@@ -52,8 +52,10 @@ int64_t anti_before(int64_t a, int64_t v) { return a * (v - 1) - a * (a - 1) / 2
 // on (0: the default, Gblk of at most 4 GB); a test hook
 int64_t g_df_block_rows = 0;
 
-void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df) {
+void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df, int64_t nao_direct) {
   naux = naux_df;
+  nao = nao_direct;
+  const bool mo_ladder = naux == 0 && nao == 0;
   Fia = &E.tensor("Fia", {o, v}, true);
   Fij = &E.tensor("Fij", {o, o}, true);
   Fab = &E.tensor("Fab", {v, v}, true);
@@ -62,7 +64,7 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df) {
   Giajb = &E.tensor("Giajb", {o, v, o, v}, true);
   Gijka = &E.tensor("Gijka", {o, o, o, v}, true);
   Giabc = &E.tensor("Giabc", {o, v, v, v}, true);
-  Gabcd = naux > 0 ? nullptr : &E.tensor("Gabcd", {v, v, v, v}, true);
+  Gabcd = mo_ladder ? &E.tensor("Gabcd", {v, v, v, v}, true) : nullptr;
   eps_o = &E.tensor("eps_o", {o}, true);
   eps_v = &E.tensor("eps_v", {v}, true);
   f_ai = &E.tensor("f_ai", {v, o}, true);
@@ -87,8 +89,27 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df) {
   W = &E.tensor("W", {o, o, o, o});
   tmp2 = &E.tensor("tmp2", {o, v, o, o});
   const int64_t np = v * (v + 1) / 2, nm = v * (v - 1) / 2, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
-  Gp = naux > 0 ? nullptr : &E.tensor("Gp", {np, np}, true);
-  Gm = naux > 0 ? nullptr : &E.tensor("Gm", {nm, nm}, true);
+  Gp = mo_ladder ? &E.tensor("Gp", {np, np}, true) : nullptr;
+  Gm = mo_ladder ? &E.tensor("Gm", {nm, nm}, true) : nullptr;
+  if (nao > 0) {
+    // the AO ladder replaces both MO pair ladders (G+- of Gabcd and of Giabc)
+    const int64_t n = nao, npa = n * (n + 1) / 2, nma = n * (n - 1) / 2;
+    Gao = &E.tensor("Gao", {n, n, n, n}, true);
+    Ca = &E.tensor("Ca", {n, v}, true);
+    Ci = &E.tensor("Ci", {n, o}, true);
+    Gpao = &E.tensor("Gpao", {npa, npa}, true);
+    Gmao = &E.tensor("Gmao", {nma, nma}, true);
+    Xq = &E.tensor("Xq", {n, v, o, o});
+    tauao = &E.tensor("tauao", {n, n, o, o});
+    tauaop = &E.tensor("tauaop", {npa, sp});
+    tauaom = &E.tensor("tauaom", {nma, sm});
+    Bpao = &E.tensor("Bpao", {npa, sp});
+    Bmao = &E.tensor("Bmao", {nma, sm});
+    u = &E.tensor("u", {n, n, o, o});
+    U1 = &E.tensor("U1", {v, n, o, o});
+    U2 = &E.tensor("U2", {o, n, o, o});
+    return;
+  }
   Gip = &E.tensor("Gip", {o * v, np}, true);
   Gim = &E.tensor("Gim", {o * v, nm}, true);
   taup = &E.tensor("taup", {np, sp});
@@ -136,6 +157,13 @@ void setup_program(Engine& E, const CcsdTensors& S) {
   E.assign(ix(*S.f_ai, "ai"), 0.0, {f1(1.0, ix(*S.Fia, "ia"))});
   E.assign(ix(*S.g_abij, "abij"), 0.0, {f1(1.0, ix(*S.Gijab, "ijab"))});
   const int64_t v = S.t1->dim[0], o = S.t1->dim[1];
+  if (S.nao > 0) {
+    const int64_t n = S.nao;
+    const double* Gao = S.Gao->d;
+    double *Gp = S.Gpao->d, *Gm = S.Gmao->d;
+    E.custom([=](cudaStream_t st) { launch_build_gpm_chem(n, Gao, Gp, Gm, st); }, 1);
+    return;
+  }
   if (S.naux > 0) {
     // density fitting: Xac(a,c,K) = Xab(K,a,c); <ia|bc> = (ib|ac) = sum_K Xai(K,b,i) Xab(K,a,c)
     E.assign(ix(*S.Xac, "acK"), 0.0, {f1(1.0, ix(*S.Xab, "Kac"))});
@@ -159,15 +187,39 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   const int64_t v = t1.dim[0], o = t1.dim[1];
   const bool minus = v > 1 && o > 1;  // otherwise the antisymmetric pair parts are empty
   const double* tau_d = tau.d;
-  double *taup = S.taup->d, *taum = S.taum->d, *Bp = S.Bp->d, *Bm = S.Bm->d, *Xp = S.Xp->d, *Xm = S.Xm->d;
   double *r1d = r1.d, *r2d = r2.d, *tmp2 = S.tmp2->d;
+  const bool direct = S.nao > 0;
 
-  // tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j) (ccsd_r1_r2.h:277) as sums over
-  // c <= d of the pair-(anti)symmetric combinations (kernels.cu), unpacked
-  E.custom([=](cudaStream_t st) { launch_tau_pm(o, v, tau_d, taup, taum, st); }, 1);
-  E.contract(ix(*S.Xp, "RS"), 0.0, 1.0, {{1.0, ix(*S.Gip, "RQ")}}, {{1.0, ix(*S.taup, "QS")}}, R);
-  if (minus) E.contract(ix(*S.Xm, "RZ"), 0.0, 1.0, {{1.0, ix(*S.Gim, "RY")}}, {{1.0, ix(*S.taum, "YZ")}}, R);
-  E.custom([=](cudaStream_t st) { launch_pair_unpack(o, v, o, false, Xp, minus ? Xm : nullptr, 0.0, tmp2, st); }, 1);
+  if (direct) {
+    // integral-direct (ccsd.h:581-603): tau_AO(q,s,i,j) = Ca(q,a) tau(a,b,i,j) Ca(s,b)
+    // and u(p,r,i,j) = (pq|rs) tau_AO(q,s,i,j) over AO pairs p <= r, q <= s
+    // (the pair-symmetric ladder of the standard method on the AO tensor);
+    // tmp2(k,a,i,j) = Ci(p,k) u(p,r,i,j) Ca(r,a) equals Giabc(k,a,c,d) tau(c,d,i,j)
+    const int64_t n = S.nao;
+    const bool minus_ao = n > 1 && o > 1;
+    const Tensor &Ca = *S.Ca, &Ci = *S.Ci, &u = *S.u;
+    E.contract(ix(*S.Xq, "qbij"), 0.0, 1.0, {{1.0, ix(Ca, "qa")}}, {{1.0, ix(tau, "abij")}}, O);
+    E.contract(ix(*S.tauao, "qsij"), 0.0, 1.0, {{1.0, ix(*S.Xq, "qbij")}}, {{1.0, ix(Ca, "sb")}}, O);
+    const double* tao = S.tauao->d;
+    double *tp = S.tauaop->d, *tm = S.tauaom->d, *bp = S.Bpao->d, *bm = S.Bmao->d, *ud = u.d;
+    E.custom([=](cudaStream_t st) { launch_tau_pm(o, n, tao, tp, tm, st); }, 1);
+    E.contract(ix(*S.Bpao, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gpao, "PQ")}}, {{1.0, ix(*S.tauaop, "QS")}}, L);
+    if (minus_ao)
+      E.contract(ix(*S.Bmao, "XZ"), 0.0, 1.0, {{1.0, ix(*S.Gmao, "XY")}}, {{1.0, ix(*S.tauaom, "YZ")}}, L);
+    E.custom([=](cudaStream_t st) { launch_pair_unpack(n, n, o, true, bp, minus_ao ? bm : nullptr, 0.0, ud, st); },
+             1);
+    E.contract(ix(*S.U2, "krij"), 0.0, 1.0, {{1.0, ix(Ci, "pk")}}, {{1.0, ix(u, "prij")}}, O);
+    E.contract(ix(*S.tmp2, "kaij"), 0.0, 1.0, {{1.0, ix(*S.U2, "krij")}}, {{1.0, ix(Ca, "ra")}}, O);
+  } else {
+    // tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j) (ccsd_r1_r2.h:277) as sums over
+    // c <= d of the pair-(anti)symmetric combinations (kernels.cu), unpacked
+    double *taup = S.taup->d, *taum = S.taum->d, *Xp = S.Xp->d, *Xm = S.Xm->d;
+    E.custom([=](cudaStream_t st) { launch_tau_pm(o, v, tau_d, taup, taum, st); }, 1);
+    E.contract(ix(*S.Xp, "RS"), 0.0, 1.0, {{1.0, ix(*S.Gip, "RQ")}}, {{1.0, ix(*S.taup, "QS")}}, R);
+    if (minus) E.contract(ix(*S.Xm, "RZ"), 0.0, 1.0, {{1.0, ix(*S.Gim, "RY")}}, {{1.0, ix(*S.taum, "YZ")}}, R);
+    E.custom([=](cudaStream_t st) { launch_pair_unpack(o, v, o, false, Xp, minus ? Xm : nullptr, 0.0, tmp2, st); },
+             1);
+  }
 
   // ----- R1 (ccsd_r1_r2.h:70-124) -----
   // r1(a,i) = Fia(i,a) - 2 (Fia(k,c) t1(c,i)) t1(a,k)
@@ -265,6 +317,14 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(W, "klij")}}, {{1.0, ix(tau, "abkl")}}, O);
   // particle-particle ladder (:275, :289): r2 += tau(c,d,i,j) Gabcd(a,b,c,d) as sums
   // over c <= d of the pair-(anti)symmetric combinations (taup / taum from above)
+  if (direct) {
+    // integral-direct (:282-286): r2 += Ca(p,a) u(p,r,i,j) Ca(r,b); the T1 parts
+    // (Ci u terms) are the tmp2 terms of r2u above
+    E.contract(ix(*S.U1, "arij"), 0.0, 1.0, {{1.0, ix(*S.Ca, "pa")}}, {{1.0, ix(*S.u, "prij")}}, O);
+    E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(*S.U1, "arij")}}, {{1.0, ix(*S.Ca, "rb")}}, O);
+    return;
+  }
+  double *Bp = S.Bp->d, *Bm = S.Bm->d;
   if (S.naux == 0) {
     E.contract(ix(*S.Bp, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
     if (minus) E.contract(ix(*S.Bm, "XZ"), 0.0, 1.0, {{1.0, ix(*S.Gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);

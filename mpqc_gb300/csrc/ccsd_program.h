@@ -34,7 +34,15 @@ struct CcsdTensors {
     Tensor xa, xb, g, gp, gm, bp, bm;
   };
   std::vector<std::unique_ptr<DfBlock>> df_blocks;
-  void create(Engine& E, int64_t o, int64_t v, int64_t naux_df = 0);
+  // integral-direct inputs (nao > 0, the reference's method "direct"): AO
+  // integrals (pq|rs) and MO coefficients instead of Gabcd.  The ladder runs
+  // in the AO basis, u(p,r,i,j) = sum_qs (pq|rs) tau_AO(q,s,i,j), and its MO
+  // images replace the (ab|cd) and the Giabc-tau terms
+  int64_t nao = 0;
+  Tensor *Gao = nullptr, *Ca = nullptr, *Ci = nullptr, *Gpao = nullptr, *Gmao = nullptr;
+  Tensor *Xq = nullptr, *tauao = nullptr, *tauaop = nullptr, *tauaom = nullptr, *Bpao = nullptr, *Bmao = nullptr;
+  Tensor *u = nullptr, *U1 = nullptr, *U2 = nullptr;
+  void create(Engine& E, int64_t o, int64_t v, int64_t naux_df = 0, int64_t nao_direct = 0);
 };
 
 void setup_program(Engine& E, const CcsdTensors& S);

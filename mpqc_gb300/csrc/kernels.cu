@@ -595,6 +595,30 @@ __global__ void __launch_bounds__(kThreads) build_gpm_rows_kernel(int64_t a0, in
   }
 }
 
+// G+ / G- over atomic-orbital pairs from (pq|rs) in chemists' order:
+// <pr|qs> = G[p][q][r][s], so Gp[sym(p,r)][sym(q,s)] = (pq|rs) + (ps|rq) and
+// Gm[anti(p,r)][anti(q,s)] = (pq|rs) - (ps|rq) (one block per p <= r).
+__global__ void __launch_bounds__(kThreads) build_gpm_chem_kernel(int64_t n, const double* __restrict__ G,
+                                                                  double* __restrict__ Gp, double* __restrict__ Gm) {
+  const int64_t np = n * (n + 1) / 2, nm = n * (n - 1) / 2;
+  for (int64_t row = blockIdx.x; row < n * n; row += gridDim.x) {
+    int64_t p, r;
+    divmod32(row, n, p, r);
+    if (p > r) continue;
+    double* gp = Gp + pair_sym(p, r, n) * np;
+    double* gm = p < r ? Gm + pair_anti(p, r, n) * nm : nullptr;
+    for (int64_t q = 0; q < n; ++q) {
+      const double* gq = G + ((p * n + q) * n + r) * n;  // (pq|r .)
+      for (int64_t s = q + threadIdx.x; s < n; s += blockDim.x) {
+        const double x = gq[s];                            // <pr|qs> = (pq|rs)
+        const double y = G[((p * n + s) * n + r) * n + q];  // <pr|sq> = (ps|rq)
+        gp[pair_sym(q, s, n)] = q < s ? x + y : x;
+        if (gm && q < s) gm[pair_anti(q, s, n)] = x - y;
+      }
+    }
+  }
+}
+
 // One block per (c <= d): taup[sym(c,d)][sym(i,j)], taum[anti(c,d)][anti(i,j)].
 __global__ void __launch_bounds__(kThreads) tau_pm_kernel(int64_t o, int64_t v, const double* __restrict__ tau,
                                                           double* __restrict__ taup, double* __restrict__ taum) {
@@ -1125,6 +1149,10 @@ void launch_make_tau(int64_t o, int64_t v, const double* t1, const double* t2, d
 void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G, double* Gp, double* Gm,
                       cudaStream_t st) {
   build_gpm_kernel<<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, ab_pairs, G, Gp, Gm);
+}
+
+void launch_build_gpm_chem(int64_t n, const double* G, double* Gp, double* Gm, cudaStream_t st) {
+  build_gpm_chem_kernel<<<grid_for(n * n, 1), kThreads, 0, st>>>(n, G, Gp, Gm);
 }
 
 void launch_build_gpm_rows(int64_t a0, int64_t a1, int64_t v, const double* Gblk, double* Gp, double* Gm,

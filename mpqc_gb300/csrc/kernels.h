@@ -217,6 +217,8 @@ void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G,
 // the block's first pair (the density-fitted ladder builds G+- block by block)
 void launch_build_gpm_rows(int64_t a0, int64_t a1, int64_t v, const double* Gblk, double* Gp, double* Gm,
                            cudaStream_t st);
+// G+ / G- over n atomic-orbital pairs from G[p][q][r][s] = (pq|rs) (chemists' order)
+void launch_build_gpm_chem(int64_t n, const double* G, double* Gp, double* Gm, cudaStream_t st);
 void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double* taum, cudaStream_t st);
 void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, const double* Bp, const double* Bm,
                         double beta, double* out, cudaStream_t st);

@@ -106,6 +106,10 @@ class Integrals:
     Gabcd: np.ndarray
     FIJ: np.ndarray | None = None
     FAB: np.ndarray | None = None
+    # the integral-direct members (method "direct"): MO coefficients of the
+    # active occupied and the virtual orbitals, Ci[p,k] and Ca[p,a]
+    Ci: np.ndarray | None = None
+    Ca: np.ndarray | None = None
 
     @property
     def o(self):
@@ -121,8 +125,17 @@ def make_tau(t1, t2):
     return t2 + _es("ai,bj->abij", t1, t1)
 
 
-def compute_cs_ccsd_r1(t1, t2, tau, ints: Integrals):
-    """ccsd_r1_r2.h:70-124 (standard branch, no U).  Writes ints.FAB / ints.FIJ."""
+def compute_u2_u11(t1, t2, ints: Integrals, G_ao):
+    """ccsd.h:580-603: U(p,r,i,j) = (t2(a,b,i,j) Ca(q,a) Ca(s,b) + tc(i,q) tc(j,s)) (p q|r s)
+    with tc(i,q) = Ca(q,c) t1(c,i) and G_ao[p,q,r,s] = (pq|rs) over atomic orbitals."""
+    tc = _es("qc,ci->iq", ints.Ca, t1)
+    tau_ao = _es("abij,qa,sb->qsij", t2, ints.Ca, ints.Ca) + _es("iq,js->qsij", tc, tc)
+    return _es("pqrs,qsij->prij", G_ao, tau_ao)
+
+
+def compute_cs_ccsd_r1(t1, t2, tau, ints: Integrals, u=None):
+    """ccsd_r1_r2.h:70-124 (standard method; with u the integral-direct branch
+    of :116-118).  Writes ints.FAB / ints.FIJ."""
     r1 = ints.Fia.T - 2.0 * _es("ki,ak->ai", _es("kc,ci->ki", ints.Fia, t1), t1)      # :82-83
     g_ijab_bar = 2.0 * ints.Gijab - _es("jiab->ijab", ints.Gijab)                     # :86
     h_ac = F_vv(ints.Fab, g_ijab_bar, tau)                                            # :88
@@ -137,15 +150,19 @@ def compute_cs_ccsd_r1(t1, t2, tau, ints: Integrals):
     y = 2.0 * ints.Gijab - _es("kaic->kica", ints.Giajb)
     # 2 Gijab(k,i,c,a) - Giajb(k,a,i,c), laid out (k,i,c,a)
     r1 = r1 + _es("kica,ck->ai", y, t1)                                               # :106-107
-    g_iabc_bar = 2.0 * ints.Giabc - _es("kadc->kacd", ints.Giabc)                     # :111-112
-    r1 = r1 + _es("kacd,cdki->ai", g_iabc_bar, tau)                                   # :113
+    if u is None:
+        g_iabc_bar = 2.0 * ints.Giabc - _es("kadc->kacd", ints.Giabc)                 # :111-112
+        r1 = r1 + _es("kacd,cdki->ai", g_iabc_bar, tau)                               # :113
+    else:
+        r1 = r1 + _es("prki,pk,ra->ai", 2.0 * u - _es("prik->prki", u), ints.Ci, ints.Ca)  # :116-118
     g_lkic = 2.0 * ints.Gijka - _es("klic->lkic", ints.Gijka)  # 2 Gijka(l,k,i,c) - Gijka(k,l,i,c)
     r1 = r1 - _es("lkic,cakl->ai", g_lkic, tau)                                       # :120-121
     return r1
 
 
-def compute_cs_ccsd_r2(t1, t2, tau, ints: Integrals):
-    """ccsd_r1_r2.h:198-293 (standard branch, no U).  Needs ints.FIJ/FAB from R1."""
+def compute_cs_ccsd_r2(t1, t2, tau, ints: Integrals, u=None):
+    """ccsd_r1_r2.h:198-293 (standard method; with u the integral-direct ladder
+    of :282-286).  Needs ints.FIJ/FAB from R1."""
     # permutation part, :206-212
     x = ints.Giabc - _es("kbic,ak->icab", ints.Giajb, t1)   # Giabc(i,c,a,b) - Giajb(k,b,i,c) t1(a,k)
     r2 = _es("icab,cj->abij", x, t1)
@@ -171,9 +188,9 @@ def compute_cs_ccsd_r2(t1, t2, tau, ints: Integrals):
               + _es("kadc,di->kaic", ints.Giabc, t1)
               - _es("kldc,dail->kaic", ints.Gijab, T))
     # ring apply, :251-256
-    u = 2.0 * j_akic - _es("kaic->akic", k_kaic)
+    jk = 2.0 * j_akic - _es("kaic->akic", k_kaic)
     w = 2.0 * t2 - _es("bckj->cbkj", t2)                 # 2 t2(c,b,k,j) - t2(b,c,k,j)
-    r2 = r2 + 0.5 * _es("akic,cbkj->abij", u, w)
+    r2 = r2 + 0.5 * _es("akic,cbkj->abij", jk, w)
     tmp = _es("kaic,cbjk->abij", k_kaic, t2)
     r2 = r2 - (0.5 * tmp + _es("baij->abij", tmp))
     # symmetrise and add Gijab(i,j,a,b), :259-262
@@ -183,6 +200,11 @@ def compute_cs_ccsd_r2(t1, t2, tau, ints: Integrals):
     a_klij = W_oooo(ints.Gijkl, ints.Gijka, ints.Gijab, tau, t1)
     r2 = r2 + _es("klij,abkl->abij", a_klij, tau)
     # particle-particle ladder, :272-280
+    if u is not None:                                                                 # :282-286
+        b_abij = (_es("prij,rb,pa->abij", u, ints.Ca, ints.Ca)
+                  - _es("rk,bk,prij,pa->abij", ints.Ci, t1, u, ints.Ca)
+                  - _es("prij,pk,rb,ak->abij", u, ints.Ci, ints.Ca, t1))
+        return r2 + b_abij
     b_abij = _es("cdij,abcd->abij", tau, ints.Gabcd)
     tmp2 = _es("kacd,cdij->kaij", ints.Giabc, tau)
     b_abij = b_abij - _es("kaji,bk->abij", tmp2, t1)
@@ -190,11 +212,14 @@ def compute_cs_ccsd_r2(t1, t2, tau, ints: Integrals):
     return r2 + b_abij
 
 
-def residual(t1, t2, ints: Integrals):
-    """One R1 then R2 evaluation (R1 first: it sets ints.FIJ/FAB read by R2)."""
+def residual(t1, t2, ints: Integrals, G_ao=None):
+    """One R1 then R2 evaluation (R1 first: it sets ints.FIJ/FAB read by R2).
+    With AO integrals G_ao (and ints.Ca / Ci) the integral-direct branches
+    (ccsd.h:581-603 U, ccsd_r1_r2.h:116-118, 282-286), as method "direct"."""
     tau = make_tau(t1, t2)
-    r1 = compute_cs_ccsd_r1(t1, t2, tau, ints)
-    r2 = compute_cs_ccsd_r2(t1, t2, tau, ints)
+    u = compute_u2_u11(t1, t2, ints, G_ao) if G_ao is not None else None
+    r1 = compute_cs_ccsd_r1(t1, t2, tau, ints, u)
+    r2 = compute_cs_ccsd_r2(t1, t2, tau, ints, u)
     return r1, r2
 
 

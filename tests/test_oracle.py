@@ -163,3 +163,25 @@ def _timed(fn, time):
     t0 = time.perf_counter()
     fn()
     return time.perf_counter() - t0
+
+
+def test_direct_branches_equal_the_standard_residual():
+    """The integral-direct branches of the oracle (U of ccsd.h:581-603 used at
+    ccsd_r1_r2.h:116-118, 282-286) are an exact rearrangement of the standard
+    residual when the MO blocks come from the same AO integrals."""
+    from oracle import molecule as M
+    from mpqc_gb300 import molecules
+    sym, xyz = molecules.water()
+    mol = M.Molecule(sym, molecules.to_bohr(xyz))
+    S, H, G = M.ao_integrals_c(mol, "6-31G")
+    scf = M.rhf(S, H, G, 5, mol.nuclear_repulsion())
+    blocks, eo, ev = M.mo_blocks(scf, G, 1)
+    o, v = len(eo), len(ev)
+    rng = np.random.default_rng(2)
+    t2 = rng.normal(0.0, 1e-2, (v, v, o, o))
+    t2 = 0.5 * (t2 + t2.transpose(1, 0, 3, 2))
+    t1 = rng.normal(0.0, 1e-2, (v, o))
+    r1, r2 = R.residual(t1, t2, R.Integrals(**blocks))
+    ints = R.Integrals(**blocks, Ci=scf.C[:, 1:5], Ca=scf.C[:, 5:])
+    d1, d2 = R.residual(t1, t2, ints, G_ao=G)
+    assert rel_err(d1, r1) < 1e-13 and rel_err(d2, r2) < 1e-13
