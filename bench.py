@@ -23,6 +23,7 @@ Reported (one JSON line):
 CPU path; the reference itself cannot be built here) the same way, on the
 same workload and config as this arm.
 --config h2o10 runs (H2O)10 / cc-pVDZ from the geometry (mixed and FP64 solves).
+--config batch64 solves 64 water clusters (H2O)1..6 together (clusters/s).
 Multi-GPU (torchrun): every rank runs an independent replica ("replicas only",
 weak scaling); value = sum of all ranks' FLOPs / max rank time.
 """
@@ -552,6 +553,85 @@ def molecule_report(args):
     return 0
 
 
+def batch_clusters(count, seed):
+    """(waters, geometry seed) of each cluster of the batched workload: sizes
+    drawn uniformly from 1..6 by the seed, geometries by
+    molecules.water_cluster (cube-corner and face-centre sites, random
+    orientations, no close contacts)."""
+    rng = np.random.default_rng(seed)
+    return [(int(n), seed * 1000 + k) for k, n in enumerate(rng.integers(1, 7, size=count))]
+
+
+def batch_report(args):
+    """Batched many-instance CCSD: `--clusters` water clusters (H2O)n, n in
+    1..6, in a polarised Pople basis, every cluster's RHF and MO integrals
+    built on the GPU, then all mixed-precision solves (split-BF16 bulk
+    contractions, FP64 denominators, DIIS, FP64 refinement; each stopping at
+    its own convergence test) in flight together through gbcc_solve_batch.
+    Reports clusters/s of the batch (wall clock of the whole batch per step,
+    from t = 0 each step) against the same clusters solved one after another,
+    and each cluster's |dE_corr| against its plain-FP64 GPU solve (converged
+    to 1e-10)."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    from mpqc_gb300 import build as gb
+    gb.build()
+    from mpqc_gb300 import RHF, Solver, molecules, solve_batch
+    specs = batch_clusters(args.clusters, args.seed)
+    t0 = time.perf_counter()
+    handles, ref, info = [], [], []
+    for n, seed in specs:
+        sym, xyz = molecules.water_cluster(n, seed=seed)
+        with RHF(sym, xyz, args.batch_basis, threshold=1e-11, max_iter=60) as scf:
+            e_scf = scf.run()
+            o = scf.nocc()
+            v = scf.nbf - o
+            s = Solver(o, v, precision="mixed", target_precision=args.solve_precision, max_iter=args.max_iter,
+                       refine_iters=2, autotune=False)
+            scf.ccsd_inputs(s)
+            handles.append(s)
+            # the plain-FP64 energy of the same MO integrals, tightly converged
+            with Solver(o, v, precision="fp64", target_precision=1e-10, max_iter=args.max_iter) as f:
+                scf.ccsd_inputs(f)
+                ef, _, _, rf = f.solve(want_amplitudes=False)
+                ref.append((ef, rf))
+        info.append({"waters": n, "seed": seed, "nbf": o + v, "o": o, "v": v, "e_rhf": e_scf})
+    prep_s = time.perf_counter() - t0
+    log(f"[batch] {len(specs)} clusters, basis {args.batch_basis}, nbf {min(i['nbf'] for i in info)}.."
+        f"{max(i['nbf'] for i in info)}: SCF + MO integrals + FP64 solves + handle set-up {prep_s:.1f} s")
+    for _ in range(max(1, args.warmup)):  # the first solve of a handle captures its solve graph
+        solve_batch(handles)
+    walls, res = [], None
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        res = solve_batch(handles)
+        walls.append(time.perf_counter() - t1)
+    t1 = time.perf_counter()
+    seq = [s.solve(want_amplitudes=False) for s in handles]
+    seq_s = time.perf_counter() - t1
+    for s in handles:
+        s.close()
+    wall = float(np.median(walls))
+    dE = [abs(e - ef) for (e, _), (ef, _) in zip(res, ref)]
+    iters = [r.iters for _, r in res]
+    line = {"workload": f"{len(specs)} water clusters (H2O)n, n in 1..6 from seed {args.seed}, "
+                        f"{args.batch_basis}, mixed-precision CCSD to {args.solve_precision:g}",
+            "metric": "clusters/s (whole batch, from t = 0)", "value": len(specs) / wall, "unit": "clusters/s",
+            "steps": len(walls), "ms_per_step": wall * 1e3,
+            "sequential_clusters_per_s": len(specs) / seq_s, "batch_speedup_vs_sequential": seq_s / wall,
+            "prep_s": prep_s, "all_converged": all(r.converged for _, r in res) and all(r.converged for _, r in ref),
+            "iters_min_max": [min(iters), max(iters)],
+            "max_abs_dE_mixed_vs_fp64": max(dE), "median_abs_dE_mixed_vs_fp64": float(np.median(dE)),
+            "sequential_max_abs_dE_vs_batch": max(abs(a[0] - b[0]) for a, b in zip(seq, res)),
+            "nbf_min_max": [min(i["nbf"] for i in info), max(i["nbf"] for i in info)],
+            "clusters": [dict(i, e_corr=e, e_corr_fp64=ef, abs_dE=d, iters=r.iters)
+                         for i, (e, r), (ef, _), d in zip(info, res, ref, dE)]}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def gemm_probe(args):
     """One GEMM shape C = A B^T on the library's kernels (profiling aid): seeded
     normal FP64 inputs through gbcc_testing_gemm_ex3 (split-BF16 tensor-core
@@ -628,10 +708,14 @@ def main():
     ap.add_argument("--gemm-repeat", type=int, default=5)
     ap.add_argument("--gemm-check", action="store_true",
                     help="also report max |C - A B^T| / max |A B^T| against numpy FP64")
-    ap.add_argument("--config", default="residual", choices=["residual", "h2o10"],
+    ap.add_argument("--config", default="residual", choices=["residual", "h2o10", "batch64"],
                     help="residual: the synthetic o=32 v=320 residual (default); h2o10: (H2O)10 / cc-pVDZ "
-                         "from the geometry, mixed and plain-FP64 solves against the oracle's energy")
+                         "from the geometry, mixed and plain-FP64 solves against the oracle's energy; "
+                         "batch64: 64 water clusters (H2O)1..6 solved together")
     ap.add_argument("--waters", type=int, default=10, help="--config h2o10: cluster size (default 10)")
+    ap.add_argument("--clusters", type=int, default=64, help="--config batch64: number of clusters")
+    ap.add_argument("--batch-basis", default="6-31G**",
+                    help="--config batch64: basis (6-31G** gives 25 AO per water; 6-31G* gives 19)")
     args = ap.parse_args()
     if args.gemm:
         return gemm_probe(args)
@@ -639,6 +723,8 @@ def main():
         if args.max_iter == 40 and args.solve_precision == 1e-8:
             args.solve_precision = 1e-9
         return molecule_report(args)
+    if args.config == "batch64":
+        return batch_report(args)
     if args.impl == "reference":
         return reference_arm(args)
     if args.solve:

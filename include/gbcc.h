@@ -254,6 +254,19 @@ gbcc_status gbcc_energy_noalloc(int64_t o, int64_t v, const double* f_ai, const 
 gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e_corr,
                        gbcc_report* report);
 
+/* Many independent solves at once (e.g. the clusters of a batch): gbcc_solve
+ * of every handle, each from its own host thread, so that all the solves --
+ * each one CUDA graph on its handle's stream, stopping by its own
+ * convergence test on the device -- are in flight on the GPU together.
+ * e_corr[k], reports[k] and statuses[k] (any of the arrays may be NULL)
+ * receive handle k's results and gbcc_solve status.  Returns the first
+ * failing status in handle order (its message in gbcc_last_error of that
+ * handle), else GBCC_ERR_NOT_CONVERGED if a solve hit max_iter, else GBCC_OK.
+ * A handle may appear once.  The reference solves one molecule at a time
+ * (ccsd.h:367-468); no counterpart. */
+gbcc_status gbcc_solve_batch(gbcc_handle* const* handles, int32_t count, double* e_corr, gbcc_report* reports,
+                             gbcc_status* statuses);
+
 /* Release the handle and all its device memory.  NULL is accepted. */
 gbcc_status gbcc_destroy(gbcc_handle* h);
 

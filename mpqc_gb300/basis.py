@@ -4,12 +4,16 @@ Libint2's basis library, src/mpqc/chemistry/qc/lcao/basis/basis.cpp:28,49).
 Published contraction tables, hydrogen and oxygen:
   6-31G    R. Ditchfield, W. J. Hehre, J. A. Pople, J. Chem. Phys. 54, 724 (1971);
            W. J. Hehre, R. Ditchfield, J. A. Pople, J. Chem. Phys. 56, 2257 (1972)
+  6-31G*   6-31G plus one Cartesian d shell on O (exponent 0.8), and
+  6-31G**  6-31G* plus one p shell on H (exponent 1.1): P. C. Hariharan,
+           J. A. Pople, Theor. Chim. Acta 28, 213 (1973)
   cc-pVDZ  T. H. Dunning, J. Chem. Phys. 90, 1007 (1989); spherical d shells
 Each shell is (l, [(exponent, coefficient of the normalised primitive), ...]);
 SP shells are listed as an S and a P shell with shared exponents.
 
-Other elements and basis sets are not provided: their tables could not be
-checked against a recorded energy of the reference.
+Other elements and basis sets are not provided.  6-31G and cc-pVDZ are pinned
+by the reference's recorded water energies; the polarised 6-31G sets have no
+recorded reference energy and are checked against the oracle's chain only.
 """
 from __future__ import annotations
 
@@ -48,9 +52,11 @@ BASIS_SETS = {
         ],
     },
 }
+BASIS_SETS["6-31G*"] = {"H": BASIS_SETS["6-31G"]["H"], "O": BASIS_SETS["6-31G"]["O"] + [(2, [(0.8, 1.0)])]}
+BASIS_SETS["6-31G**"] = {"H": BASIS_SETS["6-31G"]["H"] + [(1, [(1.1, 1.0)])], "O": BASIS_SETS["6-31G*"]["O"]}
 
-# spherical d functions in the Dunning sets, Cartesian otherwise
-PURE = {"6-31G": False, "cc-pVDZ": True}
+# spherical d functions in the Dunning sets, Cartesian (6D) in the Pople sets
+PURE = {"6-31G": False, "6-31G*": False, "6-31G**": False, "cc-pVDZ": True}
 
 NUCLEAR_CHARGE = {"H": 1, "O": 8}
 # core orbitals per atom frozen by frozen_core (first row: 1s), as

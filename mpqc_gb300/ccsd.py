@@ -281,6 +281,34 @@ class Solver:
         return e.value, t1, t2, r
 
 
+def _report(rep):
+    return Report(rep.iters, bool(rep.converged), rep.mixed_iters, rep.fp64_iters, rep.e_corr,
+                  rep.last_dE, rep.last_error, rep.seconds_total, rep.seconds_residual_mixed,
+                  rep.seconds_residual_fp64)
+
+
+def solve_batch(solvers):
+    """Solve several independent handles at once (``gbcc_solve_batch``): each
+    handle's solve runs on its own stream from its own host thread, so small
+    molecules fill the GPU together.  Returns ``[(e_corr, Report), ...]`` in
+    input order; the amplitudes stay on the device (``Solver.save_amplitudes``
+    reads them back)."""
+    solvers = list(solvers)
+    if not solvers:
+        return []
+    lib = solvers[0].lib
+    n = len(solvers)
+    hs = (C.c_void_p * n)(*[s.h for s in solvers])
+    e = (C.c_double * n)()
+    reps = (L.Report * n)()
+    sts = (C.c_int * n)()
+    st = lib.gbcc_solve_batch(hs, n, e, reps, sts)
+    if st not in (L.GBCC_OK, L.GBCC_ERR_NOT_CONVERGED):
+        bad = next((s for s, k in zip(solvers, sts) if k == st), None)
+        _check(lib, bad.h if bad else None, st)
+    return [(e[k], _report(reps[k])) for k in range(n)]
+
+
 def compute_cs_ccsd_r1_r2(t1, t2, ints, eps_o, eps_v, precision="fp64", **kw):
     """R1 and R2 of the standard closed-shell method (ccsd_r1_r2.h:70-124,
     198-293) for one amplitude set; ``ints`` maps the cc::Integrals names

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gbcc.h"
@@ -111,14 +112,22 @@ void copy_out(double* dst, const double* src, int64_t n, cudaStream_t st) {
   GBCC_CK(cudaMemcpyAsync(dst, src, static_cast<size_t>(n) * sizeof(double), cudaMemcpyDefault, st));
 }
 
+// Device-to-host read on the handle's own stream (not the legacy default
+// stream, which would serialise concurrent solves of other handles).
+void read_back(gbcc_handle* h, void* dst, const void* src, size_t bytes) {
+  GBCC_CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+  GBCC_CK(cudaStreamSynchronize(h->stream));
+}
+
 // Check the device error word and any pending CUDA error after a sync.
 void sync_check(gbcc_handle* h) {
   GBCC_CK(cudaStreamSynchronize(h->stream));
   GBCC_CK(cudaGetLastError());
   int err = 0;
-  GBCC_CK(cudaMemcpy(&err, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  read_back(h, &err, h->d_err, sizeof(int));
   if (err != gbcc::kDevOk) {
-    GBCC_CK(cudaMemset(h->d_err, 0, sizeof(int)));
+    GBCC_CK(cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    GBCC_CK(cudaStreamSynchronize(h->stream));
     throw Error(GBCC_ERR_TIMEOUT, "a bounded device-side wait gave up (tensor-core pipeline)");
   }
 }
@@ -920,15 +929,14 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
       GBCC_CK(cudaGraphLaunch(h->solve_exec, h->stream));
       sync_check(h);
       gbcc::SolveState ss{};
-      GBCC_CK(cudaMemcpy(&ss, h->d_state, sizeof(ss), cudaMemcpyDeviceToHost));
+      read_back(h, &ss, h->d_state, sizeof(ss));
       const int ntest = ss.iter + (ss.stop ? 1 : 0);
       std::vector<double> hist(3 * static_cast<size_t>(std::max(ntest, 1)));
       std::vector<unsigned long long> stamps(2 * static_cast<size_t>(std::max(ss.iter, 1)));
       if (ntest > 0)
-        GBCC_CK(cudaMemcpy(hist.data(), h->d_history, 3 * ntest * sizeof(double), cudaMemcpyDeviceToHost));
+        read_back(h, hist.data(), h->d_history, 3 * ntest * sizeof(double));
       if (ss.iter > 0)
-        GBCC_CK(cudaMemcpy(stamps.data(), h->d_stamps, 2 * ss.iter * sizeof(unsigned long long),
-                           cudaMemcpyDeviceToHost));
+        read_back(h, stamps.data(), h->d_stamps, 2 * ss.iter * sizeof(unsigned long long));
       if (ss.status) throw Error(GBCC_ERR_NUMERIC, "non-finite energy or residual at iteration " + std::to_string(ss.iter));
       for (int k = 0; k < ss.iter; ++k) {
         const double secs_k = static_cast<double>(stamps[2 * k + 1] - stamps[2 * k]) * 1e-9;
@@ -1072,6 +1080,38 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
     if (c.verbose) std::printf("CCSD Energy  %.15f\n", E1);
     return converged ? GBCC_OK : GBCC_ERR_NOT_CONVERGED;
   });
+}
+
+gbcc_status gbcc_solve_batch(gbcc_handle* const* handles, int32_t count, double* e_corr, gbcc_report* reports,
+                             gbcc_status* statuses) {
+  if (!handles || count < 0) return GBCC_ERR_INVALID_ARG;
+  for (int32_t k = 0; k < count; ++k)
+    if (!handles[k]) return GBCC_ERR_INVALID_ARG;
+  for (int32_t k = 0; k < count; ++k)
+    for (int32_t q = 0; q < k; ++q)
+      if (handles[q] == handles[k]) {
+        handles[k]->last_error = "gbcc_solve_batch: a handle appears twice";
+        return GBCC_ERR_INVALID_ARG;
+      }
+  std::vector<gbcc_status> st(count, GBCC_OK);
+  std::vector<gbcc_report> rep(count);
+  std::vector<double> e(count, 0.0);
+  std::vector<std::thread> threads;
+  threads.reserve(count);
+  for (int32_t k = 0; k < count; ++k)
+    threads.emplace_back([&, k] { st[k] = gbcc_solve(handles[k], nullptr, nullptr, &e[k], &rep[k]); });
+  for (auto& t : threads) t.join();
+  gbcc_status out = GBCC_OK;
+  for (int32_t k = 0; k < count; ++k) {
+    if (e_corr) e_corr[k] = e[k];
+    if (reports) reports[k] = rep[k];
+    if (statuses) statuses[k] = st[k];
+    if (st[k] != GBCC_OK && st[k] != GBCC_ERR_NOT_CONVERGED && (out == GBCC_OK || out == GBCC_ERR_NOT_CONVERGED))
+      out = st[k];
+    else if (st[k] == GBCC_ERR_NOT_CONVERGED && out == GBCC_OK)
+      out = GBCC_ERR_NOT_CONVERGED;
+  }
+  return out;
 }
 
 gbcc_status gbcc_destroy(gbcc_handle* h) {

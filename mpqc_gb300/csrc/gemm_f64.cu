@@ -318,6 +318,14 @@ void launch_smallk_tiles(const GemmF64Args& g, cudaStream_t st) {
     gemm_smallk_kernel<false, TM, TN><<<grid, 256, 0, st>>>(g);
 }
 
+// The stream kernels take at most 64 KB of dynamic shared memory; the limit
+// is raised once to that bound (not to each launch's size) so that launches
+// from concurrent solves never see another thread's smaller limit.
+template <typename K>
+bool allow_stream_smem(K kernel) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024) == cudaSuccess;
+}
+
 void launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return;
   const int64_t npad = (g.N + kStreamCols - 1) / kStreamCols * kStreamCols;
@@ -326,13 +334,16 @@ void launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st) {
     const int64_t mtiles = (g.M + 255) / 256;
     const unsigned grid = static_cast<unsigned>(std::min<int64_t>(mtiles, static_cast<int64_t>(num_sms()) * 3));
     if (g.beta == 0.0) {
-      cudaFuncSetAttribute(gemm_smallk_stream_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      static const bool attr0 = allow_stream_smem(gemm_smallk_stream_kernel<0>);
+      (void)attr0;
       gemm_smallk_stream_kernel<0><<<grid, 256, smem, st>>>(g);
     } else if (g.beta == 1.0) {
-      cudaFuncSetAttribute(gemm_smallk_stream_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      static const bool attr1 = allow_stream_smem(gemm_smallk_stream_kernel<1>);
+      (void)attr1;
       gemm_smallk_stream_kernel<1><<<grid, 256, smem, st>>>(g);
     } else {
-      cudaFuncSetAttribute(gemm_smallk_stream_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      static const bool attr2 = allow_stream_smem(gemm_smallk_stream_kernel<2>);
+      (void)attr2;
       gemm_smallk_stream_kernel<2><<<grid, 256, smem, st>>>(g);
     }
     return;

@@ -862,13 +862,12 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
   CUtensorMap ma, mb;
   if (!make_map(&ma, g.A, g.a_slices, g.a_rows ? g.a_rows : g.Mpad, g.Kpad, BM)) return false;
   if (!make_map(&mb, g.B, g.b_slices, g.b_rows ? g.b_rows : g.Npad, g.Kpad, Cfg::kBRows)) return false;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(gemm_tc_kernel<BN, CTA2, SPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             Cfg::kSmem) != cudaSuccess)
-      return false;
-    attr_set = true;
-  }
+  // once per instantiation; the initialisation of a function-local static is
+  // thread-safe, so concurrent solves (gbcc_solve_batch) may reach it together
+  static const bool attr_set = cudaFuncSetAttribute(gemm_tc_kernel<BN, CTA2, SPS>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    Cfg::kSmem) == cudaSuccess;
+  if (!attr_set) return false;
   const int64_t units = (g.Npad / BN) * (g.Mpad / (CTA2 ? 2 * BM : BM)) * (g.ksplit > 1 ? g.ksplit : 1);
   if (!CTA2) {
     const int grid = static_cast<int>(units < num_sms() ? units : num_sms());
@@ -886,16 +885,15 @@ bool launch_bn(const GemmTcArgs& g, cudaStream_t st) {
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  static int max_pairs = 0;
-  if (!max_pairs) {
+  static const int max_pairs = [&cfg] {
     cfg.gridDim = dim3(2 * (num_sms() / 2));
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, gemm_tc_kernel<BN, true, 1>, &cfg) != cudaSuccess || n < 1) {
       cudaGetLastError();
       n = num_sms() / 2;
     }
-    max_pairs = n;
-  }
+    return n;
+  }();
   const int64_t pairs = units < max_pairs ? units : max_pairs;
   cfg.gridDim = dim3(static_cast<unsigned>(2 * pairs));
   return cudaLaunchKernelEx(&cfg, gemm_tc_kernel<BN, true, 1>, ma, mb, g) == cudaSuccess;

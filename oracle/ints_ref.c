@@ -270,7 +270,7 @@ int eri_sph(int nshell, const int *l, const double *center, const int *nprim, co
     double Eab[3][LE + 1][LE + 1][2 * LE + 2], Ecd[3][LE + 1][LE + 1][2 * LE + 2];
     double R[LR + 1][LR + 1][LR + 1];
     static __thread double blk[6][6][6][6], W[LR + 1][LR + 1][LR + 1];
-    static __thread double sph[5][5][5][5], tmp[6][6][6][6];
+    static __thread double sph[6][6][6][6], tmp[6][6][6][6];
     int ca[6][3], cb[6][3], cc[6][3], cd[6][3];
     const shell_t *A = &sh[pa[ip]], *B = &sh[pb[ip]];
     comps(A->l, ca);

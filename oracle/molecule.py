@@ -80,6 +80,10 @@ BASIS_SETS = {
         ],
     },
 }
+# Pople polarisation shells (Hariharan & Pople 1973): Cartesian d on O
+# (exponent 0.8) for 6-31G*, plus p on H (exponent 1.1) for 6-31G**.
+BASIS_SETS["6-31G*"] = {"H": BASIS_SETS["6-31G"]["H"], "O": BASIS_SETS["6-31G"]["O"] + [(2, [(0.8, 1.0)])]}
+BASIS_SETS["6-31G**"] = {"H": BASIS_SETS["6-31G"]["H"] + [(1, [(1.1, 1.0)])], "O": BASIS_SETS["6-31G*"]["O"]}
 
 
 def cartesian_components(l):

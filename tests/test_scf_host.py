@@ -91,7 +91,7 @@ def test_scf_create_rejects_bad_input(lib):
 def test_basis_tables_match_the_oracle():
     from mpqc_gb300 import basis as B
     from oracle import molecule as M
-    for name in ("6-31G", "cc-pVDZ"):
+    for name in ("6-31G", "6-31G*", "6-31G**", "cc-pVDZ"):
         for el in ("H", "O"):
             assert B.BASIS_SETS[name][el] == M.BASIS_SETS[name][el], (name, el)
 
@@ -101,7 +101,9 @@ def test_c_integrals_match_the_python_oracle():
     from mpqc_gb300 import molecules
     sym, xyz = molecules.water()
     mol = M.Molecule(sym, molecules.to_bohr(xyz))
-    for basis in ("6-31G", "cc-pVDZ"):
+    # 6-31G* has Cartesian (6D) d shells: the C oracle's transform buffers
+    # must hold six functions per d shell, not five
+    for basis in ("6-31G", "6-31G*", "cc-pVDZ"):
         S, H, G = M.ao_integrals(mol, basis)
         S2, H2, G2 = M.ao_integrals_c(mol, basis)
         assert np.max(np.abs(S - S2)) < 1e-13
