@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define GBCC_ABI_VERSION 5
+#define GBCC_ABI_VERSION 6
 
 typedef enum gbcc_status {
   GBCC_OK = 0,
@@ -55,7 +55,11 @@ typedef enum gbcc_status {
 
 typedef enum gbcc_precision {
   GBCC_PREC_FP64 = 0,        /* every contraction in plain FP64                                */
-  GBCC_PREC_MIXED = 1        /* split-BF16 tensor-core contractions, FP64 elsewhere            */
+  GBCC_PREC_MIXED = 1,       /* split-BF16 tensor-core contractions, FP64 elsewhere            */
+  GBCC_PREC_FP64_TC = 2      /* FP64-grade contractions on the BF16 tensor cores: each operand */
+                             /* row in six 7-bit fixed-point slices under its largest         */
+                             /* exponent; slice products of one weight summed exactly in FP32,*/
+                             /* float-float across chunks (error ~2^-42 of row max x row max) */
 } gbcc_precision;
 
 typedef struct gbcc_config {
@@ -66,7 +70,7 @@ typedef struct gbcc_config {
                                /* 0, the default: chosen from the measured error, see below) */
   int32_t slices_ring;         /* ... o^3 v^3 ring terms and the ladder's T1 part (1..3)       */
   int32_t slices_other;        /* ... every remaining contraction (1..3)                       */
-  int32_t refine_iters;        /* plain-FP64 iterations after the mixed phase                  */
+  int32_t refine_iters;        /* FP64-grade iterations after the mixed phase                  */
   double mixed_switch_precision; /* mixed phase ends once converged to this precision;         */
                                /* 0 (default): target_precision                              */
   int32_t max_iter;            /* "max_iter", default 30 (ccsd.h:104)                          */
@@ -93,6 +97,8 @@ typedef struct gbcc_config {
                                /* the switch to FP64, so the refinement extrapolates with FP64 */
                                /* residuals only (DIISSolver::reset, cc/solvers.h:154-157,     */
                                /* "used when switching to a new solver subspace"); 0: keep it   */
+  int32_t refine_precision;    /* precision of the refinement iterations of a mixed handle:    */
+                               /* GBCC_PREC_FP64 (default, DFMA) or GBCC_PREC_FP64_TC          */
 } gbcc_config;
 
 typedef struct gbcc_inputs {
@@ -216,7 +222,10 @@ gbcc_status gbcc_commit_inputs(gbcc_handle* h);
 gbcc_status gbcc_residual(gbcc_handle* h, const double* t1_ai, const double* t2_abij,
                           double* r1_ai, double* r2_abij);
 
-/* As gbcc_residual with an explicit precision (gbcc_precision). */
+/* As gbcc_residual with an explicit precision (gbcc_precision).
+ * GBCC_PREC_FP64_TC needs a handle whose precision or refine_precision is
+ * GBCC_PREC_FP64_TC (its plan and slice packs are built with the inputs);
+ * otherwise GBCC_ERR_STATE. */
 gbcc_status gbcc_residual_ex(gbcc_handle* h, int32_t precision, const double* t1_ai,
                              const double* t2_abij, double* r1_ai, double* r2_abij);
 

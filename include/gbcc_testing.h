@@ -61,6 +61,24 @@ int gbcc_testing_gemm_ex3(int64_t M, int64_t N, int64_t K, const double* A, cons
  * DFMA loop over all SMs). */
 int gbcc_testing_fp64_peak(double* gflops);
 
+/* Fixed-point slices of a row-major [rows][cols] FP64 matrix as the
+ * FP64-grade contractions pack them (GBCC_PREC_FP64_TC): out[s][r][c], the
+ * BF16 bits of slice s (nslices <= 6), and rowexp[r], the row's largest
+ * biased FP64 exponent. */
+int gbcc_testing_fixed_split(const double* x, int64_t rows, int64_t cols, int nslices, uint16_t* out,
+                             uint32_t* rowexp);
+
+/* C[M][N] = A[M][K] B[N][K]^T through the FP64-grade tensor-core path: six
+ * fixed-point slices per operand row, one tcgen05 launch per weight class
+ * (bn 0: the heuristic tile width; 32, 64 or 128), K split over CTAs when
+ * ksplit > 1.  *ms: the time of one product (all class launches). */
+int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+                             int bn, int ksplit, int repeat, float* ms);
+
+/* Peak probe: FP64 tensor-core throughput (mma.sync m8n8k4 .f64, DMMA) in
+ * GFLOP/s, register operands over all SMs. */
+int gbcc_testing_dmma_peak(double* gflops);
+
 /* Rows a per block of the density-fitted ladder for handles whose inputs are
  * set from now on (0: the default size, a block of (ab|cd) of at most 4 GB). */
 int gbcc_testing_df_block_rows(int64_t rows);

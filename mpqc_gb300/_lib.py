@@ -19,6 +19,7 @@ GBCC_ERR_NUMERIC = 7
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_FP64_TC = 2
 
 # every symbol include/gbcc.h declares
 EXPORTS = (
@@ -35,7 +36,7 @@ SCF_EXPORTS = (
     "gbcc_scf_ccsd_inputs", "gbcc_scf_destroy", "gbcc_last_scf_error",
 )
 # test hooks of include/gbcc_testing.h
-TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_gemm_ex3", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_profile_residual",
+TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_gemm_ex3", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_dmma_peak", "gbcc_testing_fixed_split", "gbcc_testing_gemm_fp64tc", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims",
                    "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total", "gbcc_testing_eigh",
@@ -53,6 +54,7 @@ class Config(C.Structure):
         ("diis_ngroup", C.c_int32), ("diis_group_nstart", C.c_int32),
         ("verbose", C.c_int32), ("device", C.c_int32), ("use_graphs", C.c_int32),
         ("slice_tolerance", C.c_double), ("autotune", C.c_int32), ("refine_reset_diis", C.c_int32),
+        ("refine_precision", C.c_int32),
     ]
 
 
@@ -147,6 +149,13 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_testing_scale.argtypes = [vp, C.c_int64, C.c_double, vp]
     lib.gbcc_testing_fp64_peak.restype = C.c_int
     lib.gbcc_testing_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.gbcc_testing_dmma_peak.restype = C.c_int
+    lib.gbcc_testing_dmma_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.gbcc_testing_fixed_split.restype = C.c_int
+    lib.gbcc_testing_fixed_split.argtypes = [vp, C.c_int64, C.c_int64, C.c_int, vp, vp]
+    lib.gbcc_testing_gemm_fp64tc.restype = C.c_int
+    lib.gbcc_testing_gemm_fp64tc.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp, C.c_int, C.c_int, C.c_int,
+                                             C.POINTER(C.c_float)]
     ip = C.POINTER(C.c_int)
     lib.gbcc_testing_profile_residual.restype = C.c_int
     lib.gbcc_testing_profile_residual.argtypes = [vp, C.c_int, C.c_int, dp, dp, ip, ip, ip]

@@ -22,6 +22,9 @@ import numpy as np
 
 from . import _lib as L
 
+# precision names: plain FP64 (DFMA), split-BF16 mixed, FP64-grade on the tensor cores
+_PRECS = {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED, "fp64_tc": L.PREC_FP64_TC}
+
 INTEGRAL_NAMES = ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc", "Gabcd")
 
 
@@ -77,12 +80,12 @@ class Solver:
                  mixed_switch_precision=0.0, max_iter=30, target_precision=1e-9,
                  diis_start=1, n_diis=8, diis_damp=0.0, diis_ngroup=1, diis_group_nstart=1,
                  verbose=False, device=0, use_graphs=2, slice_tolerance=1e-5, autotune=True,
-                 refine_reset_diis=True):
+                 refine_reset_diis=True, refine_precision="fp64"):
         self.lib = L.load()
         cfg = L.Config()
         self.lib.gbcc_config_default(C.byref(cfg))
         cfg.o, cfg.v = int(o), int(v)
-        cfg.precision = {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}[precision]
+        cfg.precision = _PRECS[precision]
         cfg.slices_ladder, cfg.slices_ring, cfg.slices_other = (int(s) for s in slices)
         cfg.refine_iters = int(refine_iters)
         cfg.mixed_switch_precision = float(mixed_switch_precision)
@@ -97,6 +100,8 @@ class Solver:
         cfg.slice_tolerance = float(slice_tolerance)
         cfg.autotune = int(bool(autotune))
         cfg.refine_reset_diis = int(bool(refine_reset_diis))
+        # refinement iterations of a mixed solve: plain FP64 or FP64-grade on the tensor cores
+        cfg.refine_precision = _PRECS[refine_precision]
         self.cfg = cfg
         self.o, self.v = int(o), int(v)
         h = C.c_void_p()
@@ -183,7 +188,7 @@ class Solver:
     def profile_residual(self, precision=None, max_sites=256):
         """Per-operation CUDA-event times of one residual on the device-resident
         amplitudes: list of dicts (ms, flops, pairs, cls)."""
-        prec = self.cfg.precision if precision is None else {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}[precision]
+        prec = self.cfg.precision if precision is None else _PRECS[precision]
         ms = (C.c_double * max_sites)()
         fl = (C.c_double * max_sites)()
         pr = (C.c_int * max_sites)()
@@ -226,7 +231,7 @@ class Solver:
             r1 = np.empty((v, o)) if isinstance(t1, np.ndarray) else t1.new_empty((v, o))
         if r2 is None:
             r2 = np.empty((v, v, o, o)) if isinstance(t2, np.ndarray) else t2.new_empty((v, v, o, o))
-        prec = self.cfg.precision if precision is None else {"fp64": L.PREC_FP64, "mixed": L.PREC_MIXED}[precision]
+        prec = self.cfg.precision if precision is None else _PRECS[precision]
         _check(self.lib, self.h, self.lib.gbcc_residual_ex(self.h, prec, _ptr(t1), _ptr(t2), _ptr(r1), _ptr(r2)))
         return r1, r2
 

@@ -49,9 +49,10 @@ struct gbcc_handle {
   std::vector<double> prof_gemm_ms;
   std::vector<std::array<int64_t, 3>> prof_dims;
   std::vector<std::array<int32_t, 4>> prof_tiles;
-  // residual program captured as a CUDA graph, one per precision (FP64, mixed)
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  int graph_launches[2] = {0, 0};
+  // residual program captured as a CUDA graph, one per precision (FP64,
+  // mixed, FP64_TC: gbcc::plan_index)
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  int graph_launches[3] = {0, 0, 0};
   bool profiling = false;
   bool calibrating = false;
   // slice counts in use per class (ladder, ring, other) and, for classes the
@@ -64,8 +65,9 @@ struct gbcc_handle {
   bool seeded = false;
   bool have_solution = false;
   double last_e = 0.0;
-  // whole-solve graph (use_graphs = 2): the residual programs as graphs (FP64,
-  // mixed), the instantiated loop, its device state, history and timestamps
+  // whole-solve graph (use_graphs = 2): the residual programs as graphs (the
+  // FP64-grade precision, mixed), the instantiated loop, its device state,
+  // history and timestamps
   cudaGraph_t rgraph[2] = {nullptr, nullptr};
   cudaGraphExec_t solve_exec = nullptr;
   gbcc::SolveState* d_state = nullptr;
@@ -135,7 +137,14 @@ void sync_check(gbcc_handle* h) {
 bool check_config(const gbcc_config* c, std::string& why) {
   if (c->o < 1 || c->v < 1) { why = "o and v must be >= 1"; return false; }
   if (c->o > 4096 || c->v > 8192) { why = "o or v out of range"; return false; }
-  if (c->precision != GBCC_PREC_FP64 && c->precision != GBCC_PREC_MIXED) { why = "bad precision"; return false; }
+  if (c->precision != GBCC_PREC_FP64 && c->precision != GBCC_PREC_MIXED && c->precision != GBCC_PREC_FP64_TC) {
+    why = "bad precision";
+    return false;
+  }
+  if (c->refine_precision != GBCC_PREC_FP64 && c->refine_precision != GBCC_PREC_FP64_TC) {
+    why = "refine_precision must be GBCC_PREC_FP64 or GBCC_PREC_FP64_TC";
+    return false;
+  }
   for (int s : {c->slices_ladder, c->slices_ring, c->slices_other})
     if (s < 0 || s > 3) { why = "slices must be 0 (automatic) or 1..3"; return false; }
   if (!(c->slice_tolerance > 0.0)) { why = "slice_tolerance must be > 0"; return false; }
@@ -162,15 +171,24 @@ void drop_graphs(gbcc_handle* h) {
   }
   if (h->solve_exec) cudaGraphExecDestroy(h->solve_exec);
   h->solve_exec = nullptr;
-  h->graph_launches[0] = h->graph_launches[1] = 0;
+  for (int& n : h->graph_launches) n = 0;
 }
+
+// The FP64-grade precision of a handle: its own for FP64 and FP64_TC handles,
+// the refinement's for mixed ones.
+int hi_prec(const gbcc_handle* h) {
+  return h->cfg.precision == GBCC_PREC_MIXED ? h->cfg.refine_precision : h->cfg.precision;
+}
+
+// whether the handle's plan includes the FP64_TC contractions
+bool uses_fp64_tc(const gbcc_handle* h) { return hi_prec(h) == GBCC_PREC_FP64_TC; }
 
 // r1, r2 of the device-resident t1, t2, tau.  The first evaluation in each
 // precision is captured into a CUDA graph (every launch of the EXEC pass has
 // fixed pointers, sizes and tensor maps once the plan is finalised); later
 // evaluations replay it.  Returns the number of kernels it enqueued.
 int enqueue_residual_program(gbcc_handle* h, int precision) {
-  if (precision == GBCC_PREC_MIXED && !h->prepacked) {
+  if (precision != GBCC_PREC_FP64 && !h->prepacked) {
     h->eng->finalize(true);
     h->prepacked = true;
   }
@@ -181,7 +199,7 @@ int enqueue_residual_program(gbcc_handle* h, int precision) {
     return h->eng->kernel_launches();
   };
   if (!h->cfg.use_graphs || h->profiling || h->calibrating) return direct();
-  const int gi = precision == GBCC_PREC_MIXED ? 1 : 0;
+  const int gi = gbcc::plan_index(precision);
   if (!h->graph[gi]) {
     cudaGraph_t g = nullptr;
     GBCC_CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -242,7 +260,7 @@ void ensure_diis(gbcc_handle* h) {
 
 // The residual program of one precision as a (not instantiated) graph.
 cudaGraph_t capture_residual_graph(gbcc_handle* h, int precision) {
-  if (precision == GBCC_PREC_MIXED && !h->prepacked) {
+  if (precision != GBCC_PREC_FP64 && !h->prepacked) {
     h->eng->finalize(true);
     h->prepacked = true;
   }
@@ -316,7 +334,7 @@ void build_solve_graph(gbcc_handle* h) {
   const gbcc_config& c = h->cfg;
   const bool mixed = c.precision == GBCC_PREC_MIXED;
   cudaStream_t st = h->stream;
-  if (!h->rgraph[0]) h->rgraph[0] = capture_residual_graph(h, GBCC_PREC_FP64);
+  if (!h->rgraph[0]) h->rgraph[0] = capture_residual_graph(h, hi_prec(h));
   if (mixed && !h->rgraph[1]) h->rgraph[1] = capture_residual_graph(h, GBCC_PREC_MIXED);
   if (!h->d_state) h->d_state = static_cast<gbcc::SolveState*>(gbcc::dev_alloc(sizeof(gbcc::SolveState)));
   if (!h->d_history) h->d_history = static_cast<double*>(gbcc::dev_alloc((c.max_iter + 1) * 3 * sizeof(double)));
@@ -473,12 +491,14 @@ void plan_residual(gbcc_handle* h) {
   h->prepacked = false;
   h->eng->set_slices(h->slices_used[0], h->slices_used[1], h->slices_used[2]);
   h->eng->set_frozen({h->S.t1, h->S.t2, h->S.tau});
+  h->eng->set_emulation(uses_fp64_tc(h));
   h->eng->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
   gbcc::residual_program(*h->eng, h->S);
   h->eng->end();
-  const bool mixed = h->cfg.precision == GBCC_PREC_MIXED;
-  h->eng->finalize(mixed);
-  h->prepacked = mixed;
+  // the split packs of the constant operands for the tensor-core precisions
+  const bool pack = h->cfg.precision != GBCC_PREC_FP64;
+  h->eng->finalize(pack);
+  h->prepacked = pack;
 }
 
 // Slice counts for the classes configured as 0 (automatic), chosen from their
@@ -619,6 +639,7 @@ void gbcc_config_default(gbcc_config* c) {
   c->slices_ring = 0;
   c->slices_other = 0;
   c->refine_iters = 2;
+  c->refine_precision = GBCC_PREC_FP64;
   c->mixed_switch_precision = 0.0;
   c->max_iter = 30;
   c->target_precision = 1e-9;
@@ -828,8 +849,10 @@ gbcc_status gbcc_residual_ex(gbcc_handle* h, int32_t precision, const double* t1
                              const double* t2_abij, double* r1_ai, double* r2_abij) {
   return guarded(h, [&]() -> gbcc_status {
     if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "gbcc_residual: inputs not set");
-    if (precision != GBCC_PREC_FP64 && precision != GBCC_PREC_MIXED)
+    if (precision != GBCC_PREC_FP64 && precision != GBCC_PREC_MIXED && precision != GBCC_PREC_FP64_TC)
       throw Error(GBCC_ERR_INVALID_ARG, "gbcc_residual: bad precision");
+    if (precision == GBCC_PREC_FP64_TC && !h->eng->emulation())
+      throw Error(GBCC_ERR_STATE, "gbcc_residual: the handle has no FP64_TC plan (precision or refine_precision)");
     if (!t1_ai || !t2_abij || !r1_ai || !r2_abij)
       throw Error(GBCC_ERR_INVALID_ARG, "gbcc_residual: NULL argument");
     h->have_solution = false;
@@ -889,7 +912,7 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
       GBCC_CK(cudaMemcpyAsync(S.t1->d, h->seed1, n1 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
       GBCC_CK(cudaMemcpyAsync(S.t2->d, h->seed2, n2 * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
       h->seeded = false;
-      const int prec = mixed_phase ? GBCC_PREC_MIXED : GBCC_PREC_FP64;
+      const int prec = mixed_phase ? GBCC_PREC_MIXED : hi_prec(h);
       GBCC_CK(cudaEventRecord(h->ev0, h->stream));
       run_residual(h, prec);
       GBCC_CK(cudaEventRecord(h->ev1, h->stream));
@@ -1043,7 +1066,7 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
         GBCC_CK(cudaMemsetAsync(h->Bmat, 0, c.n_diis * c.n_diis * sizeof(double), h->stream));
       }
       // residual of the new amplitudes
-      const int prec = mixed_phase ? GBCC_PREC_MIXED : GBCC_PREC_FP64;
+      const int prec = mixed_phase ? GBCC_PREC_MIXED : hi_prec(h);
       GBCC_CK(cudaEventRecord(h->ev0, h->stream));
       h->last_launches = enqueue_residual_program(h, prec);
       GBCC_CK(cudaEventRecord(h->ev1, h->stream));
@@ -1248,8 +1271,10 @@ int gbcc_testing_profile_residual(gbcc_handle* h, int precision, int max_sites, 
                                   int* pairs, int* cls, int* nsites) {
   return guarded(h, [&]() -> gbcc_status {
     if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "profile: inputs not set");
-    if (precision != GBCC_PREC_FP64 && precision != GBCC_PREC_MIXED)
+    if (precision != GBCC_PREC_FP64 && precision != GBCC_PREC_MIXED && precision != GBCC_PREC_FP64_TC)
       throw Error(GBCC_ERR_INVALID_ARG, "profile: bad precision");
+    if (precision == GBCC_PREC_FP64_TC && !h->eng->emulation())
+      throw Error(GBCC_ERR_STATE, "profile: the handle has no FP64_TC plan");
     h->eng->set_profile(true);
     h->profiling = true;
     try {

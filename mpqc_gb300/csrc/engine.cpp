@@ -149,7 +149,13 @@ struct OperandPlan {
   bool cache_first = false;  // packs into cache_buf
   bool cache_reuse = false;  // reads cache_buf packed by an earlier contraction
   __nv_bfloat16* cache_buf = nullptr;
+  // FP64_TC: fixed-point slices under per-row exponents (rows_pad words)
+  bool fixed = false;
+  unsigned* rowexp = nullptr;
 };
+
+// slice pairs of a plan: 3 slices give 6, the fixed-point split's 6 slices 21
+constexpr int kMaxPlanPairs = 36;
 
 struct GemmPlan {
   bool use_tc = false;
@@ -162,10 +168,11 @@ struct GemmPlan {
   double alpha = 1.0, beta = 0.0;
   double* C = nullptr;
   int slices = 0, npairs = 0, bn = 0;
+  bool emu = false;        // FP64_TC: pairs ordered by weight class, one launch per class
   int ksplit = 1;         // K split over CTAs (deterministic two-pass reduction)
   bool m_major = false;   // C unit-stride along M
   int64_t k_per_split = 0;  // FP64: K elements per split; tensor cores: k-blocks per split
-  int pa[kMaxPairs] = {}, pb[kMaxPairs] = {};
+  int pa[kMaxPlanPairs] = {}, pb[kMaxPlanPairs] = {};
   double flops = 0.0;
   int sps = 1;             // tensor cores: slices per pipeline stage (2: both slices of a k-block)
   int group = 1;           // tensor cores: M tiles per band of the tile order (1: rows)
@@ -181,7 +188,7 @@ struct Site {
   int kind = 0;  // 0 assign, 1 contract, 2 custom kernels
   TermClass cls = kClassOther;
   GatherArgs gather{};
-  GemmPlan plan[2];
+  GemmPlan plan[3];  // by plan_index(precision)
   cudaEvent_t e0 = nullptr, e1 = nullptr, eg = nullptr;  // profiling: start, end, GEMM start
   bool has_gemm = false;
   ~Site() {
@@ -225,9 +232,10 @@ std::vector<SiteStat> Engine::site_stats(int precision) {
       }
     }
     if (sp->kind == 1) {
-      const GemmPlan& p = sp->plan[precision == GBCC_PREC_MIXED ? 1 : 0];
+      const GemmPlan& p = sp->plan[plan_index(precision)];
       st.flops = p.flops;
       st.pairs = p.use_tc ? p.npairs : 0;
+      st.classes = p.use_tc && p.emu ? p.slices : 0;
       st.cls = sp->cls;
       st.M = p.M;
       st.N = p.N;
@@ -438,11 +446,24 @@ __nv_bfloat16* Engine::tc_panel(OperandPlan& op, int side) {
   }
   if (op.cache_reuse) return op.cache_buf;
   __nv_bfloat16* out = op.cache_first ? op.cache_buf : (side == 0 ? wbfa_ : wbfb_);
+  pack_panel(op, out);
+  return out;
+}
+
+// Split pack of an operand into `out`: one gather, or for fixed-point slices
+// the row exponents (zeroed, then the exponent pass) and the digit pass.
+void Engine::pack_panel(const OperandPlan& op, __nv_bfloat16* out) {
   GatherArgs g = op.gather;
   g.outs = out;
+  if (op.fixed) {
+    GBCC_CK(cudaMemsetAsync(op.rowexp, 0, static_cast<size_t>(op.rows_pad) * sizeof(unsigned), stream_));
+    g.fixed = 1;
+    launch_gather(g, stream_);
+    g.fixed = 2;
+    ++n_launch_;  // the exponent pass (the memset is not a kernel)
+  }
   launch_gather(g, stream_);
   ++n_launch_;
-  return out;
 }
 
 GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* const panel[2]) const {
@@ -460,10 +481,12 @@ GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* cons
   t.b_slices = p.slices;
   // a slice limit below the packed count keeps the pairs p + q < limit: the
   // split is sequential, so these are exactly the products of a
-  // limit-slice split (used to measure the error of fewer slices)
-  const int lim = slice_limit_[cls];
+  // limit-slice split (used to measure the error of fewer slices); it
+  // applies to the mixed plan only
+  const int lim = p.emu ? 0 : slice_limit_[cls];
   t.npairs = 0;
-  for (int q = 0; q < p.npairs; ++q) {
+  // FP64_TC: the pairs of each weight class are set per launch (launch_tc_classes)
+  for (int q = 0; q < (p.emu ? 0 : p.npairs); ++q) {
     if (lim > 0 && p.pa[q] + p.pb[q] >= lim) continue;
     t.pa[t.npairs] = p.pa[q];
     t.pb[t.npairs] = p.pb[q];
@@ -477,8 +500,14 @@ GemmTcArgs Engine::tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* cons
   t.bn = p.bn;
   // the accumulation length of the slice count in effect (a calibration trial
   // under a slice limit measures the error the smaller plan will have)
-  const int eff_slices = (slice_limit_[cls] > 0 && slice_limit_[cls] < p.slices) ? slice_limit_[cls] : p.slices;
+  const int eff_slices = (lim > 0 && lim < p.slices) ? lim : p.slices;
   t.chunk = eff_slices >= 3 ? chunk_ : chunk_lo_;
+  if (p.emu) {
+    // exact FP32 chunk sums: 4 steps of 64 products below 2^14 units each,
+    // two chunks per FP32 register sum before the float-float fold
+    t.chunk = kFixedChunk;
+    t.fold = kFixedFold;
+  }
   t.err = err_;
   t.ksplit = p.ksplit;
   t.kb_per_split = static_cast<int>(p.k_per_split);
@@ -497,8 +526,19 @@ void Engine::launch_tc(const GemmPlan& p, const GemmTcArgs& t) {
   ++tc_total_;
   ++n_launch_;
   if (p.ksplit > 1) {
-    launch_splitk_reduce(p.M, p.N, p.ksplit, wpart_, t.Mpad, t.Npad, p.C, p.cm, p.cn, p.alpha, p.beta, stream_);
+    launch_splitk_reduce(p.M, p.N, p.ksplit, wpart_, t.Mpad, t.Npad, p.C, p.cm, p.cn, t.alpha, t.beta, stream_);
     ++n_launch_;
+  }
+}
+
+// FP64_TC: one launch per weight class w = p + q, the classes of the smallest
+// weight first; the first applies the call's beta, the rest accumulate.
+void Engine::launch_tc_classes(const GemmPlan& p, TermClass cls, __nv_bfloat16* const panel[2]) {
+  GemmTcArgs t = tc_args(p, cls, panel);
+  for (int w = p.slices - 1; w >= 0; --w) {
+    t.npairs = fixed_class_pairs(p.slices, w, t.pa, t.pb);
+    t.beta = w == p.slices - 1 ? p.beta : 1.0;
+    launch_tc(p, t);
   }
 }
 
@@ -578,15 +618,19 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
   Site& s = site();
   if (mode_ == Mode::kExec) {
     if (s.kind != 1) throw Error(GBCC_ERR_STATE, "engine: site kind mismatch");
-    GemmPlan& p = s.plan[prec_ == GBCC_PREC_MIXED ? 1 : 0];
+    GemmPlan& p = s.plan[plan_index(prec_)];
     flops_ += p.flops;
     prof_begin(s);
     if (p.use_tc) {
       __nv_bfloat16* panel[2];
       for (int side = 0; side < 2; ++side) panel[side] = tc_panel(p.P[side], side);
-      const GemmTcArgs t = tc_args(p, cls, panel);
       prof_gemm(s);
-      launch_tc(p, t);
+      if (p.emu) {
+        launch_tc_classes(p, cls, panel);
+      } else {
+        const GemmTcArgs t = tc_args(p, cls, panel);
+        launch_tc(p, t);
+      }
     } else {
       const double* panel[2];
       for (int side = 0; side < 2; ++side) {
@@ -667,14 +711,16 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
   for (const auto& l : B) constB = constB && l.x.t->constant && (!l.y.t || l.y.t->constant);
   const double flops = 2.0 * static_cast<double>(rowsA) * rowsB * K;
 
-  for (int pm = 0; pm < 2; ++pm) {
+  for (int pm = 0; pm < (emu_ ? 3 : 2); ++pm) {
     GemmPlan& p = s.plan[pm];
     p = GemmPlan{};
     p.flops = flops;
-    int slices = pm == 1 ? slices_for(cls, flops) : 0;
+    const bool emu = pm == 2;
+    int slices = pm == 1 ? slices_for(cls, flops) : (emu && slices_for(cls, flops) > 0 ? kFixedSlices : 0);
     // a short contraction into a large output is memory-bound: CUDA cores
-    // (measured faster for N > 32; the tensor-core kernel wins below)
-    if (slices > 0 && K <= kSmallK && std::min(rowsA, rowsB) > 32 &&
+    // (measured faster for N > 32; the tensor-core kernel wins below).  The
+    // FP64-grade plan keeps such contractions on the FP64 kernel.
+    if (slices > 0 && !emu && K <= kSmallK && std::min(rowsA, rowsB) > 32 &&
         static_cast<double>(rowsA) * static_cast<double>(rowsB) >= 1048576.0) {
       slices = 0;
       p.smallk = true;
@@ -813,21 +859,27 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     }
     if (p.use_tc) {
       p.slices = slices;
+      p.emu = emu;
       // the ladder and ring contractions take the faster 192/256-wide tiles
-      const bool wide = cls == kClassLadder || cls == kClassRing;
+      // (not FP64_TC: its chunk sums need the float-float fold of tiles up to 128)
+      const bool wide = !emu && (cls == kClassLadder || cls == kClassRing);
       p.bn = gemm_tc_pick_bn(p.N, wide);
       int bns[4];
       const int nbn = gemm_tc_bn_candidates(p.N, wide, bns);
       int64_t npanel = 0;  // N-side panel rows: room for every candidate tile width
       for (int c = 0; c < nbn; ++c) npanel = std::max<int64_t>(npanel, round_up(p.N, bns[c]));
       p.npairs = 0;
-      for (int a = 0; a < slices; ++a)
-        for (int b = 0; b < slices; ++b)
-          if (a + b < slices) {
-            p.pa[p.npairs] = a;
-            p.pb[p.npairs] = b;
-            ++p.npairs;
-          }
+      if (emu) {
+        for (int w = 0; w < slices; ++w) p.npairs += fixed_class_pairs(slices, w, p.pa + p.npairs, p.pb + p.npairs);
+      } else {
+        for (int a = 0; a < slices; ++a)
+          for (int b = 0; b < slices; ++b)
+            if (a + b < slices) {
+              p.pa[p.npairs] = a;
+              p.pb[p.npairs] = b;
+              ++p.npairs;
+            }
+      }
       const int64_t Kpad = round_up(std::max<int64_t>(K, 1), kTcBK);
       for (int side = 0; side < 2; ++side) {
         OperandPlan& op = p.P[side];
@@ -841,6 +893,14 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         g.out = nullptr;
         g.nslices = slices;
         g.slice_stride = op.rows_pad * Kpad;
+        if (emu) {
+          op.fixed = true;
+          op.rowexp = static_cast<unsigned*>(dev_alloc(static_cast<size_t>(op.rows_pad) * sizeof(unsigned)));
+          owned_.push_back(op.rowexp);
+          bytes_ += static_cast<size_t>(op.rows_pad) * sizeof(unsigned);
+          g.rowexp = op.rowexp;
+          g.fixed = 2;
+        }
         const size_t need = static_cast<size_t>(slices) * op.rows_pad * Kpad;
         if (!op.constant) {
           bool frozen = true;
@@ -854,7 +914,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
             sig += "*" + std::to_string(coef) + ";";
           }
           if (frozen) {
-            op.sig = sig + op.ext + "|" + op.kord + "|" + std::to_string(slices) + "|" +
+            op.sig = sig + op.ext + "|" + op.kord + "|" + (emu ? "fixed" : "float") + std::to_string(slices) + "|" +
                      std::to_string(op.rows_pad) + "|" + std::to_string(Kpad);
             op.pack_elems = need;
             pack_uses_[op.sig].push_back(&op);
@@ -915,7 +975,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
   }
 }
 
-void Engine::finalize(bool prepack_mixed) {
+void Engine::finalize(bool prepack) {
   if (!planned_) throw Error(GBCC_ERR_STATE, "engine: finalize before PLAN");
   dev_free(w64a_);
   dev_free(w64b_);
@@ -943,22 +1003,22 @@ void Engine::finalize(bool prepack_mixed) {
       kv.second[i]->cache_buf = first->cache_buf;
     }
   }
-  if (prepack_mixed) {
+  if (prepack) {
     for (auto& sp : sites_) {
       if (sp->kind != 1) continue;
-      GemmPlan& p = sp->plan[1];
-      if (!p.use_tc) continue;
-      for (int side = 0; side < 2; ++side) {
-        OperandPlan& op = p.P[side];
-        if (!op.constant) continue;
-        if (!op.packed) {
-          op.packed = static_cast<__nv_bfloat16*>(dev_alloc(op.pack_elems * sizeof(__nv_bfloat16)));
-          owned_.push_back(op.packed);
-          bytes_ += op.pack_elems * sizeof(__nv_bfloat16);
+      for (int pi = 1; pi < (emu_ ? 3 : 2); ++pi) {
+        GemmPlan& p = sp->plan[pi];
+        if (!p.use_tc) continue;
+        for (int side = 0; side < 2; ++side) {
+          OperandPlan& op = p.P[side];
+          if (!op.constant) continue;
+          if (!op.packed) {
+            op.packed = static_cast<__nv_bfloat16*>(dev_alloc(op.pack_elems * sizeof(__nv_bfloat16)));
+            owned_.push_back(op.packed);
+            bytes_ += op.pack_elems * sizeof(__nv_bfloat16);
+          }
+          pack_panel(op, op.packed);
         }
-        GatherArgs g = op.gather;
-        g.outs = op.packed;
-        launch_gather(g, stream_);
       }
     }
     GBCC_CK(cudaGetLastError());

@@ -96,6 +96,11 @@ enum TermClass { kClassLadder = 0, kClassRing = 1, kClassOther = 2 };
 
 enum class Mode { kPlan, kExec };
 
+// index of a precision's plan in a call site: FP64 0, MIXED 1, FP64_TC 2
+inline int plan_index(int precision) {
+  return precision == GBCC_PREC_MIXED ? 1 : (precision == GBCC_PREC_FP64_TC ? 2 : 0);
+}
+
 struct DevTable {
   int64_t* d = nullptr;
   int64_t n = 0;
@@ -108,6 +113,7 @@ struct SiteStat {
   double gemm_ms = 0.0;  // of which the GEMM kernel
   double flops = 0.0;  // 2 M N K of a contraction, 0 for an assignment
   int pairs = 0;       // BF16 slice products on the tensor cores (0: FP64 / elementwise)
+  int classes = 0;     // FP64_TC: launches, one per weight class (0 otherwise)
   int cls = -1;        // TermClass of a contraction, -1 for an assignment
   int64_t M = 0, N = 0, K = 0;  // GEMM shape (assignment: rows, columns, 0)
   int bn = 0;          // tensor cores: N tile width; -1: the short-K CUDA-core kernel
@@ -147,6 +153,10 @@ class Engine {
     chunk_ = three_slices;
     chunk_lo_ = fewer;
   }
+  // Whether the next PLAN also builds the FP64-grade tensor-core plan
+  // (GBCC_PREC_FP64_TC: fixed-point slices, one launch per weight class)
+  void set_emulation(bool on) { emu_ = on; }
+  bool emulation() const { return emu_; }
   // Record CUDA events around every operation of EXEC passes.
   void set_profile(bool on) { profile_ = on; }
   // Tensors a residual program reads but never writes (its amplitude inputs);
@@ -163,8 +173,9 @@ class Engine {
   void end();
   bool planned() const { return planned_; }
   void reset_plans();  // inputs changed: rebuild everything on the next PLAN
-  // After a PLAN pass: allocate workspaces; pack constant operands for MIXED.
-  void finalize(bool prepack_mixed);
+  // After a PLAN pass: allocate workspaces; pack the constant operands of the
+  // tensor-core plans (MIXED, and FP64_TC where planned).
+  void finalize(bool prepack);
 
   // C = beta*C + sum_t coef_t * a_t (* b_t); labels of each factor must be a
   // subset of C's labels (missing labels broadcast).
@@ -194,6 +205,8 @@ class Engine {
   void prof_gemm(Site& s);
   DevTable upload(const std::vector<int64_t>& v);
   __nv_bfloat16* tc_panel(OperandPlan& op, int side);
+  void pack_panel(const OperandPlan& op, __nv_bfloat16* out);
+  void launch_tc_classes(const GemmPlan& p, TermClass cls, __nv_bfloat16* const panel[2]);
   GemmTcArgs tc_args(const GemmPlan& p, TermClass cls, __nv_bfloat16* const panel[2]) const;
   void launch_tc(const GemmPlan& p, const GemmTcArgs& t);
   int slices_for(TermClass cls, double flops) const;
@@ -226,6 +239,7 @@ class Engine {
   int chunk_ = 4;
   int chunk_lo_ = 24;
   bool profile_ = false;
+  bool emu_ = false;
   std::unordered_set<const Tensor*> frozen_;
   std::unordered_map<std::string, std::vector<struct OperandPlan*>> pack_uses_;
   double flops_ = 0.0;

@@ -7,6 +7,7 @@
 // BF16 split works on bit patterns and FP32 remainders, and single-term packs
 // are plain copies (their coefficient scales the GEMM instead).
 #include "fp_bits.cuh"
+#include "gather.cuh"
 #include "kernels.h"
 
 #include <algorithm>
@@ -24,339 +25,11 @@ inline unsigned grid_for(int64_t n, int threads, int64_t cap = 152 * 32) {
   return static_cast<unsigned>(b);
 }
 
-// q = x / d and r = x % d for 0 <= x, d < 2^32 (every index split in these
-// kernels: x < v^2, v o, o^2).  32-bit division is a few integer and FP32
-// instructions; 64-bit integer division is a long sequence that also occupies
-// the FP64 pipe, which measurably slowed the elementwise kernels.
-__device__ __forceinline__ void divmod32(int64_t x, int64_t d, int64_t& q, int64_t& r) {
-  const unsigned xx = static_cast<unsigned>(x), dd = static_cast<unsigned>(d);
-  const unsigned qq = xx / dd;
-  q = qq;
-  r = xx - qq * dd;
-}
-
-// BF16 bits of a finite float, rounded to nearest even (integer operations only)
-__device__ __forceinline__ unsigned bf16_rne(float f) {
-  const unsigned b = __float_as_uint(f);
-  return (b + 0x7FFFu + ((b >> 16) & 1u)) >> 16;
-}
-
-// Split of an FP64 value into nslices (<= 3) BF16 slices, x ~ s1 + s2 + s3.
-// The value is first taken apart without FP64 arithmetic (GB300 runs FP64
-// and its conversions at ~2 per clock per SM): hi = x truncated to 24
-// significant bits, exact, from the bit pattern; lo = the remaining 29
-// mantissa bits, one integer-to-float conversion (relative error 2^-24 of lo,
-// i.e. 2^-47 of x).  Each slice is then the remainder rounded to BF16 (nearest
-// even), remainders in FP32: s1 = bf16(hi), r = (hi - s1) + lo, s2 = bf16(r),
-// r -= s2, s3 = bf16(r); hi - s1 and r - s2 are exact, so
-// |x - s1 - s2 - s3| <= 2^-24 |x| (plus 2^-33 |x| from absorbing lo).
-// |x| >= 2^128 gives infinity, |x| < 2^-126 signed zeros, nan stays nan.
-// The numpy emulation in the tests follows these steps bit for bit.
-__device__ __forceinline__ void split_bits(double x, unsigned short* out, int nslices) {
-  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(x));
-  const unsigned sign = static_cast<unsigned>(u >> 63);
-  const int E = static_cast<int>((u >> 52) & 0x7FFull);
-  out[0] = out[1] = out[2] = 0;
-  const int e32 = E - 896;  // biased FP32 exponent of x
-  if (E == 0x7FF) {
-    out[0] = static_cast<unsigned short>((sign << 15) | ((u & 0xFFFFFFFFFFFFFull) ? 0x7FC0u : 0x7F80u));
-    return;
-  }
-  if (e32 >= 255) {
-    out[0] = static_cast<unsigned short>((sign << 15) | 0x7F80u);
-    return;
-  }
-  if (e32 <= 0) {  // zero, FP64 subnormals and magnitudes below FP32's normal range
-    out[0] = static_cast<unsigned short>(sign << 15);
-    return;
-  }
-  const float hi = __uint_as_float((sign << 31) | (static_cast<unsigned>(e32) << 23) |
-                                   (static_cast<unsigned>(u >> 29) & 0x7FFFFFu));
-  const unsigned lo_int = static_cast<unsigned>(u) & 0x1FFFFFFFu;  // value lo_int * 2^(E - 1075)
-  const int es = E - 948;                                           // biased FP32 exponent of 2^(E - 1075)
-  float lo = 0.f;
-  if (lo_int != 0u) {
-    // 2^(E - 1075) is below FP32's normal range for |x| < 2^-74: scale in two steps
-    lo = es >= 1 ? __uint2float_rn(lo_int) * __uint_as_float(static_cast<unsigned>(es) << 23)
-                 : (__uint2float_rn(lo_int) * 0x1p-64f) * __uint_as_float(static_cast<unsigned>(es + 64) << 23);
-    if (sign) lo = -lo;
-  }
-  const unsigned b1 = bf16_rne(hi);
-  out[0] = static_cast<unsigned short>(b1);
-  if (nslices < 2) return;
-  float r = __fadd_rn(__fsub_rn(hi, __uint_as_float(b1 << 16)), lo);
-  const unsigned b2 = bf16_rne(r);
-  out[1] = static_cast<unsigned short>(b2);
-  if (nslices < 3) return;
-  r = __fsub_rn(r, __uint_as_float(b2 << 16));
-  out[2] = static_cast<unsigned short>(bf16_rne(r));
-}
-
-// Element (r, c) of a BF16 slice panel, k-block major: [Cpad / 64][Rpad][64]
-// per slice, so that a 64-wide k-block of consecutive rows (one TMA box of
-// the tensor-core GEMM) is a contiguous run of memory.  Cpad is a multiple of 64.
-__device__ __forceinline__ int64_t panel_index(const GatherArgs& g, int64_t r, int64_t c) {
-  return (c >> 6) * (g.Rpad << 6) + (r << 6) + (c & 63);
-}
-
-__device__ __forceinline__ void split_store(double x, __nv_bfloat16* out, int nslices,
-                                            int64_t slice_stride, int64_t idx) {
-  unsigned short b[3];
-  split_bits(x, b, nslices);
-  for (int s = 0; s < nslices; ++s) out[s * slice_stride + idx] = __ushort_as_bfloat16(b[s]);
-}
-
-// coef * x for one gather term whose coefficient is +-2^k (GatherTerm.pow2)
-__device__ __forceinline__ double term_scale(const GatherTerm& T, double x) {
-  return flip_sign(scale_pow2(x, T.pow2_k), T.pow2_sign != 0ull);
-}
-
-// Value of one packed element from NT terms: NT = 0 is a plain load (a single
-// unscaled term whose coefficient was folded into the GEMM's alpha), otherwise
-// the sum of the scaled terms, one FP64 add per term after the first.  PROD:
-// some terms carry a second factor.  The term count, PROD and the
-// read-modify-write of the output are template parameters, dispatched once per
-// launch: as runtime conditions inside the element loop the compiler
-// if-converts them, and the predicated FP64 instructions still occupy the FP64
-// pipe.
-// NT = -1: any coefficients (GatherArgs.general), an FP64 multiply-add per term.
-template <int NT, bool PROD>
-__device__ __forceinline__ double gather_value(const GatherArgs& g, int64_t r, int64_t c) {
-  if constexpr (NT == 0) {
-    return g.t[0].a[g.t[0].ra[r] + g.t[0].ca[c]];
-  } else if constexpr (NT < 0) {
-    double val = 0.0;
-    for (int t = 0; t < g.nterms; ++t) {
-      const GatherTerm& T = g.t[t];
-      double x = T.a[T.ra[r] + T.ca[c]];
-      if (T.b) x *= T.b[T.rb[r] + T.cb[c]];
-      val = fma(T.coef, x, val);
-    }
-    return val;
-  } else {
-    double x[NT];
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-      const GatherTerm& T = g.t[t];
-      x[t] = T.a[T.ra[r] + T.ca[c]];
-      if constexpr (PROD) {
-        if (T.b) x[t] *= T.b[T.rb[r] + T.cb[c]];
-      }
-    }
-    double val = term_scale(g.t[0], x[0]);
-#pragma unroll
-    for (int t = 1; t < NT; ++t) val += term_scale(g.t[t], x[t]);
-    return val;
-  }
-}
-
-// calls BODY(NT, PROD) for the launch's term count and product flag
-#define GBCC_GATHER_DISPATCH(g, BODY)                        \
-  do {                                                       \
-    const int nt_ = (g).plain ? 0 : (g).nterms;              \
-    if ((g).general && nt_ > 0) {                            \
-      BODY(-1, true);                                        \
-    } else if ((g).products) {                               \
-      switch (nt_) {                                         \
-        case 1: BODY(1, true); break;                        \
-        case 2: BODY(2, true); break;                        \
-        case 3: BODY(3, true); break;                        \
-        default: BODY(4, true); break;                       \
-      }                                                      \
-    } else {                                                 \
-      switch (nt_) {                                         \
-        case 0: BODY(0, false); break;                       \
-        case 1: BODY(1, false); break;                       \
-        case 2: BODY(2, false); break;                       \
-        case 3: BODY(3, false); break;                       \
-        default: BODY(4, false); break;                      \
-      }                                                      \
-    }                                                        \
-  } while (0)
-
-// blockDim = (bx, by): threads along C, rows along R.  Each thread takes
-// kGatherRows rows per step and issues all their loads (and the old output
-// values when beta != 0) before its stores, so that several DRAM loads per
-// thread are in flight; one load at a time leaves a pass latency-bound.
-constexpr int kGatherRows = 4;
-
-template <int NT, bool PROD, bool RMW>
-__device__ __forceinline__ void gather_rows(const GatherArgs& g) {
-  const int64_t c0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int64_t cstep = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  const int64_t r0 = static_cast<int64_t>(blockIdx.y) * blockDim.y + threadIdx.y;
-  const int64_t rstep = static_cast<int64_t>(gridDim.y) * blockDim.y;
-  for (int64_t c = c0; c < g.Cpad; c += cstep) {
-    const bool cin = c < g.C;
-    for (int64_t r = r0; r < g.Rpad; r += kGatherRows * rstep) {
-      double val[kGatherRows], old[kGatherRows];
-#pragma unroll
-      for (int u = 0; u < kGatherRows; ++u) {
-        const int64_t ru = r + u * rstep;
-        val[u] = (cin && ru < g.R) ? gather_value<NT, PROD>(g, ru, c) : 0.0;
-        if constexpr (RMW) old[u] = ru < g.Rpad ? g.out[ru * g.ldo + c] : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < kGatherRows; ++u) {
-        const int64_t ru = r + u * rstep;
-        if (ru >= g.Rpad) break;
-        if (g.out) {
-          if constexpr (RMW) g.out[ru * g.ldo + c] = fma(g.beta, old[u], val[u]);
-          else g.out[ru * g.ldo + c] = val[u];
-        } else {
-          split_store(val[u], g.outs, g.nslices, g.slice_stride, panel_index(g, ru, c));
-        }
-      }
-    }
-  }
-}
-
 __global__ void __launch_bounds__(kThreads, 4) gather_kernel(GatherArgs g) {
   const bool rmw = g.out && g.beta != 0.0;
-#define GBCC_ROWS(N, P) (rmw ? gather_rows<N, P, true>(g) : gather_rows<N, P, false>(g))
+#define GBCC_ROWS(N, P) (rmw ? gather_rows<N, P, true, 0>(g) : gather_rows<N, P, false, 0>(g))
   GBCC_GATHER_DISPATCH(g, GBCC_ROWS);
 #undef GBCC_ROWS
-}
-
-// Packs into BF16 slices, 4 consecutive K elements of kSplitRows rows per
-// thread step, all loads issued before the stores, any number of terms.  A
-// term whose K offsets run in contiguous, even-aligned groups of four (c4) is
-// read with two 16-byte vector loads per group where its row offset is even;
-// otherwise its K offsets are read as 16-byte vectors and the elements one by
-// one.  Every slice gets one 8-byte store per thread and row; the launcher
-// checks Cpad, ldo and slice_stride are multiples of 4 (K is padded to 64) so
-// the stores are 8-byte aligned.
-constexpr int kSplitRows = 2;
-
-// x[0..3] = the term's source at row offset rb and K elements c..c+3
-__device__ __forceinline__ void load4(const GatherTerm& T, int64_t rb, int64_t c, int64_t C, double x[4]) {
-  const double* __restrict__ a = T.a;
-  const int64_t* __restrict__ ca = T.ca;
-  if (c + 3 < C) {
-    if (T.c4 && (rb & 1) == 0) {
-      const int64_t o = ca[c];
-      const double2 v01 = *reinterpret_cast<const double2*>(a + rb + o);
-      const double2 v23 = *reinterpret_cast<const double2*>(a + rb + o + 2);
-      x[0] = v01.x;
-      x[1] = v01.y;
-      x[2] = v23.x;
-      x[3] = v23.y;
-    } else {
-      const longlong2 o01 = *reinterpret_cast<const longlong2*>(ca + c);
-      const longlong2 o23 = *reinterpret_cast<const longlong2*>(ca + c + 2);
-      x[0] = a[rb + o01.x];
-      x[1] = a[rb + o01.y];
-      x[2] = a[rb + o23.x];
-      x[3] = a[rb + o23.y];
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) x[j] = c + j < C ? a[rb + ca[c + j]] : 0.0;
-  }
-}
-
-// values of K elements c..c+3 of row r (0 outside R x C), NT terms as in gather_value
-template <int NT, bool PROD>
-__device__ __forceinline__ void split4_values(const GatherArgs& g, int64_t r, int64_t c, double v[4]) {
-  if (r >= g.R) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) v[j] = 0.0;
-    return;
-  }
-  if constexpr (NT == 0) {
-    load4(g.t[0], g.t[0].ra[r], c, g.C, v);
-  } else if constexpr (NT < 0) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) v[j] = c + j < g.C ? gather_value<NT, PROD>(g, r, c + j) : 0.0;
-  } else {
-    double x[NT][4];
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-      const GatherTerm& T = g.t[t];
-      load4(T, T.ra[r], c, g.C, x[t]);
-      if constexpr (PROD) {
-        if (T.b) {
-          double y[4];
-          GatherTerm U = T;
-          U.a = T.b;
-          U.ca = T.cb;
-          U.c4 = 0;
-          load4(U, T.rb[r], c, g.C, y);
-#pragma unroll
-          for (int j = 0; j < 4; ++j) x[t][j] *= y[j];
-        }
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      double val = term_scale(g.t[0], x[0][j]);
-#pragma unroll
-      for (int t = 1; t < NT; ++t) val += term_scale(g.t[t], x[t][j]);
-      v[j] = val;
-    }
-  }
-}
-
-// the 4 values split into BF16 slices, one 8-byte store per slice
-__device__ __forceinline__ void split4_store(const GatherArgs& g, int64_t r, int64_t c, const double v[4]) {
-  unsigned short* o4 = reinterpret_cast<unsigned short*>(g.outs) + panel_index(g, r, c);
-  unsigned short b[4][3];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) split_bits(v[j], b[j], g.nslices);
-#pragma unroll
-  for (int s = 0; s < 3; ++s) {
-    if (s >= g.nslices) break;
-    uint2 w;
-    w.x = static_cast<unsigned>(b[0][s]) | (static_cast<unsigned>(b[1][s]) << 16);
-    w.y = static_cast<unsigned>(b[2][s]) | (static_cast<unsigned>(b[3][s]) << 16);
-    *reinterpret_cast<uint2*>(o4 + s * g.slice_stride) = w;
-  }
-}
-
-// OUT 0: BF16 slices; 1: FP64 stores; 2: FP64 read-modify-write (beta)
-template <int NT, bool PROD, int OUT>
-__device__ __forceinline__ void split4_rows(const GatherArgs& g) {
-  const int64_t nq = g.Cpad / 4;
-  const int64_t q0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int64_t qstep = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  const int64_t r0 = static_cast<int64_t>(blockIdx.y) * blockDim.y + threadIdx.y;
-  const int64_t rstep = static_cast<int64_t>(gridDim.y) * blockDim.y;
-  for (int64_t r = r0; r < g.Rpad; r += kSplitRows * rstep) {
-    for (int64_t q = q0; q < nq; q += qstep) {
-      const int64_t c = 4 * q;
-      double v[kSplitRows][4];
-      double2 old[kSplitRows][2];
-#pragma unroll
-      for (int u = 0; u < kSplitRows; ++u) {
-        const int64_t ru = r + u * rstep;
-        split4_values<NT, PROD>(g, ru, c, v[u]);
-        if constexpr (OUT == 2) {
-          if (ru < g.Rpad) {
-            const double2* po = reinterpret_cast<const double2*>(g.out + ru * g.ldo + c);
-            old[u][0] = po[0];
-            old[u][1] = po[1];
-          }
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kSplitRows; ++u) {
-        const int64_t ru = r + u * rstep;
-        if (ru >= g.Rpad) break;
-        if constexpr (OUT == 0) {
-          split4_store(g, ru, c, v[u]);
-        } else {
-          double2* po = reinterpret_cast<double2*>(g.out + ru * g.ldo + c);
-          if constexpr (OUT == 2) {
-            po[0] = make_double2(fma(g.beta, old[u][0].x, v[u][0]), fma(g.beta, old[u][0].y, v[u][1]));
-            po[1] = make_double2(fma(g.beta, old[u][1].x, v[u][2]), fma(g.beta, old[u][1].y, v[u][3]));
-          } else {
-            po[0] = make_double2(v[u][0], v[u][1]);
-            po[1] = make_double2(v[u][2], v[u][3]);
-          }
-        }
-      }
-    }
-  }
 }
 
 // 4 K elements per thread into BF16 slices
@@ -366,6 +39,7 @@ __global__ void __launch_bounds__(kThreads, 4) gather_split4_kernel(GatherArgs g
 #undef GBCC_SPLIT4
 }
 
+
 // 4 columns per thread into 16-byte aligned FP64 rows (assignments, FP64 panels)
 __global__ void __launch_bounds__(kThreads, 3) gather4_f64_kernel(GatherArgs g) {
   const bool rmw = g.beta != 0.0;
@@ -374,64 +48,10 @@ __global__ void __launch_bounds__(kThreads, 3) gather4_f64_kernel(GatherArgs g) 
 #undef GBCC_F64X4
 }
 
-// Same contract as gather_kernel for sources contiguous along R: a 32 x 32
-// tile is read with the lanes along R (coalesced), transposed through shared
-// memory and written with the lanes along C (coalesced).  Block 32 x 8.
-template <int NT, bool PROD, bool RMW>
-__device__ __forceinline__ void gather_tiles(const GatherArgs& g, double (*tile)[33]) {
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int64_t nrt = (g.Rpad + 31) / 32, nct = (g.Cpad + 31) / 32;
-  // BF16-slice output with 4-aligned rows: each thread writes 4 consecutive
-  // columns of one row (one 8-byte store per slice) instead of one column
-  const bool wide = g.outs && ((g.Cpad | g.ldo | g.slice_stride) & 3) == 0 &&
-                    (reinterpret_cast<uintptr_t>(g.outs) & 7) == 0;
-  for (int64_t t = blockIdx.x; t < nrt * nct; t += gridDim.x) {
-    int64_t tr, tc;
-    divmod32(t, nct, tr, tc);
-    const int64_t r0 = tr * 32, c0 = tc * 32;
-    // read: lanes along r
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int64_t r = r0 + tx, c = c0 + ty + 8 * k;
-      tile[ty + 8 * k][tx] = (r < g.R && c < g.C) ? gather_value<NT, PROD>(g, r, c) : 0.0;
-    }
-    __syncthreads();
-    if (wide) {
-      // thread (row rl, columns cg..cg+3); a warp covers 4 rows x 32 columns
-      const int t = ty * 32 + tx, rl = t >> 3, cg = (t & 7) * 4;
-      const int64_t r = r0 + rl, c = c0 + cg;
-      if (r < g.Rpad && c < g.Cpad) {
-        double v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = tile[cg + j][rl];
-        split4_store(g, r, c, v);
-      }
-      __syncthreads();
-      continue;
-    }
-    // write: lanes along c
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int64_t r = r0 + ty + 8 * k, c = c0 + tx;
-      if (r < g.Rpad && c < g.Cpad) {
-        const double val = tile[tx][ty + 8 * k];
-        if (g.out) {
-          double* p = g.out + r * g.ldo + c;
-          if constexpr (RMW) *p = fma(g.beta, *p, val);
-          else *p = val;
-        } else {
-          split_store(val, g.outs, g.nslices, g.slice_stride, panel_index(g, r, c));
-        }
-      }
-    }
-    __syncthreads();
-  }
-}
-
 __global__ void __launch_bounds__(256) gather_t_kernel(GatherArgs g) {
   __shared__ double tile[32][33];
   const bool rmw = g.out && g.beta != 0.0;
-#define GBCC_TILES(N, P) (rmw ? gather_tiles<N, P, true>(g, tile) : gather_tiles<N, P, false>(g, tile))
+#define GBCC_TILES(N, P) (rmw ? gather_tiles<N, P, true, 0>(g, tile) : gather_tiles<N, P, false, 0>(g, tile))
   GBCC_GATHER_DISPATCH(g, GBCC_TILES);
 #undef GBCC_TILES
 }
@@ -1091,45 +711,15 @@ void launch_splitk_reduce(int64_t M, int64_t N, int ksplit, const double* partia
 
 void launch_gather(const GatherArgs& g, cudaStream_t st) {
   if (g.Rpad <= 0 || g.Cpad <= 0) return;
-  if (g.transpose) {
-    const int64_t tiles = ((g.Rpad + 31) / 32) * ((g.Cpad + 31) / 32);
-    const int64_t grid = std::min<int64_t>(tiles, 152LL * 16);
-    gather_t_kernel<<<static_cast<unsigned>(grid), dim3(32, 8), 0, st>>>(g);
+  if (g.outs && g.fixed) {
+    launch_gather_fixed(g, st);
     return;
   }
-  bool tables16 = true;
-  for (int t = 0; t < g.nterms; ++t)
-    tables16 = tables16 && reinterpret_cast<uintptr_t>(g.t[t].ca) % 16 == 0 &&
-               (!g.t[t].b || reinterpret_cast<uintptr_t>(g.t[t].cb) % 16 == 0);
-  const bool split_ok = g.outs && g.slice_stride % 4 == 0 && reinterpret_cast<uintptr_t>(g.outs) % 8 == 0;
-  const bool fp64_ok = g.out && reinterpret_cast<uintptr_t>(g.out) % 16 == 0;
-  if ((split_ok || fp64_ok) && tables16 && g.Cpad % 4 == 0 && g.ldo % 4 == 0) {
-    const int64_t nq = g.Cpad / 4;
-    int bx = 32;
-    while (bx < nq && bx < kThreads) bx <<= 1;
-    const int by = kThreads / bx;
-    const int64_t gx = std::min<int64_t>((nq + bx - 1) / bx, 152LL * 64);
-    const int64_t gy = std::min<int64_t>({(g.Rpad + by - 1) / by, std::max<int64_t>(1, 152LL * 64 / gx), 65535LL});
-    const dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy)), block(bx, by);
-    if (g.outs) gather_split4_kernel<<<grid, block, 0, st>>>(g);
-    else gather4_f64_kernel<<<grid, block, 0, st>>>(g);
-    return;
-  }
-  int bx = 1;
-  while (bx < g.Cpad && bx < kThreads) bx <<= 1;
-  if (bx < 32) bx = 32;
-  const int by = kThreads / bx;
-  int64_t gx = (g.Cpad + bx - 1) / bx;
-  int64_t gy = (g.Rpad + by - 1) / by;
-  // cap the grid; the kernel loops over the remainder
-  const int64_t cap_total = 152LL * 64;
-  if (gx > cap_total) gx = cap_total;
-  int64_t gy_cap = std::max<int64_t>(1, cap_total / gx);
-  if (gy > gy_cap) gy = gy_cap;
-  if (gy > 65535) gy = 65535;
-  dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
-  dim3 block(bx, by);
-  gather_kernel<<<grid, block, 0, st>>>(g);
+  const GatherShape sh = gather_shape(g);
+  if (sh.kind == GatherShape::kTiles) gather_t_kernel<<<sh.grid, sh.block, 0, st>>>(g);
+  else if (sh.kind == GatherShape::kFour && g.outs) gather_split4_kernel<<<sh.grid, sh.block, 0, st>>>(g);
+  else if (sh.kind == GatherShape::kFour) gather4_f64_kernel<<<sh.grid, sh.block, 0, st>>>(g);
+  else gather_kernel<<<sh.grid, sh.block, 0, st>>>(g);
 }
 
 void launch_energy_terms(int64_t o, int64_t v, const double* r1, const double* r2,

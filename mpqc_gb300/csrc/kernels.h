@@ -82,7 +82,35 @@ struct GatherArgs {
   int products;
   // 1: some coefficient is not +-2^k (set by gather_finish)
   int general;
+  // split output in fixed point (GBCC_PREC_FP64_TC): 1, the exponent pass --
+  // rowexp[r] = max over the row of the biased FP64 exponent of the packed
+  // value (rowexp zeroed first; nothing stored); 2, the split pass -- every
+  // element of row r in nslices 7-bit digits under that exponent
+  int fixed;
+  unsigned* rowexp;
 };
+
+// Fixed-point slices of the FP64-grade tensor-core contractions.  A row with
+// largest |x| < 2^E is held as X = round(x 2^(7n - E)) in n balanced base-128
+// digits, I_0 in [-128, 128], I_1.. in [-64, 63]; slice p stores I_p 2^(E - 7(p+1))
+// exactly in BF16.  Every product of slices p of A and q of B with p + q = w
+// is then an integer multiple of 2^(E_A + E_B - 7(w + 2)) below 2^14 of it,
+// so FP32 sums of up to 2^10 of them (one TMEM chunk) are exact.
+constexpr int kFixedBits = 7;
+constexpr int kFixedSlices = 6;   // 43 bits below the row's leading power of two
+constexpr int kFixedChunk = 4;    // (k-block, pair) steps per TMEM accumulation: 256 products
+constexpr int kFixedFold = 2;     // chunks summed in FP32 registers before the float-float fold
+// The pairs (p, w - p), both below n, of weight class w; returns their number.
+inline int fixed_class_pairs(int n, int w, int* pa, int* pb) {
+  int k = 0;
+  for (int p = 0; p < n; ++p)
+    if (w - p >= 0 && w - p < n) {
+      pa[k] = p;
+      pb[k] = w - p;
+      ++k;
+    }
+  return k;
+}
 
 inline void gather_set_c4(GatherTerm& T, const int64_t* hca, int64_t n) {
   bool ok = reinterpret_cast<uintptr_t>(T.a) % 16 == 0;
@@ -99,6 +127,9 @@ inline void gather_finish(GatherArgs& g) {
 }
 
 void launch_gather(const GatherArgs& args, cudaStream_t st);
+// one fixed-point pass (args.fixed 1 or 2) of a split pack (pack_fixed.cu);
+// launch_gather forwards to it
+void launch_gather_fixed(const GatherArgs& args, cudaStream_t st);
 
 // out[i] = coef * x[i] as the gather kernels scale a term (exponent arithmetic
 // for power-of-two coefficients)

@@ -24,6 +24,24 @@ __global__ void fp64_fma_probe(double* out, int iters) {
   if (s == 12345.678) out[0] = s;  // keeps the loop alive
 }
 
+// FP64 tensor-core (DMMA) throughput: each warp issues
+// mma.sync.aligned.m8n8k4.row.col.f64 (512 FLOP) on register operands, four
+// independent accumulators deep.
+__global__ void fp64_dmma_probe(double* out, int iters) {
+  const double a = 1.0 + threadIdx.x * 1e-9, b = 0.999999;
+  double c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(c[2 * j]), "+d"(c[2 * j + 1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+  for (int j = 0; j < 8; ++j) s += c[j];
+  if (s == 12345.678) out[0] = s;  // keeps the loop alive
+}
+
 }  // namespace
 
 extern "C" int gbcc_testing_gemm(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
@@ -241,4 +259,193 @@ extern "C" int gbcc_testing_fp64_peak(double* gflops) {
   } catch (const Error& e) {
     return e.status;
   }
+}
+
+extern "C" int gbcc_testing_dmma_peak(double* gflops) {
+  using namespace gbcc;
+  if (!gflops) return GBCC_ERR_INVALID_ARG;
+  try {
+    int dev = 0, sms = 0;
+    GBCC_CK(cudaGetDevice(&dev));
+    GBCC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* out = static_cast<double*>(dev_alloc(sizeof(double)));
+    const int blocks = sms * 4, threads = 256, iters = 1 << 14;
+    fp64_dmma_probe<<<blocks, threads>>>(out, 256);
+    cudaEvent_t e0, e1;
+    GBCC_CK(cudaEventCreate(&e0));
+    GBCC_CK(cudaEventCreate(&e1));
+    GBCC_CK(cudaEventRecord(e0));
+    fp64_dmma_probe<<<blocks, threads>>>(out, iters);
+    GBCC_CK(cudaEventRecord(e1));
+    GBCC_CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    GBCC_CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dev_free(out);
+    const double warps = static_cast<double>(blocks) * threads / 32;
+    *gflops = 512.0 * 4.0 * iters * warps / (ms * 1e-3) / 1e9;
+    return GBCC_OK;
+  } catch (const Error& e) {
+    return e.status;
+  }
+}
+
+namespace {
+
+// Fixed-point pack of a row-major [rows][cols] FP64 matrix into the GEMM's
+// slice panel ([nslices][Cpad/64][rows_pad][64]) through the gather kernels:
+// row exponents zeroed, the exponent pass, the digit pass.
+void fixed_pack(const double* src, int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad, int nslices,
+                unsigned* rowexp, __nv_bfloat16* dst, const int64_t* ra, const int64_t* ca, cudaStream_t st) {
+  using namespace gbcc;
+  GatherArgs g{};
+  g.nterms = 1;
+  gather_set_coef(g.t[0], 1.0);
+  g.t[0].a = src;
+  g.t[0].ra = ra;
+  g.t[0].ca = ca;
+  g.plain = 1;
+  g.R = rows; g.C = cols; g.Rpad = rows_pad; g.Cpad = cols_pad; g.ldo = cols_pad;
+  g.outs = dst; g.nslices = nslices; g.slice_stride = rows_pad * cols_pad;
+  g.rowexp = rowexp;
+  GBCC_CK(cudaMemsetAsync(rowexp, 0, rows_pad * sizeof(unsigned), st));
+  g.fixed = 1;
+  launch_gather(g, st);
+  g.fixed = 2;
+  launch_gather(g, st);
+}
+
+}  // namespace
+
+extern "C" int gbcc_testing_fixed_split(const double* x, int64_t rows, int64_t cols, int nslices, uint16_t* out,
+                                        uint32_t* rowexp) {
+  using namespace gbcc;
+  if (!x || !out || !rowexp || rows < 1 || cols < 1 || nslices < 1 || nslices > kFixedSlices)
+    return GBCC_ERR_INVALID_ARG;
+  std::vector<void*> owned;
+  auto alloc = [&](size_t bytes) {
+    void* p = dev_alloc(bytes);
+    owned.push_back(p);
+    return p;
+  };
+  int status = GBCC_OK;
+  try {
+    const int64_t rows_pad = rup(rows, kTcBM), cols_pad = rup(cols, kTcBK);
+    double* dx = static_cast<double*>(alloc(rows * cols * sizeof(double)));
+    GBCC_CK(cudaMemcpy(dx, x, rows * cols * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<int64_t> hra(rows), hca(cols);
+    for (int64_t r = 0; r < rows; ++r) hra[r] = r * cols;
+    for (int64_t c = 0; c < cols; ++c) hca[c] = c;
+    auto* ra = static_cast<int64_t*>(alloc(rows * sizeof(int64_t)));
+    auto* ca = static_cast<int64_t*>(alloc(cols * sizeof(int64_t)));
+    GBCC_CK(cudaMemcpy(ra, hra.data(), rows * sizeof(int64_t), cudaMemcpyHostToDevice));
+    GBCC_CK(cudaMemcpy(ca, hca.data(), cols * sizeof(int64_t), cudaMemcpyHostToDevice));
+    auto* re = static_cast<unsigned*>(alloc(rows_pad * sizeof(unsigned)));
+    const int64_t n = nslices * rows_pad * cols_pad;
+    auto* panel = static_cast<__nv_bfloat16*>(alloc(n * sizeof(__nv_bfloat16)));
+    fixed_pack(dx, rows, cols, rows_pad, cols_pad, nslices, re, panel, ra, ca, nullptr);
+    GBCC_CK(cudaGetLastError());
+    std::vector<uint16_t> hp(n);
+    GBCC_CK(cudaMemcpy(hp.data(), panel, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    GBCC_CK(cudaMemcpy(rowexp, re, rows * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    // panel element (r, c) of slice s: s * rows_pad * cols_pad + (c / 64) * rows_pad * 64 + r * 64 + c % 64
+    for (int s = 0; s < nslices; ++s)
+      for (int64_t r = 0; r < rows; ++r)
+        for (int64_t c = 0; c < cols; ++c)
+          out[(s * rows + r) * cols + c] = hp[s * rows_pad * cols_pad + (c >> 6) * (rows_pad << 6) + (r << 6) + (c & 63)];
+  } catch (const Error& e) {
+    status = e.status;
+  }
+  for (void* p : owned) dev_free(p);
+  return status;
+}
+
+extern "C" int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
+                                        double* Cout, int bn_req, int ksplit, int repeat, float* ms) {
+  using namespace gbcc;
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || repeat < 1 || ksplit < 1) return GBCC_ERR_INVALID_ARG;
+  if (bn_req != 0 && bn_req != 32 && bn_req != 64 && bn_req != 128) return GBCC_ERR_INVALID_ARG;
+  std::vector<void*> owned;
+  auto alloc = [&](size_t bytes) {
+    void* p = dev_alloc(bytes);
+    owned.push_back(p);
+    return p;
+  };
+  int status = GBCC_OK;
+  try {
+    cudaStream_t st = nullptr;
+    const int nsl = kFixedSlices;
+    const int bn = bn_req ? bn_req : gemm_tc_pick_bn(N, false);
+    const int64_t Mpad = rup(M, kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
+    double* dA = static_cast<double*>(alloc(M * K * sizeof(double)));
+    double* dB = static_cast<double*>(alloc(N * K * sizeof(double)));
+    double* dC = static_cast<double*>(alloc(M * N * sizeof(double)));
+    int* err = static_cast<int*>(alloc(sizeof(int)));
+    GBCC_CK(cudaMemset(err, 0, sizeof(int)));
+    GBCC_CK(cudaMemcpy(dA, A, M * K * sizeof(double), cudaMemcpyHostToDevice));
+    GBCC_CK(cudaMemcpy(dB, B, N * K * sizeof(double), cudaMemcpyHostToDevice));
+    auto table = [&](int64_t n, int64_t stride) {
+      std::vector<int64_t> h(n);
+      for (int64_t i = 0; i < n; ++i) h[i] = i * stride;
+      int64_t* d = static_cast<int64_t*>(alloc(n * sizeof(int64_t)));
+      GBCC_CK(cudaMemcpy(d, h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
+      return d;
+    };
+    const int64_t* cm = table(M, N);
+    const int64_t* cn = table(N, 1);
+    const int64_t* ck = table(K, 1);
+    auto* sa = static_cast<__nv_bfloat16*>(alloc(nsl * Mpad * Kpad * sizeof(__nv_bfloat16)));
+    auto* sb = static_cast<__nv_bfloat16*>(alloc(nsl * Npad * Kpad * sizeof(__nv_bfloat16)));
+    auto* ea = static_cast<unsigned*>(alloc(Mpad * sizeof(unsigned)));
+    auto* eb = static_cast<unsigned*>(alloc(Npad * sizeof(unsigned)));
+    fixed_pack(dA, M, K, Mpad, Kpad, nsl, ea, sa, table(M, K), ck, st);
+    fixed_pack(dB, N, K, Npad, Kpad, nsl, eb, sb, table(N, K), ck, st);
+    GemmTcArgs t{};
+    t.M = M; t.N = N; t.Mpad = Mpad; t.Npad = Npad; t.Kpad = Kpad;
+    t.A = sa; t.a_slices = nsl; t.B = sb; t.b_slices = nsl;
+    t.C = dC; t.cm = cm; t.cn = cn; t.alpha = 1.0; t.bn = bn; t.err = err;
+    t.chunk = kFixedChunk;
+    t.fold = kFixedFold;
+    t.sps = 1;
+    t.group = 1;
+    if (ksplit > 1) {
+      const int64_t kblocks = Kpad / kTcBK;
+      t.kb_per_split = static_cast<int>((kblocks + ksplit - 1) / ksplit);
+      t.ksplit = static_cast<int>((kblocks + t.kb_per_split - 1) / t.kb_per_split);
+      t.partial = static_cast<double*>(alloc(t.ksplit * Mpad * Npad * sizeof(double)));
+    }
+    // one launch per weight class, smallest weight first, as the engine runs them
+    auto run = [&]() {
+      for (int w = nsl - 1; w >= 0; --w) {
+        t.npairs = fixed_class_pairs(nsl, w, t.pa, t.pb);
+        t.beta = w == nsl - 1 ? 0.0 : 1.0;
+        if (!launch_gemm_tc(t, st)) throw Error(GBCC_ERR_CUDA, "tcgen05 launch rejected");
+        if (t.ksplit > 1) launch_splitk_reduce(M, N, t.ksplit, t.partial, Mpad, Npad, dC, cm, cn, 1.0, t.beta, st);
+      }
+    };
+    cudaEvent_t e0, e1;
+    GBCC_CK(cudaEventCreate(&e0));
+    GBCC_CK(cudaEventCreate(&e1));
+    run();
+    GBCC_CK(cudaEventRecord(e0, st));
+    for (int r = 0; r < repeat; ++r) run();
+    GBCC_CK(cudaEventRecord(e1, st));
+    GBCC_CK(cudaEventSynchronize(e1));
+    GBCC_CK(cudaGetLastError());
+    float t_ms = 0.f;
+    GBCC_CK(cudaEventElapsedTime(&t_ms, e0, e1));
+    if (ms) *ms = t_ms / repeat;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int herr = 0;
+    GBCC_CK(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr != kDevOk) status = GBCC_ERR_TIMEOUT;
+    GBCC_CK(cudaMemcpy(Cout, dC, M * N * sizeof(double), cudaMemcpyDeviceToHost));
+  } catch (const Error& e) {
+    std::fprintf(stderr, "gbcc_testing_gemm_fp64tc: %s\n", e.what());
+    status = e.status;
+  }
+  for (void* p : owned) dev_free(p);
+  return status;
 }

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
     for header in ("gbcc.h", "gbcc_scf.h", "gbcc_testing.h"):
         for name in declared_symbols(header):
             assert hasattr(lib, name), name
-    assert lib.gbcc_abi_version() == 5
+    assert lib.gbcc_abi_version() == 6
 
 
 def test_defaults_follow_the_reference(lib):
@@ -47,12 +47,14 @@ def test_defaults_follow_the_reference(lib):
     assert c.target_precision == 1e-9 and c.precision == 0 and c.use_graphs == 2
     assert (c.slices_ladder, c.slices_ring, c.slices_other) == (0, 0, 0) and c.slice_tolerance == 1e-5
     assert c.mixed_switch_precision == 0.0 and c.autotune == 1 and c.refine_reset_diis == 1
+    assert c.refine_precision == 0
 
 
 @pytest.mark.parametrize("field,value", [("o", 0), ("v", -1), ("n_diis", 0), ("n_diis", 17),
                                          ("slices_ladder", 4), ("slices_ring", -1), ("slice_tolerance", 0.0), ("precision", 7), ("max_iter", 0),
                                          ("target_precision", 0.0), ("diis_damp", -1.0),
-                                         ("refine_reset_diis", 2)])
+                                         ("refine_reset_diis", 2), ("refine_precision", 1),
+                                         ("refine_precision", 3), ("precision", 3)])
 def test_create_rejects_bad_config(lib, field, value):
     from mpqc_gb300._lib import Config, GBCC_ERR_INVALID_ARG
     c = Config()

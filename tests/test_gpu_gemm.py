@@ -61,6 +61,10 @@ def test_fp64_probe_runs(tlib):
     g = C.c_double()
     assert tlib.gbcc_testing_fp64_peak(C.byref(g)) == 0
     assert g.value > 10.0
+    d = C.c_double()
+    assert tlib.gbcc_testing_dmma_peak(C.byref(d)) == 0
+    assert d.value > 10.0
+    print(f"FP64 DFMA {g.value:.0f} GFLOP/s, DMMA {d.value:.0f} GFLOP/s")
 
 
 @pytest.mark.parametrize("slices", [0, 3])

@@ -142,13 +142,15 @@ def test_flop_count_matches_contraction_list():
 
 def test_sampled_residual_time_tracks_the_full_residual():
     """The CPU baseline's bounded sample (every contraction of the oracle's
-    residual on a slab of its first output index, scaled back) estimates the
-    time of the full residual to within a factor of two."""
+    residual, operands in the oracle's memory orders, on a slab of its first
+    output index, scaled back) estimates the time of the full residual.  It
+    leaves out the array additions between contractions, so it reads low:
+    measured 0.54-0.61 of the full time at o = 12..16, v = 48..96."""
     import time
     from mpqc_gb300 import synth
     from oracle import ccsd_sample as S
     tr = S.trace()
-    assert len(tr) > 40 and any(spec == "cdij,abcd->abij" for spec, _ in tr)
+    assert len(tr) > 40 and any(spec == "cdij,abcd->abij" for spec, _, _ in tr)
     o, v = 12, 48
     inp = synth.make_inputs(o, v, 40, seed=1, t1_scale=1e-3)
     ints = R.Integrals(inp.Fia, inp.Fij, inp.Fab, inp.Gijab, inp.Gijkl, inp.Giajb, inp.Gijka, inp.Giabc,
@@ -156,7 +158,7 @@ def test_sampled_residual_time_tracks_the_full_residual():
     R.residual(inp.t1, inp.t2, ints)
     full = min(_timed(lambda: R.residual(inp.t1, inp.t2, ints), time) for _ in range(3))
     est = min(S.sampled_seconds(o, v, 0.5, tr)[0] for _ in range(3))
-    assert 0.5 * full < est < 2.0 * full, (full, est)
+    assert 0.35 * full < est < 1.5 * full, (full, est)
 
 
 def _timed(fn, time):
