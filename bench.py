@@ -415,9 +415,9 @@ def ours(args):
 
 def solve_report(args):
     """Whole Jacobi+DIIS solves from t = 0 on one synthetic input: mixed precision
-    (split-BF16 bulk contractions, then plain-FP64 refinement iterations) and plain
-    FP64, with s/iter of each and the mixed result's |dE_corr| and max|dT2|
-    against the FP64 one."""
+    (split-BF16 bulk contractions, then refinement iterations in --refine
+    precision) and plain FP64, with s/iter of each and the mixed result's
+    |dE_corr| and max|dT2| against the FP64 one."""
     import torch
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
@@ -432,7 +432,7 @@ def solve_report(args):
     runs, amps = {}, {}
     for prec in ("mixed",) if args.no_solve_fp64 else ("mixed", "fp64"):
         s = Solver(o, v, precision=prec, slices=(args.slices,) * 3, target_precision=args.solve_precision,
-                   max_iter=args.max_iter, refine_iters=2)
+                   max_iter=args.max_iter, refine_iters=2, refine_precision=args.refine)
         build_inputs(torch, s, o, v, naux, args.seed, dev, b_scale=bs)
         sl_used, sl_err = s.slice_policy()
         t0 = time.perf_counter()
@@ -453,7 +453,8 @@ def solve_report(args):
         log(f"[solve] {prec}: E={e:.12f} iters={rep.iters} ({rep.mixed_iters} mixed) "
             f"converged={rep.converged} {wall:.1f} s")
     line = {"solve": True, "o": o, "v": v, "naux": naux, "b_scale": bs, "seed": args.seed,
-            "flops_per_iter": F, "target_precision": args.solve_precision, "runs": runs,
+            "flops_per_iter": F, "target_precision": args.solve_precision, "refine_precision": args.refine,
+            "runs": runs,
             "data": "synthetic DF-factored integrals, B ~ N(0, b_scale), t = 0 start"}
     if "fp64" in runs:
         m, f = runs["mixed"], runs["fp64"]
@@ -469,13 +470,14 @@ def solve_report(args):
 
 def molecule_report(args):
     """The (H2O)10 / cc-pVDZ target on the GPU, from the geometry: AO integrals,
-    RHF and the AO -> MO transform on the device, then a mixed-precision solve
-    (split-BF16 bulk contractions, FP64 denominators, DIIS, energy, then FP64
-    refinement iterations) and a plain-FP64 solve on the same MO integrals.
-    Reports |dE_corr| of both against the FP64 oracle's energy
-    (tests/golden/h2o10_ccpvdz.json, computed on the CPU by
-    tests/golden/make_h2o10.py), max|dT2| mixed vs FP64, s/iter and TFLOP/s of
-    each path, and the ladder GEMM's fraction of the BF16 tensor peak."""
+    RHF and the AO -> MO transform on the device, then three solves on the
+    same MO integrals: mixed precision (split-BF16 bulk contractions, FP64
+    denominators, DIIS, energy, then two refinement iterations in
+    --refine precision), FP64-grade on the tensor cores throughout (fp64_tc),
+    and plain FP64 (DFMA).  Reports |dE_corr| of each against the FP64
+    oracle's energy (tests/golden/h2o10_ccpvdz.json, computed on the CPU by
+    tests/golden/make_h2o10.py), max|dT2| against the FP64 solve, s/iter and
+    TFLOP/s of each path, and the ladder GEMM's fraction of the BF16 peak."""
     import torch
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
@@ -496,9 +498,9 @@ def molecule_report(args):
     log(f"[h2o{nw}] N={scf.nbf} o={o} v={v}: E_RHF {e_scf:.10f} ({srep.iters} it., ERI {srep.seconds_eri:.2f} s, "
         f"SCF {srep.seconds_scf:.2f} s, wall {time.perf_counter() - t0:.1f} s)")
     runs, amps = {}, {}
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed", "fp64_tc") if args.no_solve_fp64 else ("mixed", "fp64_tc", "fp64"):
         s = Solver(o, v, precision=prec, target_precision=args.solve_precision, max_iter=args.max_iter,
-                   refine_iters=2)
+                   refine_iters=2, refine_precision=args.refine)
         t1 = time.perf_counter()
         scf.ccsd_inputs(s)
         t_in = time.perf_counter() - t1
@@ -531,24 +533,33 @@ def molecule_report(args):
         amps[prec] = a2
         log(f"[h2o{nw}] {prec}: E_corr {e:.12f}, {rep.iters} it. ({rep.mixed_iters} mixed), {wall:.1f} s")
     scf.close()
-    m, f = runs["mixed"], runs["fp64"]
+    m, t = runs["mixed"], runs["fp64_tc"]
     line = {"molecule": f"(H2O){nw}", "basis": "cc-pVDZ", "nbf": srep.nbf, "o": o, "v": v, "frozen_core": False,
             "geometry": f"mpqc_gb300.molecules.water_cluster({nw}, seed=0)", "flops_per_iter": F,
             "e_rhf": e_scf, "scf": {"iters": srep.iters, "eri_s": srep.seconds_eri, "scf_s": srep.seconds_scf,
                                     "one_body_s": srep.seconds_one_body},
-            "target_precision": args.solve_precision, "runs": runs,
-            "abs_dE_mixed_vs_fp64_gpu": abs(m["e_corr"] - f["e_corr"]),
-            "max_abs_dT2_mixed_vs_fp64_gpu": float(np.max(np.abs(amps["mixed"] - amps["fp64"])))}
-    if m["s_per_iter_mixed"] and f["s_per_iter_fp64"]:
+            "target_precision": args.solve_precision, "refine_precision": args.refine, "runs": runs}
+    if m["s_per_iter_mixed"]:
         line["tflops_mixed"] = F / m["s_per_iter_mixed"] / 1e12
-        line["tflops_fp64"] = F / f["s_per_iter_fp64"] / 1e12
-        line["per_iteration_speedup"] = f["s_per_iter_fp64"] / m["s_per_iter_mixed"]
-    line["solve_speedup"] = f["solve_s"] / m["solve_s"]
+    if t["s_per_iter_fp64"]:
+        line["tflops_fp64_tc"] = F / t["s_per_iter_fp64"] / 1e12
+    if "fp64" in runs:
+        f = runs["fp64"]
+        line["abs_dE_mixed_vs_fp64_gpu"] = abs(m["e_corr"] - f["e_corr"])
+        line["abs_dE_fp64_tc_vs_fp64_gpu"] = abs(t["e_corr"] - f["e_corr"])
+        line["max_abs_dT2_mixed_vs_fp64_gpu"] = float(np.max(np.abs(amps["mixed"] - amps["fp64"])))
+        line["max_abs_dT2_fp64_tc_vs_fp64_gpu"] = float(np.max(np.abs(amps["fp64_tc"] - amps["fp64"])))
+        if f["s_per_iter_fp64"]:
+            line["tflops_fp64"] = F / f["s_per_iter_fp64"] / 1e12
+            if m["s_per_iter_mixed"]:
+                line["per_iteration_speedup"] = f["s_per_iter_fp64"] / m["s_per_iter_mixed"]
+        line["solve_speedup_mixed_vs_fp64"] = f["solve_s"] / m["solve_s"]
+        line["solve_speedup_fp64_tc_vs_fp64"] = f["solve_s"] / t["solve_s"]
     if ref:
         line["oracle"] = {"e_rhf": ref["e_rhf"], "e_ccsd_corr": ref["e_ccsd_corr"], "source": fixture.name}
         line["abs_dE_rhf_vs_oracle"] = abs(e_scf - ref["e_rhf"])
-        line["abs_dE_corr_mixed_vs_oracle"] = abs(m["e_corr"] - ref["e_ccsd_corr"])
-        line["abs_dE_corr_fp64_vs_oracle"] = abs(f["e_corr"] - ref["e_ccsd_corr"])
+        for k, r in runs.items():
+            line[f"abs_dE_corr_{k}_vs_oracle"] = abs(r["e_corr"] - ref["e_ccsd_corr"])
     print(json.dumps(line), flush=True)
     return 0
 
@@ -566,7 +577,7 @@ def batch_report(args):
     """Batched many-instance CCSD: `--clusters` water clusters (H2O)n, n in
     1..6, in a polarised Pople basis, every cluster's RHF and MO integrals
     built on the GPU, then all mixed-precision solves (split-BF16 bulk
-    contractions, FP64 denominators, DIIS, FP64 refinement; each stopping at
+    contractions, FP64 denominators, DIIS, --refine refinement; each stopping at
     its own convergence test) in flight together through gbcc_solve_batch.
     Reports clusters/s of the batch (wall clock of the whole batch per step,
     from t = 0 each step) against the same clusters solved one after another,
@@ -588,7 +599,7 @@ def batch_report(args):
             o = scf.nocc()
             v = scf.nbf - o
             s = Solver(o, v, precision="mixed", target_precision=args.solve_precision, max_iter=args.max_iter,
-                       refine_iters=2, autotune=False)
+                       refine_iters=2, refine_precision=args.refine, autotune=False)
             scf.ccsd_inputs(s)
             handles.append(s)
             # the plain-FP64 energy of the same MO integrals, tightly converged
@@ -617,7 +628,8 @@ def batch_report(args):
     dE = [abs(e - ef) for (e, _), (ef, _) in zip(res, ref)]
     iters = [r.iters for _, r in res]
     line = {"workload": f"{len(specs)} water clusters (H2O)n, n in 1..6 from seed {args.seed}, "
-                        f"{args.batch_basis}, mixed-precision CCSD to {args.solve_precision:g}",
+                        f"{args.batch_basis}, mixed-precision CCSD to {args.solve_precision:g}, "
+                        f"2 refinement iterations in {args.refine}",
             "metric": "clusters/s (whole batch, from t = 0)", "value": len(specs) / wall, "unit": "clusters/s",
             "steps": len(walls), "ms_per_step": wall * 1e3,
             "sequential_clusters_per_s": len(specs) / seq_s, "batch_speedup_vs_sequential": seq_s / wall,
@@ -692,6 +704,9 @@ def main():
     ap.add_argument("--solve-precision", type=float, default=1e-8)
     ap.add_argument("--max-iter", type=int, default=40)
     ap.add_argument("--no-solve-fp64", action="store_true")
+    ap.add_argument("--refine", default="fp64_tc", choices=["fp64", "fp64_tc"],
+                    help="precision of the refinement iterations of mixed solves (--solve, h2o10, batch64): "
+                         "fp64_tc, FP64-grade contractions on the tensor cores (default), or plain FP64")
     ap.add_argument("--cpu-frac", type=float, default=1.0 / 16,
                     help="slab of each contraction's first output index timed by the CPU oracle sample")
     ap.add_argument("--gemm", type=lambda s: tuple(int(x) for x in s.split(",")), default=None,

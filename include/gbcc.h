@@ -210,6 +210,9 @@ gbcc_status gbcc_set_direct_inputs(gbcc_handle* h, const gbcc_direct_inputs* in)
  * input arrays (writable, same layouts as gbcc_inputs); the caller fills
  * them on the device and then calls gbcc_commit_inputs, which validates the
  * orbital energies and prepares the contractions as gbcc_set_inputs does.
+ * The commit gives the (ab|cd) storage back (the residual reads only its
+ * pair-symmetric copies): the Gabcd pointer is invalid afterwards, and the
+ * next gbcc_device_inputs allocates it again (zeroed).
  * No counterpart in the reference (its integrals live in TiledArray arrays). */
 gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out);
 gbcc_status gbcc_commit_inputs(gbcc_handle* h);

@@ -584,6 +584,9 @@ void commit_inputs(gbcc_handle* h) {
   h->aux->begin(gbcc::Mode::kExec, GBCC_PREC_FP64);
   gbcc::setup_program(*h->aux, S);
   h->aux->end();
+  // (ab|cd) is read only by the set-up (its pair-symmetric G+/G- copies feed
+  // the ladder): its v^4 storage is given back until inputs are set again
+  if (S.Gabcd) h->eng->release(*S.Gabcd);
   const int req[3] = {h->cfg.slices_ladder, h->cfg.slices_ring, h->cfg.slices_other};
   if (h->cfg.precision == GBCC_PREC_MIXED && (req[0] == 0 || req[1] == 0 || req[2] == 0)) {
     calibrate_slices(h, nullptr, nullptr);
@@ -730,6 +733,7 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
     copy_in(S.Giajb->d, in->Giajb, o * v * o * v, h->stream);
     copy_in(S.Gijka->d, in->Gijka, o * o * o * v, h->stream);
     copy_in(S.Giabc->d, in->Giabc, o * v * v * v, h->stream);
+    h->eng->acquire(*S.Gabcd);
     copy_in(S.Gabcd->d, in->Gabcd, v * v * v * v, h->stream);
     commit_inputs(h);
     return GBCC_OK;
@@ -815,8 +819,9 @@ gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out) {
     if (!h->S.t1) h->S.create(*h->eng, h->cfg.o, h->cfg.v);
     if (h->S.naux > 0 || h->S.nao > 0)
       throw Error(GBCC_ERR_STATE, "gbcc_device_inputs: the handle holds density-fitted or integral-direct inputs");
+    gbcc::CcsdTensors& S = h->S;
+    h->eng->acquire(*S.Gabcd);  // given back by the previous commit
     GBCC_CK(cudaStreamSynchronize(h->stream));  // zero-initialisation done
-    const gbcc::CcsdTensors& S = h->S;
     out->eps_o = S.eps_o->d;
     out->eps_v = S.eps_v->d;
     out->Fia = S.Fia->d;

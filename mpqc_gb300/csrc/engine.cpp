@@ -290,6 +290,22 @@ Tensor& Engine::tensor(const std::string& name, std::initializer_list<int64_t> d
   return ref;
 }
 
+void Engine::release(Tensor& t) {
+  if (!t.d) return;
+  GBCC_CK(cudaStreamSynchronize(stream_));
+  dev_free(t.d);
+  t.d = nullptr;
+  bytes_ -= static_cast<size_t>(t.size()) * sizeof(double);
+}
+
+void Engine::acquire(Tensor& t) {
+  if (t.d) return;
+  const size_t bytes = static_cast<size_t>(t.size()) * sizeof(double);
+  t.d = static_cast<double*>(dev_alloc(bytes));
+  GBCC_CK(cudaMemsetAsync(t.d, 0, bytes, stream_));
+  bytes_ += bytes;
+}
+
 Tensor* Engine::find(const std::string& name) {
   auto it = tensors_.find(name);
   return it == tensors_.end() ? nullptr : it->second.get();

@@ -167,6 +167,10 @@ class Engine {
   // Persistent device tensor owned by the engine (allocated on first request).
   Tensor& tensor(const std::string& name, std::initializer_list<int64_t> dims, bool constant = false);
   Tensor* find(const std::string& name);
+  // Give back a tensor's device storage (d becomes null; plans made while it
+  // was allocated must not run again) and take it again, zeroed.
+  void release(Tensor& t);
+  void acquire(Tensor& t);
 
   // Program passes.  precision: GBCC_PREC_FP64 or GBCC_PREC_MIXED.
   void begin(Mode m, int precision);

@@ -142,6 +142,30 @@ def test_device_pointers_match_host():
     assert np.array_equal(h1, d1.cpu().numpy()) and np.array_equal(h2, d2.cpu().numpy())
 
 
+def test_zero_copy_inputs_twice_match_host_inputs():
+    """gbcc_device_inputs / gbcc_commit_inputs twice on one handle: the commit
+    gives the (ab|cd) storage back and the next gbcc_device_inputs takes it
+    again, so a refill with other integrals gives that input's residual."""
+    torch = pytest.importorskip("torch")
+
+    class _Dev:
+        def __init__(self, ptr, shape):
+            self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f8", "data": (int(ptr), False),
+                                             "version": 3, "strides": None}
+
+    with _solver(synth.make_inputs(4, 13, 12, seed=5, t1_scale=1e-2)) as s:
+        for seed in (6, 7):
+            inp = synth.make_inputs(4, 13, 12, seed=seed, t1_scale=1e-2)
+            ptr = s.device_inputs()
+            arrays = dict(ints_dict(inp), eps_o=inp.eps_o, eps_v=inp.eps_v)
+            for name, x in arrays.items():
+                torch.as_tensor(_Dev(ptr[name], x.shape), device="cuda").copy_(torch.from_numpy(x))
+            s.commit_inputs()
+            r1, r2 = s.residual(inp.t1, inp.t2)
+            r1_ref, r2_ref = R.residual(inp.t1, inp.t2, oracle_ints(inp))
+            assert rel_err(r2, r2_ref) < FP64_TOL and rel_err(r1, r1_ref) < FP64_TOL
+
+
 def test_call_order_and_argument_errors():
     inp = synth.make_inputs(2, 5, 6, seed=1)
     s = Solver(2, 5)
