@@ -13,7 +13,9 @@ Reported (one JSON line):
   value      algorithmic TFLOP/s of the mixed-precision residual, F(o,v) / (s/iter),
              F = 2o^2v^4 + 12o^3v^3 + 4o^4v^2 + 14o^2v^3 + 18o^3v^2, inputs resident in HBM
   e2e        the same through the C ABI with host (pinned) t1/t2 in and r1/r2 out
-  fp64       the plain-FP64 residual on the same inputs (s/iter, TFLOP/s)
+  fp64       the plain-FP64 (DFMA) residual on the same inputs (s/iter, TFLOP/s)
+  fp64_tc    the FP64-grade residual on the tensor cores (fixed-point slices) on
+             the same inputs, with its speed-up and max|dr2| against plain FP64
   roofline   the particle-particle ladder GEMM (dominant kernel) against the BF16 tensor peak
   cpu_baseline  the FP64 oracle on the host cores at the same o, v: each of the
              residual's contractions timed on a slab of its first output index
@@ -365,21 +367,44 @@ def ours(args):
         key = {0: "ladder", 1: "ring", 2: "other", -1: "elementwise"}[p["cls"]]
         terms[key] = terms.get(key, 0.0) + p["ms"]
 
-    # ---- plain FP64 residual on the same inputs
-    fp64 = None
-    if args.fp64_steps > 0:
-        s.residual(t1, t2, r1, r2, precision="fp64")
-        barrier()
-        s.record(4)
-        for _ in range(args.fp64_steps):
-            s.residual(t1, t2, r1, r2, precision="fp64")
-        s.record(5)
-        f_ms = s.elapsed_ms(4, 5) / args.fp64_steps
-        err = float((r2_mixed - r2).abs().max() / r2.abs().max())
-        fp64 = {"s_per_iter": f_ms * 1e-3, "tflops": F / (f_ms * 1e-3) / 1e12, "steps": args.fp64_steps,
-                "warmup": 1, "mixed_speedup": f_ms / ms_step,
-                "mixed_vs_fp64_max_rel_err_r2": err}
     s.close()
+
+    # ---- plain FP64 (DFMA) and FP64-grade tensor-core residuals on the same
+    # inputs, from a second handle (its fixed-point slice packs and the mixed
+    # ones together would not fit in HBM at v = 320)
+    fp64 = fp64_tc = None
+    if args.fp64_steps > 0 or not args.no_fp64_tc:
+        s = Solver(o, v, precision="fp64" if args.no_fp64_tc else "fp64_tc", device=local)
+        build_inputs(torch, s, o, v, naux, args.seed, dev, b_scale=0.05 if args.b_scale is None else args.b_scale)
+        r2_fp64 = None
+        if args.fp64_steps > 0:
+            s.residual(t1, t2, r1, r2, precision="fp64")
+            barrier()
+            s.record(4)
+            for _ in range(args.fp64_steps):
+                s.residual(t1, t2, r1, r2, precision="fp64")
+            s.record(5)
+            f_ms = s.elapsed_ms(4, 5) / args.fp64_steps
+            err = float((r2_mixed - r2).abs().max() / r2.abs().max())
+            fp64 = {"s_per_iter": f_ms * 1e-3, "tflops": F / (f_ms * 1e-3) / 1e12, "steps": args.fp64_steps,
+                    "warmup": 1, "mixed_speedup": f_ms / ms_step,
+                    "mixed_vs_fp64_max_rel_err_r2": err}
+            r2_fp64 = r2.clone()
+        if not args.no_fp64_tc:
+            s.residual(t1, t2, r1, r2, precision="fp64_tc")
+            barrier()
+            s.record(6)
+            for _ in range(args.steps):
+                s.residual(t1, t2, r1, r2, precision="fp64_tc")
+            s.record(7)
+            c_ms = s.elapsed_ms(6, 7) / args.steps
+            fp64_tc = {"s_per_iter": c_ms * 1e-3, "tflops": F / (c_ms * 1e-3) / 1e12, "steps": args.steps,
+                       "warmup": 1, "dtype": "fixed-point bf16x6 (7-bit digits under each row's exponent), exact "
+                                             "FP32 class sums, float-float chunks, f64 I/O"}
+            if r2_fp64 is not None:
+                fp64_tc["speedup_vs_fp64"] = fp64["s_per_iter"] / fp64_tc["s_per_iter"]
+                fp64_tc["max_rel_err_r2_vs_fp64"] = float((r2 - r2_fp64).abs().max() / r2_fp64.abs().max())
+        s.close()
 
     if rank != 0:
         return 0
@@ -403,6 +428,7 @@ def ours(args):
         "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io, "ms_per_step": e2e_ms},
         "fp64": fp64,
+        "fp64_tc": fp64_tc,
         "roofline": roof,
         "term_ms": terms,
         "gpu_launches": launches * args.steps,
@@ -662,15 +688,21 @@ def gemm_probe(args):
     Cm = np.empty((M, N))
     ms = C.c_float()
     sl = args.gemm_slices
-    st = lib.gbcc_testing_gemm_ex3(M, N, K, A.ctypes.data, B.ctypes.data, Cm.ctypes.data, sl, args.gemm_ksplit,
-                                   args.gemm_bn, args.gemm_cta2, args.gemm_chunk, 0, args.gemm_sps,
-                                   args.gemm_group, args.gemm_cmode, args.gemm_repeat, C.byref(ms))
-    pairs = sl * (sl + 1) // 2 if sl > 0 else 1
+    if sl < 0:
+        # FP64-grade: six fixed-point slices, 21 pair products in six class launches
+        st = lib.gbcc_testing_gemm_fp64tc(M, N, K, A.ctypes.data, B.ctypes.data, Cm.ctypes.data, args.gemm_bn,
+                                          args.gemm_ksplit, args.gemm_repeat, C.byref(ms))
+    else:
+        st = lib.gbcc_testing_gemm_ex3(M, N, K, A.ctypes.data, B.ctypes.data, Cm.ctypes.data, sl, args.gemm_ksplit,
+                                       args.gemm_bn, args.gemm_cta2, args.gemm_chunk, 0, args.gemm_sps,
+                                       args.gemm_group, args.gemm_cmode, args.gemm_repeat, C.byref(ms))
+    pairs = 21 if sl < 0 else (sl * (sl + 1) // 2 if sl > 0 else 1)
     flops = 2.0 * M * N * K
     out = {"gemm": True, "M": M, "N": N, "K": K, "slices": sl, "bn": args.gemm_bn, "ksplit": args.gemm_ksplit,
            "cta2": args.gemm_cta2, "sps": args.gemm_sps, "group": args.gemm_group, "cmode": args.gemm_cmode,
            "chunk": args.gemm_chunk, "status": st, "ms": ms.value,
-           "executed_tflops": pairs * flops / (ms.value * 1e-3) / 1e12 if st == 0 and ms.value > 0 else None}
+           "executed_tflops": pairs * flops / (ms.value * 1e-3) / 1e12 if st == 0 and ms.value > 0 else None,
+           "algorithmic_tflops": flops / (ms.value * 1e-3) / 1e12 if st == 0 and ms.value > 0 else None}
     if args.gemm_check and st == 0:
         ref = A @ B.T
         out["max_rel_err"] = float(np.max(np.abs(Cm - ref)) / np.max(np.abs(ref)))
@@ -694,6 +726,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile per contraction (fewer launches before the first residual)")
     ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--no-fp64-tc", action="store_true",
+                    help="skip the FP64-grade tensor-core residual (and its slice packs)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--residual-only", action="store_true",
                     help="profiling driver: run warmup+steps mixed residuals only")
@@ -711,7 +745,8 @@ def main():
                     help="slab of each contraction's first output index timed by the CPU oracle sample")
     ap.add_argument("--gemm", type=lambda s: tuple(int(x) for x in s.split(",")), default=None,
                     metavar="M,N,K", help="profiling aid: time one GEMM shape on the library's kernels")
-    ap.add_argument("--gemm-slices", type=int, default=2, help="BF16 slices (0: plain FP64 kernel)")
+    ap.add_argument("--gemm-slices", type=int, default=2,
+                    help="BF16 slices (0: plain FP64 kernel; -1: the FP64-grade fixed-point path)")
     ap.add_argument("--gemm-bn", type=int, default=0, help="N tile width (0: the heuristic one)")
     ap.add_argument("--gemm-ksplit", type=int, default=1)
     ap.add_argument("--gemm-cta2", type=int, default=0, help="1: CTA-pair (cta_group::2) variant")

@@ -33,7 +33,6 @@ struct gbcc_handle {
   std::unique_ptr<gbcc::Engine> aux;  // one-off setup operations
   gbcc::CcsdTensors S{};
   bool inputs_set = false;
-  bool prepacked = false;
   int* d_err = nullptr;
   double* d_partial = nullptr;  // reduction scratch [kReduceBlocks * 16]
   double* d_out = nullptr;      // reduction results
@@ -188,10 +187,7 @@ bool uses_fp64_tc(const gbcc_handle* h) { return hi_prec(h) == GBCC_PREC_FP64_TC
 // fixed pointers, sizes and tensor maps once the plan is finalised); later
 // evaluations replay it.  Returns the number of kernels it enqueued.
 int enqueue_residual_program(gbcc_handle* h, int precision) {
-  if (precision != GBCC_PREC_FP64 && !h->prepacked) {
-    h->eng->finalize(true);
-    h->prepacked = true;
-  }
+  h->eng->prepack(precision);  // once per plan; no workspace changes
   auto direct = [&]() {
     h->eng->begin(gbcc::Mode::kExec, precision);
     gbcc::residual_program(*h->eng, h->S);
@@ -260,10 +256,7 @@ void ensure_diis(gbcc_handle* h) {
 
 // The residual program of one precision as a (not instantiated) graph.
 cudaGraph_t capture_residual_graph(gbcc_handle* h, int precision) {
-  if (precision != GBCC_PREC_FP64 && !h->prepacked) {
-    h->eng->finalize(true);
-    h->prepacked = true;
-  }
+  h->eng->prepack(precision);
   cudaGraph_t g = nullptr;
   GBCC_CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   try {
@@ -488,17 +481,17 @@ void check_pair_symmetric(gbcc_handle* h) {
 void plan_residual(gbcc_handle* h) {
   drop_graphs(h);
   h->eng->reset_plans();
-  h->prepacked = false;
   h->eng->set_slices(h->slices_used[0], h->slices_used[1], h->slices_used[2]);
   h->eng->set_frozen({h->S.t1, h->S.t2, h->S.tau});
   h->eng->set_emulation(uses_fp64_tc(h));
   h->eng->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
   gbcc::residual_program(*h->eng, h->S);
   h->eng->end();
-  // the split packs of the constant operands for the tensor-core precisions
-  const bool pack = h->cfg.precision != GBCC_PREC_FP64;
-  h->eng->finalize(pack);
-  h->prepacked = pack;
+  // workspaces, then the split packs of the constant operands for the
+  // tensor-core precisions the handle runs (others are packed on first use)
+  h->eng->finalize();
+  if (h->cfg.precision == GBCC_PREC_MIXED) h->eng->prepack(GBCC_PREC_MIXED);
+  if (uses_fp64_tc(h)) h->eng->prepack(GBCC_PREC_FP64_TC);
 }
 
 // Slice counts for the classes configured as 0 (automatic), chosen from their
@@ -580,7 +573,7 @@ void commit_inputs(gbcc_handle* h) {
   h->aux->begin(gbcc::Mode::kPlan, GBCC_PREC_FP64);
   gbcc::setup_program(*h->aux, S);
   h->aux->end();
-  h->aux->finalize(false);
+  h->aux->finalize();
   h->aux->begin(gbcc::Mode::kExec, GBCC_PREC_FP64);
   gbcc::setup_program(*h->aux, S);
   h->aux->end();

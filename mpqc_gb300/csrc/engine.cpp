@@ -937,7 +937,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
           }
         }
         if (op.constant) {
-          op.pack_elems = need;  // allocated and packed by finalize(true)
+          op.pack_elems = need;  // allocated and packed by prepack()
         } else if (side == 0) {
           wsbf_a_ = std::max(wsbf_a_, need);
         } else {
@@ -991,7 +991,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
   }
 }
 
-void Engine::finalize(bool prepack) {
+void Engine::finalize() {
   if (!planned_) throw Error(GBCC_ERR_STATE, "engine: finalize before PLAN");
   dev_free(w64a_);
   dev_free(w64b_);
@@ -1019,26 +1019,31 @@ void Engine::finalize(bool prepack) {
       kv.second[i]->cache_buf = first->cache_buf;
     }
   }
-  if (prepack) {
-    for (auto& sp : sites_) {
-      if (sp->kind != 1) continue;
-      for (int pi = 1; pi < (emu_ ? 3 : 2); ++pi) {
-        GemmPlan& p = sp->plan[pi];
-        if (!p.use_tc) continue;
-        for (int side = 0; side < 2; ++side) {
-          OperandPlan& op = p.P[side];
-          if (!op.constant) continue;
-          if (!op.packed) {
-            op.packed = static_cast<__nv_bfloat16*>(dev_alloc(op.pack_elems * sizeof(__nv_bfloat16)));
-            owned_.push_back(op.packed);
-            bytes_ += op.pack_elems * sizeof(__nv_bfloat16);
-          }
-          pack_panel(op, op.packed);
-        }
+  packed_[0] = packed_[1] = packed_[2] = false;
+}
+
+void Engine::prepack(int precision) {
+  const int pi = plan_index(precision);
+  if (!planned_) throw Error(GBCC_ERR_STATE, "engine: prepack before PLAN");
+  if (pi == 0 || packed_[pi]) return;
+  if (pi == 2 && !emu_) throw Error(GBCC_ERR_STATE, "engine: no FP64_TC plan");
+  for (auto& sp : sites_) {
+    if (sp->kind != 1) continue;
+    GemmPlan& p = sp->plan[pi];
+    if (!p.use_tc) continue;
+    for (int side = 0; side < 2; ++side) {
+      OperandPlan& op = p.P[side];
+      if (!op.constant) continue;
+      if (!op.packed) {
+        op.packed = static_cast<__nv_bfloat16*>(dev_alloc(op.pack_elems * sizeof(__nv_bfloat16)));
+        owned_.push_back(op.packed);
+        bytes_ += op.pack_elems * sizeof(__nv_bfloat16);
       }
+      pack_panel(op, op.packed);
     }
-    GBCC_CK(cudaGetLastError());
   }
+  GBCC_CK(cudaGetLastError());
+  packed_[pi] = true;
 }
 
 }  // namespace gbcc

@@ -177,9 +177,12 @@ class Engine {
   void end();
   bool planned() const { return planned_; }
   void reset_plans();  // inputs changed: rebuild everything on the next PLAN
-  // After a PLAN pass: allocate workspaces; pack the constant operands of the
-  // tensor-core plans (MIXED, and FP64_TC where planned).
-  void finalize(bool prepack);
+  // After a PLAN pass: allocate the workspaces of every plan (once: EXEC
+  // passes captured into graphs keep their pointers).
+  void finalize();
+  // Split packs of the constant operands of one tensor-core plan (MIXED or
+  // FP64_TC), made once per PLAN; dedicated buffers, no workspace changes.
+  void prepack(int precision);
 
   // C = beta*C + sum_t coef_t * a_t (* b_t); labels of each factor must be a
   // subset of C's labels (missing labels broadcast).
@@ -244,6 +247,7 @@ class Engine {
   int chunk_lo_ = 24;
   bool profile_ = false;
   bool emu_ = false;
+  bool packed_[3] = {false, false, false};
   std::unordered_set<const Tensor*> frozen_;
   std::unordered_map<std::string, std::vector<struct OperandPlan*>> pack_uses_;
   double flops_ = 0.0;
