@@ -399,7 +399,7 @@ def ours(args):
             s.record(7)
             c_ms = s.elapsed_ms(6, 7) / args.steps
             fp64_tc = {"s_per_iter": c_ms * 1e-3, "tflops": F / (c_ms * 1e-3) / 1e12, "steps": args.steps,
-                       "warmup": 1, "dtype": "fixed-point bf16x6 (7-bit digits under each row's exponent), exact "
+                       "warmup": 1, "dtype": "fixed-point bf16x6 (8-bit digits under each row's exponent), exact "
                                              "FP32 class sums, float-float chunks, f64 I/O"}
             if r2_fp64 is not None:
                 fp64_tc["speedup_vs_fp64"] = fp64["s_per_iter"] / fp64_tc["s_per_iter"]
@@ -691,7 +691,7 @@ def gemm_probe(args):
     if sl < 0:
         # FP64-grade: six fixed-point slices, 21 pair products in six class launches
         st = lib.gbcc_testing_gemm_fp64tc(M, N, K, A.ctypes.data, B.ctypes.data, Cm.ctypes.data, args.gemm_bn,
-                                          args.gemm_ksplit, args.gemm_repeat, C.byref(ms))
+                                          args.gemm_ksplit, args.gemm_cta2, args.gemm_repeat, C.byref(ms))
     else:
         st = lib.gbcc_testing_gemm_ex3(M, N, K, A.ctypes.data, B.ctypes.data, Cm.ctypes.data, sl, args.gemm_ksplit,
                                        args.gemm_bn, args.gemm_cta2, args.gemm_chunk, 0, args.gemm_sps,

@@ -57,9 +57,9 @@ typedef enum gbcc_precision {
   GBCC_PREC_FP64 = 0,        /* every contraction in plain FP64                                */
   GBCC_PREC_MIXED = 1,       /* split-BF16 tensor-core contractions, FP64 elsewhere            */
   GBCC_PREC_FP64_TC = 2      /* FP64-grade contractions on the BF16 tensor cores: each operand */
-                             /* row in six 7-bit fixed-point slices under its largest         */
+                             /* row in six 8-bit fixed-point slices under its largest         */
                              /* exponent; slice products of one weight summed exactly in FP32,*/
-                             /* float-float across chunks (error ~2^-42 of row max x row max) */
+                             /* float-float across chunks (error ~2^-47 of row max x row max) */
 } gbcc_precision;
 
 typedef struct gbcc_config {

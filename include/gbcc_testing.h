@@ -71,9 +71,10 @@ int gbcc_testing_fixed_split(const double* x, int64_t rows, int64_t cols, int ns
 /* C[M][N] = A[M][K] B[N][K]^T through the FP64-grade tensor-core path: six
  * fixed-point slices per operand row, one tcgen05 launch per weight class
  * (bn 0: the heuristic tile width; 32, 64 or 128), K split over CTAs when
- * ksplit > 1.  *ms: the time of one product (all class launches). */
+ * ksplit > 1, CTA pairs (cta_group::2, 256-row tiles; bn 64 or 128) when
+ * cta2.  *ms: the time of one product (all class launches). */
 int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
-                             int bn, int ksplit, int repeat, float* ms);
+                             int bn, int ksplit, int cta2, int repeat, float* ms);
 
 /* Peak probe: FP64 tensor-core throughput (mma.sync m8n8k4 .f64, DMMA) in
  * GFLOP/s, register operands over all SMs. */

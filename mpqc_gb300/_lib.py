@@ -155,7 +155,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_testing_fixed_split.argtypes = [vp, C.c_int64, C.c_int64, C.c_int, vp, vp]
     lib.gbcc_testing_gemm_fp64tc.restype = C.c_int
     lib.gbcc_testing_gemm_fp64tc.argtypes = [C.c_int64, C.c_int64, C.c_int64, vp, vp, vp, C.c_int, C.c_int, C.c_int,
-                                             C.POINTER(C.c_float)]
+                                             C.c_int, C.POINTER(C.c_float)]
     ip = C.POINTER(C.c_int)
     lib.gbcc_testing_profile_residual.restype = C.c_int
     lib.gbcc_testing_profile_residual.argtypes = [vp, C.c_int, C.c_int, dp, dp, ip, ip, ip]

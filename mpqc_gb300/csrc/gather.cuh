@@ -90,26 +90,29 @@ __device__ __forceinline__ unsigned exp_field(double x) {
   return e == 0x7FFu ? 0u : e;
 }
 
-// BF16 bits of I 2^k for |I| <= 128, the biased BF16 exponent of 2^k being
+// BF16 bits of I 2^k for |I| <= 256, the biased BF16 exponent of 2^k being
 // `base` (exact: |I| has at most 8 significant bits); flushed to zero below
 // BF16's normal range
 __device__ __forceinline__ unsigned short bf16_int_pow2(int I, int base) {
   if (I == 0) return 0;
   const unsigned sign = I < 0 ? 0x8000u : 0u;
   const unsigned a = static_cast<unsigned>(I < 0 ? -I : I);
-  const int L = 31 - __clz(static_cast<int>(a));
+  const int L = 31 - __clz(static_cast<int>(a));  // 0..8
   const int be = base + L;
   if (be <= 0) return static_cast<unsigned short>(sign);
   if (be >= 255) return static_cast<unsigned short>(sign | 0x7F80u);
-  return static_cast<unsigned short>(sign | (static_cast<unsigned>(be) << 7) | ((a << (7 - L)) & 0x7Fu));
+  const unsigned mant = (L <= 7 ? (a << (7 - L)) : (a >> (L - 7))) & 0x7Fu;
+  return static_cast<unsigned short>(sign | (static_cast<unsigned>(be) << 7) | mant);
 }
 
 // x as n fixed-point digits under the row exponent eb (the biased FP64
-// exponent of the row's largest |x|, so |x| < 2^E, E = eb - 1022), integer
-// operations only: X = round(x 2^(7n - E)) from the 53-bit significand (|X| <=
-// 2^(7n)), then balanced base-128 digits from the least significant up; slice
-// p = I_p 2^(E - 7(p+1)), whose biased BF16 exponent base is eb - 902 - 7p.
-// Zeros and subnormals give zero slices; infinities and NaN pass to slice 0.
+// exponent of the row's largest |x|, so |x| < 2^(E-1) with E = eb - 1021: one
+// bit of headroom keeps the leading digit within [-128, 128]), integer
+// operations only: X = round(x 2^(8n - E)) from the 53-bit significand (|X| <=
+// 2^(8n-1)), then balanced base-256 digits from the least significant up;
+// slice p = I_p 2^(E - 8(p+1)), whose biased BF16 exponent base is
+// eb - 902 - 8p.  Zeros and subnormals give zero slices; infinities and NaN
+// pass to slice 0.
 __device__ __forceinline__ void fixed_split(double x, unsigned eb, int n, unsigned short* out) {
 #pragma unroll
   for (int p = 0; p < kFixedSlices; ++p) out[p] = 0;
@@ -120,7 +123,7 @@ __device__ __forceinline__ void fixed_split(double x, unsigned eb, int n, unsign
     return;
   }
   if (e == 0 || eb == 0u) return;
-  const int sh = 53 + (static_cast<int>(eb) - e) - kFixedBits * n;  // >= 53 - 7n >= 11
+  const int sh = 54 + (static_cast<int>(eb) - e) - kFixedBits * n;  // >= 54 - 8n >= 6
   if (sh > 62) return;
   const long long m = static_cast<long long>((u & 0xFFFFFFFFFFFFFull) | (1ull << 52));
   long long X = (m + (1ll << (sh - 1))) >> sh;
@@ -129,9 +132,9 @@ __device__ __forceinline__ void fixed_split(double x, unsigned eb, int n, unsign
 #pragma unroll
   for (int p = kFixedSlices - 1; p >= 1; --p) {
     if (p >= n) continue;
-    const long long r = ((X + 64) & 127) - 64;
+    const long long r = ((X + 128) & 255) - 128;
     d[p] = static_cast<int>(r);
-    X = (X - r) >> 7;
+    X = (X - r) >> 8;
   }
   d[0] = static_cast<int>(X);
 #pragma unroll

@@ -85,20 +85,23 @@ struct GatherArgs {
   // split output in fixed point (GBCC_PREC_FP64_TC): 1, the exponent pass --
   // rowexp[r] = max over the row of the biased FP64 exponent of the packed
   // value (rowexp zeroed first; nothing stored); 2, the split pass -- every
-  // element of row r in nslices 7-bit digits under that exponent
+  // element of row r in nslices 8-bit digits under that exponent
   int fixed;
   unsigned* rowexp;
 };
 
 // Fixed-point slices of the FP64-grade tensor-core contractions.  A row with
-// largest |x| < 2^E is held as X = round(x 2^(7n - E)) in n balanced base-128
-// digits, I_0 in [-128, 128], I_1.. in [-64, 63]; slice p stores I_p 2^(E - 7(p+1))
-// exactly in BF16.  Every product of slices p of A and q of B with p + q = w
-// is then an integer multiple of 2^(E_A + E_B - 7(w + 2)) below 2^14 of it,
-// so FP32 sums of up to 2^10 of them (one TMEM chunk) are exact.
-constexpr int kFixedBits = 7;
-constexpr int kFixedSlices = 6;   // 43 bits below the row's leading power of two
-constexpr int kFixedChunk = 4;    // (k-block, pair) steps per TMEM accumulation: 256 products
+// largest |x| < 2^(E-1) is held as X = round(x 2^(8n - E)), |X| <= 2^(8n-1),
+// in n balanced base-256 digits, every one in [-128, 128]; slice p stores
+// I_p 2^(E - 8(p+1)) exactly in BF16 (at most 8 significant bits).  Every
+// product of slices p of A and q of B with p + q = w is then an integer
+// multiple of 2^(E_A + E_B - 8(w + 2)) of magnitude at most 2^14 of it, so
+// FP32 sums of up to 2^10 of them stay within 2^24 units and are exact: one
+// TMEM chunk (8 (k-block, pair) steps, 512 products) and the FP32 register
+// sum of two chunks before each float-float fold.
+constexpr int kFixedBits = 8;
+constexpr int kFixedSlices = 6;   // 47 bits below the row's leading power of two
+constexpr int kFixedChunk = 8;    // (k-block, pair) steps per TMEM accumulation: 512 products
 constexpr int kFixedFold = 2;     // chunks summed in FP32 registers before the float-float fold
 // The pairs (p, w - p), both below n, of weight class w; returns their number.
 inline int fixed_class_pairs(int n, int w, int* pa, int* pb) {

@@ -362,10 +362,11 @@ extern "C" int gbcc_testing_fixed_split(const double* x, int64_t rows, int64_t c
 }
 
 extern "C" int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
-                                        double* Cout, int bn_req, int ksplit, int repeat, float* ms) {
+                                        double* Cout, int bn_req, int ksplit, int cta2, int repeat, float* ms) {
   using namespace gbcc;
   if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || repeat < 1 || ksplit < 1) return GBCC_ERR_INVALID_ARG;
   if (bn_req != 0 && bn_req != 32 && bn_req != 64 && bn_req != 128) return GBCC_ERR_INVALID_ARG;
+  if (cta2 && bn_req != 64 && bn_req != 128) return GBCC_ERR_INVALID_ARG;
   std::vector<void*> owned;
   auto alloc = [&](size_t bytes) {
     void* p = dev_alloc(bytes);
@@ -377,7 +378,7 @@ extern "C" int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const d
     cudaStream_t st = nullptr;
     const int nsl = kFixedSlices;
     const int bn = bn_req ? bn_req : gemm_tc_pick_bn(N, false);
-    const int64_t Mpad = rup(M, kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
+    const int64_t Mpad = rup(M, cta2 ? 2 * kTcBM : kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
     double* dA = static_cast<double*>(alloc(M * K * sizeof(double)));
     double* dB = static_cast<double*>(alloc(N * K * sizeof(double)));
     double* dC = static_cast<double*>(alloc(M * N * sizeof(double)));
@@ -409,6 +410,7 @@ extern "C" int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const d
     t.fold = kFixedFold;
     t.sps = 1;
     t.group = 1;
+    t.cta2 = cta2 ? 1 : 0;
     if (ksplit > 1) {
       const int64_t kblocks = Kpad / kTcBK;
       t.kb_per_split = static_cast<int>((kblocks + ksplit - 1) / ksplit);
