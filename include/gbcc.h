@@ -279,6 +279,18 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
 gbcc_status gbcc_solve_batch(gbcc_handle* const* handles, int32_t count, double* e_corr, gbcc_report* reports,
                              gbcc_status* statuses);
 
+/* Perturbative triples correction (T) of closed-shell CCSD: the reference's
+ * CCSD_T::compute_ccsd_t (src/mpqc/chemistry/qc/lcao/cc/ccsd_t.h:143-172)
+ * with its "straight" approach (:1127-1167, denominators :2274-2333), from
+ * t1/t2 (host or device pointers in gbcc_residual's layouts; NULL: the
+ * amplitudes of the handle's last gbcc_solve) and the handle's <ij|ab>,
+ * <ij|ka>, <ia|bc> and orbital energies.  precision (gbcc_precision) sets the
+ * arithmetic of the o^3 v^4 contractions -- GBCC_PREC_FP64, MIXED (three
+ * BF16 slices) or FP64_TC; the energy sums are FP64.  *e_t receives E(T);
+ * the CCSD(T) energy is the CCSD energy plus E(T) (ccsd_t.h:183-195). */
+gbcc_status gbcc_triples(gbcc_handle* h, int32_t precision, const double* t1_ai, const double* t2_abij,
+                         double* e_t);
+
 /* Release the handle and all its device memory.  NULL is accepted. */
 gbcc_status gbcc_destroy(gbcc_handle* h);
 

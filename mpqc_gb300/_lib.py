@@ -28,7 +28,7 @@ EXPORTS = (
     "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error", "gbcc_set_amplitudes",
     "gbcc_save_amplitudes", "gbcc_load_amplitudes", "gbcc_set_df_inputs", "gbcc_set_direct_inputs",
-    "gbcc_solve_batch",
+    "gbcc_solve_batch", "gbcc_triples",
 )
 # every symbol include/gbcc_scf.h declares
 SCF_EXPORTS = (
@@ -183,6 +183,8 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_energy_noalloc.argtypes = [C.c_int64, C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.gbcc_solve.restype = C.c_int
     lib.gbcc_solve.argtypes = [vp, vp, vp, dp, C.POINTER(Report)]
+    lib.gbcc_triples.restype = C.c_int
+    lib.gbcc_triples.argtypes = [vp, i32, vp, vp, dp]
     lib.gbcc_solve_batch.restype = C.c_int
     lib.gbcc_solve_batch.argtypes = [C.POINTER(vp), i32, dp, C.POINTER(Report), C.POINTER(C.c_int)]
     lib.gbcc_destroy.restype = C.c_int

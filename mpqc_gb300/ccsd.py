@@ -271,6 +271,16 @@ class Solver:
         _check(self.lib, self.h, self.lib.gbcc_load_amplitudes(self.h, str(path).encode(), C.byref(e)))
         return e.value
 
+    def triples(self, precision="mixed", t1=None, t2=None):
+        """E(T), the perturbative triples correction (``gbcc_triples``; the
+        reference's CCSD_T, ccsd_t.h:143-172) from t1/t2 or, when they are
+        None, from the amplitudes of the last ``solve()``.  ``precision``
+        ("fp64", "mixed", "fp64_tc") sets the arithmetic of the o^3 v^4
+        contractions; the energy sums are FP64."""
+        e = C.c_double()
+        _check(self.lib, self.h, self.lib.gbcc_triples(self.h, _PRECS[precision], _ptr(t1), _ptr(t2), C.byref(e)))
+        return e.value
+
     def solve(self, want_amplitudes=True):
         o, v = self.o, self.v
         t1 = np.empty((v, o)) if want_amplitudes else None

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/gbcc.h"
+#include "triples.h"
 #include "../../include/gbcc_testing.h"
 #include "ccsd_program.h"
 #include "engine.h"
@@ -1100,6 +1101,40 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
     if (report) *report = rep;
     if (c.verbose) std::printf("CCSD Energy  %.15f\n", E1);
     return converged ? GBCC_OK : GBCC_ERR_NOT_CONVERGED;
+  });
+}
+
+gbcc_status gbcc_triples(gbcc_handle* h, int32_t precision, const double* t1_ai, const double* t2_abij,
+                         double* e_t) {
+  return guarded(h, [&]() -> gbcc_status {
+    if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "gbcc_triples: inputs not set");
+    if (precision != GBCC_PREC_FP64 && precision != GBCC_PREC_MIXED && precision != GBCC_PREC_FP64_TC)
+      throw Error(GBCC_ERR_INVALID_ARG, "gbcc_triples: bad precision");
+    if (!e_t) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_triples: NULL e_t");
+    if ((t1_ai == nullptr) != (t2_abij == nullptr))
+      throw Error(GBCC_ERR_INVALID_ARG, "gbcc_triples: give both amplitudes or neither");
+    gbcc::CcsdTensors& S = h->S;
+    if (t1_ai) {
+      h->have_solution = false;
+      copy_in(S.t1->d, t1_ai, n1_of(h), h->stream);
+      copy_in(S.t2->d, t2_abij, n2_of(h), h->stream);
+      check_pair_symmetric(h);
+    } else if (!h->have_solution) {
+      throw Error(GBCC_ERR_STATE, "gbcc_triples: no amplitudes given and no solve to take them from");
+    }
+    gbcc::TriplesInputs in;
+    in.o = h->cfg.o;
+    in.v = h->cfg.v;
+    in.t1 = S.t1->d;
+    in.t2 = S.t2->d;
+    in.Gijab = S.Gijab->d;
+    in.Gijka = S.Gijka->d;
+    in.Giabc = S.Giabc->d;
+    in.eps_o = S.eps_o->d;
+    in.eps_v = S.eps_v->d;
+    *e_t = gbcc::triples_energy(in, precision, h->stream, h->d_err);
+    sync_check(h);
+    return GBCC_OK;
   });
 }
 

@@ -429,6 +429,9 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
     if (lane == 0) {
       prefetch_tmap(&tmA);
       prefetch_tmap(&tmB);
+      // first panel row of the operands (a window of a larger panel); rows
+      // past the panel's end load as zeros, rows past M or N are not stored
+      const int a_row0 = static_cast<int>(g.a_row0), b_row0 = static_cast<int>(g.b_row0);
       uint32_t gi = 0;  // stage-use counter across tiles
       bool ok = true;
       // stage-ring position kept incrementally (no divisions in the loop)
@@ -450,19 +453,21 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
             // the leader's full barrier counts the bytes of both CTAs
             const uint32_t bar = full0 + static_cast<uint32_t>(s) * 8u;
             if (leader) mbar_expect_tx(&full[s], 2 * Cfg::kStageBytes);
-            tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kAStage, 0, m0, g.pa[pr] * kblocks + kb);
-            tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBStage, 0, nb0, g.pb[pr] * kblocks + kb);
+            tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kAStage, 0, m0 + a_row0, g.pa[pr] * kblocks + kb);
+            tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBStage, 0, nb0 + b_row0, g.pb[pr] * kblocks + kb);
           } else if constexpr (SPS == 1) {
             mbar_expect_tx(&full[s], Cfg::kStageBytes);
-            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage, 0, m0, g.pa[pr] * kblocks + kb);
-            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage, 0, nb0, g.pb[pr] * kblocks + kb);
+            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage, 0, m0 + a_row0, g.pa[pr] * kblocks + kb);
+            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage, 0, nb0 + b_row0, g.pb[pr] * kblocks + kb);
           } else {
             // every slice of A and B of this k-block
             mbar_expect_tx(&full[s], Cfg::kStageBytes);
 #pragma unroll
             for (int j = 0; j < SPS; ++j) {
-              tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage + j * Cfg::kABytes, 0, m0, j * kblocks + kb);
-              tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage + j * Cfg::kBBytes, 0, nb0, j * kblocks + kb);
+              tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage + j * Cfg::kABytes, 0, m0 + a_row0,
+                          j * kblocks + kb);
+              tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage + j * Cfg::kBBytes, 0, nb0 + b_row0,
+                          j * kblocks + kb);
             }
           }
           if (SPS > 1 || ++pr == g.npairs) {
@@ -937,6 +942,8 @@ bool launch_gemm_tc(const GemmTcArgs& g, cudaStream_t st) {
     return false;
   if (g.Mpad > (1LL << 31) - 1 || g.Npad > (1LL << 31) - 1 || g.Kpad > (1LL << 31) - 1) return false;
   if ((g.a_rows && g.a_rows < g.Mpad) || (g.b_rows && g.b_rows < g.Npad)) return false;
+  if (g.a_row0 < 0 || g.b_row0 < 0 || g.a_row0 + g.Mpad > (1LL << 31) - 1 || g.b_row0 + g.Npad > (1LL << 31) - 1)
+    return false;
   if ((g.Npad / g.bn) * (g.Mpad / BM) * (g.ksplit > 1 ? g.ksplit : 1) > (1LL << 31) - 1) return false;
   if (g.ksplit > 1 && (!g.partial || g.kb_per_split < 1 ||
                        static_cast<int64_t>(g.ksplit - 1) * g.kb_per_split >= g.Kpad / BK))

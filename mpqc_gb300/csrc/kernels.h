@@ -209,6 +209,9 @@ struct GemmTcArgs {
   // (CTAs working at the same time then share fewer, wider operand panels in
   // L2); 0 or 1: N fastest over whole rows of tiles
   int group;
+  // first row of A / B within their panels (a window of a larger panel:
+  // rows past the panel's end load as zeros; 0 for whole panels)
+  int64_t a_row0, b_row0;
 };
 // Deterministic K-split reduction: C[cm[m] + cn[n]] = beta*C + alpha * sum_s
 // partial[s][m][n] (splits summed in order), partial rows of length ldp and

@@ -663,3 +663,54 @@ def mo_blocks_inplace(scf: RHFResult, G, n_frozen, chunk=8):
     )
     eps = np.diag(Fmo)
     return blocks, eps[:o].copy(), eps[o:].copy()
+
+
+def df_factors_c(mol: Molecule, obs: str, dfbs: str):
+    """Density-fitting factors of the two-electron integrals in the Coulomb
+    metric: B[K, mu, nu] = sum_Q (P|Q)^(-1/2)[K,Q] (Q|mu nu), so that
+    (mu nu|la si) ~ sum_K B[K,mu,nu] B[K,la,si] -- the "[df]" integrals of
+    the reference's LCAO factory ((K|G|p q)[inv_sqr], lcao_factory.h) and of
+    its RI-RHF.  The orbital basis is normalised as in ``ao_integrals_c``; the
+    fitting functions' normalisation cancels.  The three- and two-centre
+    integrals come from the C restatement's four-centre routine with a unit
+    s function (exponent 0) next to each fitting function: (P 1|mu nu) and
+    (P 1|Q 1).  Small molecules only: it fills an (N + Naux + 1)^4 array.
+    Returns (S, H, B) with S and H of the orbital basis."""
+    lib = _ints_lib()
+    o_sh = build_shells(mol, obs)
+    a_sh = build_shells(mol, dfbs)
+    if any(s.pure and s.l >= 2 for s in a_sh) and any(not s.pure and s.l >= 2 for s in o_sh):
+        raise ValueError("the C routine takes one pure flag: Cartesian d in the orbital basis "
+                         "and spherical d in the fitting basis cannot be combined")
+    pure = any(s.pure for s in a_sh)
+    unit = Shell(0, np.array(mol.coords[0], dtype=float), np.array([0.0]), np.array([1.0]), pure)
+    shells = [Shell(s.l, s.center, s.exps, s.coefs, pure) for s in o_sh + a_sh] + [unit]
+    args, keep = _flat_shells(shells)
+    nf = sum(s.nfunc for s in o_sh)
+    na = sum(s.nfunc for s in a_sh)
+    n = nf + na + 1
+    G = np.empty((n, n, n, n))
+    import ctypes as C
+    lib.eri_sph(*args, G.ctypes.data_as(C.POINTER(C.c_double)))
+    del keep
+    S, H, _ = ao_integrals_c(mol, obs, eri=False)
+    # ao_integrals_c scales each orbital-basis function to unit self-overlap;
+    # the same factors from the raw overlap of the orbital shells
+    S_raw = np.zeros((nf, nf))
+    T_raw = np.zeros((nf, nf))
+    V_raw = np.zeros((nf, nf))
+    oargs, okeep = _flat_shells(o_sh)
+    Zn = np.array([float(Z_OF[s]) for s in mol.symbols])
+    xyz = np.ascontiguousarray(mol.coords, dtype=float)
+    dp = C.POINTER(C.c_double)
+    lib.oneint_sph(*oargs, len(mol.symbols), Zn.ctypes.data_as(dp), xyz.ctypes.data_as(dp),
+                   S_raw.ctypes.data_as(dp), T_raw.ctypes.data_as(dp), V_raw.ctypes.data_as(dp))
+    del okeep
+    d = 1.0 / np.sqrt(np.diag(S_raw))
+    P3 = G[nf:nf + na, n - 1, :nf, :nf] * d[None, :, None] * d[None, None, :]   # (P|mu nu)
+    M = G[nf:nf + na, n - 1, nf:nf + na, n - 1]                                   # (P|Q)
+    M = 0.5 * (M + M.T)
+    w, U = np.linalg.eigh(M)
+    Minv_half = (U / np.sqrt(w)) @ U.T
+    B = np.einsum("kq,qmn->kmn", Minv_half, P3)
+    return S, H, B
