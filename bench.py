@@ -24,7 +24,8 @@ Reported (one JSON line):
 --impl reference times the FP64 CPU oracle (the restatement of the reference's
 CPU path; the reference itself cannot be built here) the same way, on the
 same workload and config as this arm.
---config h2o10 runs (H2O)10 / cc-pVDZ from the geometry (mixed and FP64 solves).
+--config h2o10 runs (H2O)10 / cc-pVDZ from the geometry (mixed, FP64-grade
+tensor-core and FP64 solves, and the (T) correction of the mixed solve).
 --config batch64 solves 64 water clusters (H2O)1..6 together (clusters/s).
 Multi-GPU (torchrun): every rank runs an independent replica ("replicas only",
 weak scaling); value = sum of all ranks' FLOPs / max rank time.
@@ -539,6 +540,13 @@ def molecule_report(args):
                "fp64_iters": rep.fp64_iters, "solve_s": wall, "inputs_s": t_in,
                "s_per_iter_mixed": rep.seconds_residual_mixed or None,
                "s_per_iter_fp64": rep.seconds_residual_fp64 or None}
+        if prec == "mixed" or (prec == "fp64_tc" and args.triples_fp64_tc):
+            # (T) of the converged amplitudes on this handle, in the solve's arithmetic
+            t3 = time.perf_counter()
+            e_t = s.triples("mixed" if prec == "mixed" else "fp64_tc")
+            run["triples"] = {"e_t": e_t, "seconds": time.perf_counter() - t3,
+                              "precision": "mixed" if prec == "mixed" else "fp64_tc"}
+            log(f"[h2o{nw}] (T) {run['triples']['precision']}: {e_t:.12f} in {run['triples']['seconds']:.1f} s")
         if prec == "mixed":
             sl, se = s.slice_policy()
             run["slices"], run["slice_rel_change_vs_3"] = list(sl), list(se)
@@ -581,6 +589,8 @@ def molecule_report(args):
                 line["per_iteration_speedup"] = f["s_per_iter_fp64"] / m["s_per_iter_mixed"]
         line["solve_speedup_mixed_vs_fp64"] = f["solve_s"] / m["solve_s"]
         line["solve_speedup_fp64_tc_vs_fp64"] = f["solve_s"] / t["solve_s"]
+    if "triples" in m and "triples" in t:
+        line["abs_dE_triples_mixed_vs_fp64_tc"] = abs(m["triples"]["e_t"] - t["triples"]["e_t"])
     if ref:
         line["oracle"] = {"e_rhf": ref["e_rhf"], "e_ccsd_corr": ref["e_ccsd_corr"], "source": fixture.name}
         line["abs_dE_rhf_vs_oracle"] = abs(e_scf - ref["e_rhf"])
@@ -763,6 +773,8 @@ def main():
                          "from the geometry, mixed and plain-FP64 solves against the oracle's energy; "
                          "batch64: 64 water clusters (H2O)1..6 solved together")
     ap.add_argument("--waters", type=int, default=10, help="--config h2o10: cluster size (default 10)")
+    ap.add_argument("--triples-fp64-tc", action="store_true",
+                    help="--config h2o10: also the FP64-grade (T) on the fp64_tc solve (mixed (T) always)")
     ap.add_argument("--clusters", type=int, default=64, help="--config batch64: number of clusters")
     ap.add_argument("--batch-basis", default="6-31G**",
                     help="--config batch64: basis (6-31G** gives 25 AO per water; 6-31G* gives 19)")

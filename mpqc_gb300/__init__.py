@@ -9,7 +9,7 @@ mirror of the reference interface.  Build the library with
 """
 from . import basis, molecules, synth  # noqa: F401
 from ._lib import LIB_PATH, GbccError, load  # noqa: F401
-from .ccsd import CCSD, FeatureDisabled, InputError, Solver, compute_cs_ccsd_r1_r2, solve_batch  # noqa: F401
+from .ccsd import CCSD, CCSD_T, FeatureDisabled, InputError, Solver, compute_cs_ccsd_r1_r2, solve_batch  # noqa: F401
 from .scf import RHF, ccsd_energy  # noqa: F401
 
 __all__ = ["CCSD", "Solver", "compute_cs_ccsd_r1_r2", "GbccError", "InputError", "FeatureDisabled",

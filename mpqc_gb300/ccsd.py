@@ -335,16 +335,18 @@ def compute_cs_ccsd_r1_r2(t1, t2, ints, eps_o, eps_v, precision="fp64", **kw):
 
 
 class CCSD:
-    """KeyVal-compatible CCSD front end (standard method, Jacobi+DIIS solver).
+    """KeyVal-compatible CCSD front end (Jacobi+DIIS solver).
 
-    Recognised keys (reference defaults): ``method`` ("standard"),
+    Recognised keys (reference defaults): ``method`` ("standard"; "df" and
+    "direct" as well, whose integrals ``compute`` then takes in their form),
     ``max_iter`` (30), ``solver`` ("jacobi_diis"), ``verbose`` (False),
     ``reduced_abcd_memory`` (True; no effect for the dense standard method),
     ``diis_start`` (1), ``n_diis`` (8), ``diis_damp`` (0.0), ``diis_ngroup`` (1),
     ``diis_group_nstart`` (1), ``precision`` (the Energy property precision,
     1e-9).  Additional keys of this implementation: ``gbcc_precision``
-    ("fp64" | "mixed"), ``slices`` ([ladder, ring, other], default [0,0,0]: chosen from the measured error),
-    ``refine_iters`` (2), ``mixed_switch_precision`` (0: the target precision), ``device`` (0).
+    ("fp64" | "mixed" | "fp64_tc"), ``slices`` ([ladder, ring, other], default [0,0,0]: chosen from the measured
+    error), ``refine_iters`` (2), ``refine_precision`` ("fp64" | "fp64_tc"), ``mixed_switch_precision`` (0: the
+    target precision), ``device`` (0).
     """
 
     def __init__(self, kv: dict):
@@ -354,8 +356,9 @@ class CCSD:
         method = kv.get("method", "standard")
         if method not in ("standard", "df", "direct", "direct_df"):
             raise InputError(f"invalid method {method!r}")
-        if method != "standard":
-            raise FeatureDisabled(f"method {method!r} is not provided by this solver (standard only)")
+        if method == "direct_df":
+            raise FeatureDisabled("method 'direct_df' is not provided by this solver")
+        self.method = method
         solver = kv.get("solver", "jacobi_diis")
         if solver not in ("jacobi_diis", "pno"):
             raise InputError(f"invalid solver {solver!r}")
@@ -371,22 +374,50 @@ class CCSD:
         self.report = None
         self.energy = None
 
+    def _solver(self, o, v):
+        kv = self.kv
+        return Solver(o, v, precision=kv.get("gbcc_precision", "fp64"), slices=kv.get("slices", (0, 0, 0)),
+                      refine_iters=kv.get("refine_iters", 2), refine_precision=kv.get("refine_precision", "fp64"),
+                      mixed_switch_precision=kv.get("mixed_switch_precision", 0.0),
+                      max_iter=self.max_iter, target_precision=self.precision,
+                      diis_start=kv.get("diis_start", 1), n_diis=kv.get("n_diis", 8),
+                      diis_damp=kv.get("diis_damp", 0.0), diis_ngroup=kv.get("diis_ngroup", 1),
+                      diis_group_nstart=kv.get("diis_group_nstart", 1), verbose=self.verbose,
+                      device=kv.get("device", 0))
+
+    def _set(self, s, eps_o, eps_v, ints):
+        """The integrals of the method: standard -- the nine cc::Integrals
+        blocks; df -- the seven blocks without Giabc / Gabcd plus the factors
+        Xai, Xab; direct -- the eight blocks without Gabcd plus the AO
+        integrals Gao and the MO coefficients Ca, Ci."""
+        ints = dict(ints)
+        if self.method == "df":
+            for k in ("Xai", "Xab"):
+                if k not in ints:
+                    raise InputError(f"method 'df' needs {k}")
+            xai, xab = ints.pop("Xai"), ints.pop("Xab")
+            s.set_df_inputs(eps_o, eps_v, xai, xab, **{k: x for k, x in ints.items() if k not in ("Giabc", "Gabcd")})
+        elif self.method == "direct":
+            for k in ("Gao", "Ca", "Ci"):
+                if k not in ints:
+                    raise InputError(f"method 'direct' needs {k}")
+            g, ca, ci = ints.pop("Gao"), ints.pop("Ca"), ints.pop("Ci")
+            s.set_direct_inputs(eps_o, eps_v, g, ca, ci, **{k: x for k, x in ints.items() if k != "Gabcd"})
+        else:
+            s.set_inputs(eps_o, eps_v, **ints)
+
     def compute(self, eps_o, eps_v, ints) -> float:
         o, v = np.asarray(eps_o).size if isinstance(eps_o, np.ndarray) else eps_o.numel(), \
             np.asarray(eps_v).size if isinstance(eps_v, np.ndarray) else eps_v.numel()
-        kv = self.kv
-        with Solver(o, v, precision=kv.get("gbcc_precision", "fp64"), slices=kv.get("slices", (0, 0, 0)),
-                    refine_iters=kv.get("refine_iters", 2),
-                    mixed_switch_precision=kv.get("mixed_switch_precision", 0.0),
-                    max_iter=self.max_iter, target_precision=self.precision,
-                    diis_start=kv.get("diis_start", 1), n_diis=kv.get("n_diis", 8),
-                    diis_damp=kv.get("diis_damp", 0.0), diis_ngroup=kv.get("diis_ngroup", 1),
-                    diis_group_nstart=kv.get("diis_group_nstart", 1), verbose=self.verbose,
-                    device=kv.get("device", 0)) as s:
-            s.set_inputs(eps_o, eps_v, **ints)
+        with self._solver(o, v) as s:
+            self._set(s, eps_o, eps_v, ints)
             e, t1, t2, rep = s.solve()
+            self._after_solve(s)
         self._t1, self._t2, self.report, self.energy = t1, t2, rep, e
         return e
+
+    def _after_solve(self, s):
+        """Hook of subclasses that consume the converged amplitudes on the handle."""
 
     def t1(self):
         if self._t1 is None:
@@ -397,3 +428,32 @@ class CCSD:
         if self._t2 is None:
             raise RuntimeError("CCSD T2 amplitudes have not been computed")
         return self._t2
+
+
+class CCSD_T(CCSD):
+    """KeyVal-compatible CCSD(T) front end (CCSD_T, ccsd_t.h:33-195): the CCSD
+    energy plus the perturbative triples correction of the converged
+    amplitudes.  Keys of CCSD plus ``approach`` ("coarse", the reference's
+    default, "fine" and "straight" give the same energy -- they differ in how
+    the reference distributes the triples over processes -- ; "laplace", a
+    quadrature approximation, is not provided), ``reblock_occ`` /
+    ``reblock_unocc`` / ``reblock_inner`` (tiling only, accepted and ignored)
+    and, of this implementation, ``triples_precision`` ("fp64" | "mixed" |
+    "fp64_tc", default "fp64")."""
+
+    def __init__(self, kv: dict):
+        super().__init__(kv)
+        approach = self.kv.get("approach", "coarse")
+        if approach not in ("coarse", "fine", "straight", "laplace"):
+            raise InputError(f"invalid approach {approach!r}")
+        if approach == "laplace":
+            raise FeatureDisabled("the Laplace-transform (T) is not provided by this solver")
+        self.triples_energy = None
+
+    def _after_solve(self, s):
+        self.triples_energy = s.triples(self.kv.get("triples_precision", "fp64"))
+
+    def compute(self, eps_o, eps_v, ints) -> float:
+        e_ccsd = super().compute(eps_o, eps_v, ints)
+        self.energy = e_ccsd + self.triples_energy
+        return self.energy

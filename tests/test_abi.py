@@ -97,13 +97,21 @@ def test_keyval_front_end_validation():
     with pytest.raises(InputError):
         CCSD({"ref": "scf", "method": "bogus"})
     with pytest.raises(FeatureDisabled):
-        CCSD({"ref": "scf", "method": "df"})
+        CCSD({"ref": "scf", "method": "direct_df"})
     with pytest.raises(FeatureDisabled):
         CCSD({"ref": "scf", "solver": "pno"})
+    assert CCSD({"ref": "scf", "method": "df"}).method == "df"
+    assert CCSD({"ref": "scf", "method": "direct"}).method == "direct"
     c = CCSD({"ref": "scf"})
     assert c.max_iter == 30 and c.precision == 1e-9
     with pytest.raises(RuntimeError):
         c.t1()
+    from mpqc_gb300 import CCSD_T
+    with pytest.raises(InputError):
+        CCSD_T({"ref": "scf", "approach": "bogus"})
+    with pytest.raises(FeatureDisabled):
+        CCSD_T({"ref": "scf", "approach": "laplace"})
+    assert CCSD_T({"ref": "scf", "approach": "straight"}).triples_energy is None
 
 
 def test_array_checks():

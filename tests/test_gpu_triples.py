@@ -84,3 +84,16 @@ def test_triples_argument_errors():
         with pytest.raises(_lib.GbccError) as ex:
             s.triples("fp64", inp.t1, bad)
         assert ex.value.status == _lib.GBCC_ERR_INVALID_ARG
+
+
+def test_keyval_ccsd_t_front_end(water_t):
+    """The KeyVal front end (CCSD(T), method df, approach straight as in the
+    recorded input) gives the recorded CCSD(T) energy."""
+    from mpqc_gb300 import CCSD_T
+    g, blocks = water_t
+    ints = {k: blocks[k] for k in ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka")}
+    ints.update(Xai=np.ascontiguousarray(g["Xai"]), Xab=np.ascontiguousarray(g["Xab"]))
+    w = CCSD_T({"ref": "scf", "method": "df", "approach": "straight", "precision": 1e-11, "max_iter": 60})
+    e = w.compute(g["eps_o"], g["eps_v"], ints)
+    assert abs(w.triples_energy - float(g["ref_e_t"])) < 1e-11
+    assert abs(e - float(g["ref_e_ccsd"]) - float(g["ref_e_t"])) < 1e-9
