@@ -76,6 +76,16 @@ int gbcc_testing_fixed_split(const double* x, int64_t rows, int64_t cols, int ns
 int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
                              int bn, int ksplit, int cta2, int repeat, float* ms);
 
+/* Failure detection of the tensor-core GEMM without a GPU fault: one launch
+ * of C = A B^T (3 BF16 slices) whose producer leaves stage skip_stage of
+ * every CTA unloaded, with the pipeline barriers' wait limit shortened to
+ * wait_ns; the kernel's bounded wait runs out, it records the timeout, drains
+ * its copies, waits for its MMAs, frees its tensor memory and returns.
+ * *first = that launch's status (GBCC_ERR_TIMEOUT), *second = the status of
+ * the same product run normally afterwards, whose result is written to C. */
+int gbcc_testing_gemm_timeout(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+                              uint64_t wait_ns, int64_t skip_stage, int* first, int* second);
+
 /* Peak probe: FP64 tensor-core throughput (mma.sync m8n8k4 .f64, DMMA) in
  * GFLOP/s, register operands over all SMs. */
 int gbcc_testing_dmma_peak(double* gflops);

@@ -90,14 +90,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait for the phase of `parity` to complete.  Gives up (false) after
-// kWaitNs, or early once any CTA has recorded an error.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const int* err) {
+// limit_ns, or early once any CTA has recorded an error.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const int* err,
+                                          uint64_t limit_ns = kWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 0) {
-      if (globaltimer() - t0 > kWaitNs) return false;
+      if (globaltimer() - t0 > limit_ns) return false;
       if (*reinterpret_cast<const volatile int*>(err) != kDevOk) return false;
     }
   }
@@ -424,6 +425,8 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
   if constexpr (CTA2) cluster_sync();  // both CTAs' barriers exist before any remote arrive
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // wait limit of the pipeline's barriers (a test hook may shorten it)
+  const uint64_t wait_ns = g.wait_ns ? g.wait_ns : kWaitNs;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -444,7 +447,7 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
         const int nb0 = n0 + static_cast<int>(rank) * Cfg::kBRows;
         int kb = kb0, pr = 0;
         for (int it = 0; it < n_iter; ++it, ++gi) {
-          if (!mbar_wait(&empty[s], ph ^ 1, g.err)) {
+          if (!mbar_wait(&empty[s], ph ^ 1, g.err, wait_ns)) {
             record_error(g.err, kDevTimeout);
             ok = false;
             break;
@@ -456,9 +459,13 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
             tma_load_3d_pair(&tmA, bar, sA + s * Cfg::kAStage, 0, m0 + a_row0, g.pa[pr] * kblocks + kb);
             tma_load_3d_pair(&tmB, bar, sB + s * Cfg::kBStage, 0, nb0 + b_row0, g.pb[pr] * kblocks + kb);
           } else if constexpr (SPS == 1) {
-            mbar_expect_tx(&full[s], Cfg::kStageBytes);
-            tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage, 0, m0 + a_row0, g.pa[pr] * kblocks + kb);
-            tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage, 0, nb0 + b_row0, g.pb[pr] * kblocks + kb);
+            // test hook (gbcc_testing_gemm_timeout): leave one stage unloaded,
+            // so that its consumer's bounded wait runs out
+            if (g.skip_stage1 == 0 || static_cast<int64_t>(gi) + 1 != g.skip_stage1) {
+              mbar_expect_tx(&full[s], Cfg::kStageBytes);
+              tma_load_3d(&tmA, &full[s], sA + s * Cfg::kAStage, 0, m0 + a_row0, g.pa[pr] * kblocks + kb);
+              tma_load_3d(&tmB, &full[s], sB + s * Cfg::kBStage, 0, nb0 + b_row0, g.pb[pr] * kblocks + kb);
+            }
           } else {
             // every slice of A and B of this k-block
             mbar_expect_tx(&full[s], Cfg::kStageBytes);
@@ -506,12 +513,12 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
         int pos = 0;
         for (int it = 0; it < n_iter; ++it, ++gi) {
           const uint32_t b = c & 1;
-          if (pos == 0 && !mbar_wait(&acc_empty[b], ((c >> 1) & 1) ^ 1, g.err)) {
+          if (pos == 0 && !mbar_wait(&acc_empty[b], ((c >> 1) & 1) ^ 1, g.err, wait_ns)) {
             record_error(g.err, kDevTimeout);
             ok = false;
             break;
           }
-          if (!mbar_wait(&full[s], ph, g.err)) {
+          if (!mbar_wait(&full[s], ph, g.err, wait_ns)) {
             record_error(g.err, kDevTimeout);
             ok = false;
             break;
@@ -587,7 +594,7 @@ __global__ void __launch_bounds__(TcCfg<BN, CTA2, SPS>::kThreads, 1)
       bool first_fold = true;
       for (int cc = 0; cc < nchunks; ++cc, ++c) {
         const uint32_t b = c & 1;
-        if (!mbar_wait(&acc_full[b], (c >> 1) & 1, g.err)) {
+        if (!mbar_wait(&acc_full[b], (c >> 1) & 1, g.err, wait_ns)) {
           record_error(g.err, kDevTimeout);
           ok = false;
           break;

@@ -212,6 +212,11 @@ struct GemmTcArgs {
   // first row of A / B within their panels (a window of a larger panel:
   // rows past the panel's end load as zeros; 0 for whole panels)
   int64_t a_row0, b_row0;
+  // test hooks: the pipeline barriers' wait limit in ns (0: 2 s), and 1 +
+  // the stage (counted over a CTA's stage uses; one pair per stage) whose
+  // loads the producer leaves out (0: none -- the value-initialised default)
+  uint64_t wait_ns;
+  int64_t skip_stage1;
 };
 // Deterministic K-split reduction: C[cm[m] + cn[n]] = beta*C + alpha * sum_s
 // partial[s][m][n] (splits summed in order), partial rows of length ldp and

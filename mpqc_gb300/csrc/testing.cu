@@ -451,3 +451,86 @@ extern "C" int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const d
   for (void* p : owned) dev_free(p);
   return status;
 }
+
+// Failure detection of the tensor-core pipeline: one GEMM whose producer
+// leaves stage `skip_stage` of every CTA unloaded, with the barriers' wait
+// limit shortened to wait_ns, so the MMA thread's bounded wait runs out; the
+// kernel records the timeout, drains its copies, waits for its MMAs, frees
+// TMEM and returns.  *first gets that launch's status (GBCC_ERR_TIMEOUT
+// expected); the same product is then run normally and *second gets its
+// status, C its result.
+extern "C" int gbcc_testing_gemm_timeout(int64_t M, int64_t N, int64_t K, const double* A, const double* B,
+                                         double* Cout, uint64_t wait_ns, int64_t skip_stage, int* first,
+                                         int* second) {
+  using namespace gbcc;
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !Cout || !first || !second || skip_stage < 0 || wait_ns == 0)
+    return GBCC_ERR_INVALID_ARG;
+  std::vector<void*> owned;
+  auto alloc = [&](size_t bytes) {
+    void* p = dev_alloc(bytes);
+    owned.push_back(p);
+    return p;
+  };
+  int status = GBCC_OK;
+  try {
+    cudaStream_t st = nullptr;
+    const int slices = 3, bn = 128;
+    const int64_t Mpad = rup(M, kTcBM), Npad = rup(N, bn), Kpad = rup(K, kTcBK);
+    double* dA = static_cast<double*>(alloc(M * K * sizeof(double)));
+    double* dB = static_cast<double*>(alloc(N * K * sizeof(double)));
+    double* dC = static_cast<double*>(alloc(M * N * sizeof(double)));
+    int* err = static_cast<int*>(alloc(sizeof(int)));
+    GBCC_CK(cudaMemcpy(dA, A, M * K * sizeof(double), cudaMemcpyHostToDevice));
+    GBCC_CK(cudaMemcpy(dB, B, N * K * sizeof(double), cudaMemcpyHostToDevice));
+    auto table = [&](int64_t n, int64_t stride) {
+      std::vector<int64_t> h(n);
+      for (int64_t i = 0; i < n; ++i) h[i] = i * stride;
+      int64_t* d = static_cast<int64_t*>(alloc(n * sizeof(int64_t)));
+      GBCC_CK(cudaMemcpy(d, h.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
+      return d;
+    };
+    auto* sa = static_cast<__nv_bfloat16*>(alloc(slices * Mpad * Kpad * sizeof(__nv_bfloat16)));
+    auto* sb = static_cast<__nv_bfloat16*>(alloc(slices * Npad * Kpad * sizeof(__nv_bfloat16)));
+    auto pack = [&](const double* src, int64_t rows, int64_t rows_pad, __nv_bfloat16* dst) {
+      GatherArgs g{};
+      g.nterms = 1;
+      gather_set_coef(g.t[0], 1.0);
+      g.t[0].a = src;
+      g.t[0].ra = table(rows, K);
+      g.t[0].ca = table(K, 1);
+      g.plain = 1;
+      g.R = rows; g.C = K; g.Rpad = rows_pad; g.Cpad = Kpad; g.ldo = Kpad;
+      g.outs = dst; g.nslices = slices; g.slice_stride = rows_pad * Kpad;
+      launch_gather(g, st);
+    };
+    pack(dA, M, Mpad, sa);
+    pack(dB, N, Npad, sb);
+    GemmTcArgs t{};
+    t.M = M; t.N = N; t.Mpad = Mpad; t.Npad = Npad; t.Kpad = Kpad;
+    t.A = sa; t.a_slices = slices; t.B = sb; t.b_slices = slices;
+    for (int a = 0; a < slices; ++a)
+      for (int b = 0; b < slices; ++b)
+        if (a + b < slices) { t.pa[t.npairs] = a; t.pb[t.npairs] = b; ++t.npairs; }
+    t.C = dC; t.cm = table(M, N); t.cn = table(N, 1); t.alpha = 1.0; t.beta = 0.0; t.bn = bn; t.err = err;
+    t.chunk = 4; t.sps = 1; t.group = 1;
+    auto run = [&](int64_t skip1, uint64_t limit) {
+      GBCC_CK(cudaMemset(err, 0, sizeof(int)));
+      t.skip_stage1 = skip1;
+      t.wait_ns = limit;
+      if (!launch_gemm_tc(t, st)) throw Error(GBCC_ERR_CUDA, "tcgen05 launch rejected");
+      GBCC_CK(cudaStreamSynchronize(st));
+      GBCC_CK(cudaGetLastError());
+      int herr = 0;
+      GBCC_CK(cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost));
+      return herr == kDevOk ? static_cast<int>(GBCC_OK) : static_cast<int>(GBCC_ERR_TIMEOUT);
+    };
+    *first = run(skip_stage + 1, wait_ns);
+    *second = run(0, 0);
+    GBCC_CK(cudaMemcpy(Cout, dC, M * N * sizeof(double), cudaMemcpyDeviceToHost));
+  } catch (const Error& e) {
+    std::fprintf(stderr, "gbcc_testing_gemm_timeout: %s\n", e.what());
+    status = e.status;
+  }
+  for (void* p : owned) dev_free(p);
+  return status;
+}

@@ -190,3 +190,35 @@ def test_gemm_output_forms(tlib, slices, bn, sps, cmode, ksplit):
     ref = A @ B.T
     tol = (TOL[slices] + 8 * 2.0**-24 * np.sqrt(K)) if slices else TOL[0]
     assert np.max(np.abs(outs[1] - ref)) <= tol * np.max(np.abs(ref))
+
+
+def test_bounded_wait_returns_a_timeout_and_the_context_stays_usable(tlib):
+    """Failure detection without a GPU fault: the producer leaves one stage of
+    every CTA unloaded and the barriers' wait limit is 1 ms, so the MMA
+    thread's bounded wait runs out; the kernel records GBCC_ERR_TIMEOUT,
+    drains its copies, waits for its MMAs, frees its tensor memory and
+    returns.  The same product then runs normally, and so does a residual
+    through a handle (tensor memory was given back, the context is intact)."""
+    from mpqc_gb300 import Solver, synth
+    from mpqc_gb300._lib import GBCC_ERR_TIMEOUT
+    from oracle import ccsd_ref as R
+    from conftest import ints_dict, oracle_ints, rel_err
+    lib = tlib
+    rng = np.random.default_rng(5)
+    M, N, K = 256, 256, 1024                   # 4 tiles; 16 k-blocks x 6 slice pairs each
+    A = rng.normal(size=(M, K))
+    B = rng.normal(size=(N, K))
+    out = np.zeros((M, N))
+    first, second = C.c_int(-1), C.c_int(-1)
+    st = lib.gbcc_testing_gemm_timeout(M, N, K, A.ctypes.data, B.ctypes.data, out.ctypes.data, 1_000_000, 3,
+                                       C.byref(first), C.byref(second))
+    assert st == 0
+    assert first.value == GBCC_ERR_TIMEOUT and second.value == 0
+    ref = A @ B.T
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < 5e-6
+    inp = synth.make_inputs(4, 12, 10, seed=11, t1_scale=1e-2)
+    with Solver(inp.o, inp.v, precision="mixed", slices=(3, 3, 3)) as s:
+        s.set_inputs(inp.eps_o, inp.eps_v, **ints_dict(inp))
+        r1, r2 = s.residual(inp.t1, inp.t2)
+    r1_ref, r2_ref = R.residual(inp.t1, inp.t2, oracle_ints(inp))
+    assert rel_err(r2, r2_ref) < 2e-6 and rel_err(r1, r1_ref) < 2e-6
