@@ -524,6 +524,13 @@ def molecule_report(args):
     F = flop_count(o, v)
     log(f"[h2o{nw}] N={scf.nbf} o={o} v={v}: E_RHF {e_scf:.10f} ({srep.iters} it., ERI {srep.seconds_eri:.2f} s, "
         f"SCF {srep.seconds_scf:.2f} s, wall {time.perf_counter() - t0:.1f} s)")
+    if args.scf_only:
+        # profiling aid: the input producer alone (integrals, RHF)
+        print(json.dumps({"molecule": f"(H2O){nw}", "basis": "cc-pVDZ", "nbf": srep.nbf, "e_rhf": e_scf,
+                          "scf": {"iters": srep.iters, "eri_s": srep.seconds_eri, "scf_s": srep.seconds_scf,
+                                  "one_body_s": srep.seconds_one_body}}), flush=True)
+        scf.close()
+        return 0
     runs, amps = {}, {}
     for prec in ("mixed", "fp64_tc") if args.no_solve_fp64 else ("mixed", "fp64_tc", "fp64"):
         s = Solver(o, v, precision=prec, target_precision=args.solve_precision, max_iter=args.max_iter,
@@ -680,6 +687,29 @@ def batch_report(args):
     return 0
 
 
+def triples_probe(args):
+    """(T) on seeded synthetic inputs at (--o, --v) (profiling aid): the
+    residual-engine handle takes the synthetic integrals, gbcc_triples runs
+    twice from the synthetic amplitudes; one JSON line with E(T) and the
+    seconds of the second run."""
+    from mpqc_gb300 import Solver, synth
+    from mpqc_gb300 import build as gb
+    gb.build()
+    o, v = args.o, args.v
+    inp = synth.make_inputs(o, v, 40, seed=args.seed, t1_scale=1e-2)
+    ints = {k: np.ascontiguousarray(getattr(inp, k)) for k in
+            ("Fia", "Fij", "Fab", "Gijab", "Gijkl", "Giajb", "Gijka", "Giabc", "Gabcd")}
+    with Solver(o, v, precision="fp64_tc" if args.triples_precision == "fp64_tc" else "fp64") as s:
+        s.set_inputs(inp.eps_o, inp.eps_v, **ints)
+        s.triples(args.triples_precision, inp.t1, inp.t2)
+        t0 = time.perf_counter()
+        e_t = s.triples(args.triples_precision, inp.t1, inp.t2)
+        sec = time.perf_counter() - t0
+    print(json.dumps({"triples": True, "o": o, "v": v, "precision": args.triples_precision, "e_t": e_t,
+                      "seconds": sec, "flops_d_terms": 2 * o**3 * v**4}), flush=True)
+    return 0
+
+
 def gemm_probe(args):
     """One GEMM shape C = A B^T on the library's kernels (profiling aid): seeded
     normal FP64 inputs through gbcc_testing_gemm_ex3 (split-BF16 tensor-core
@@ -773,6 +803,10 @@ def main():
                          "from the geometry, mixed and plain-FP64 solves against the oracle's energy; "
                          "batch64: 64 water clusters (H2O)1..6 solved together")
     ap.add_argument("--waters", type=int, default=10, help="--config h2o10: cluster size (default 10)")
+    ap.add_argument("--triples", action="store_true",
+                    help="profiling aid: (T) on synthetic inputs at --o/--v (default 32/320: pass smaller)")
+    ap.add_argument("--triples-precision", default="mixed", choices=["fp64", "mixed", "fp64_tc"])
+    ap.add_argument("--scf-only", action="store_true", help="--config h2o10: the integrals and RHF only")
     ap.add_argument("--triples-fp64-tc", action="store_true",
                     help="--config h2o10: also the FP64-grade (T) on the fp64_tc solve (mixed (T) always)")
     ap.add_argument("--clusters", type=int, default=64, help="--config batch64: number of clusters")
@@ -781,6 +815,8 @@ def main():
     args = ap.parse_args()
     if args.gemm:
         return gemm_probe(args)
+    if args.triples:
+        return triples_probe(args)
     if args.config == "h2o10":
         if args.max_iter == 40 and args.solve_precision == 1e-8:
             args.solve_precision = 1e-9
