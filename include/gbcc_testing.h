@@ -86,6 +86,10 @@ int gbcc_testing_gemm_fp64tc(int64_t M, int64_t N, int64_t K, const double* A, c
 int gbcc_testing_gemm_timeout(int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
                               uint64_t wait_ns, int64_t skip_stage, int* first, int* second);
 
+/* Triplets per (T) batch for calls from now on (0: the default, as many as
+ * keep the batch's slice of t3 in L2). */
+int gbcc_testing_triples_chunk(int64_t k);
+
 /* Peak probe: FP64 tensor-core throughput (mma.sync m8n8k4 .f64, DMMA) in
  * GFLOP/s, register operands over all SMs. */
 int gbcc_testing_dmma_peak(double* gflops);

@@ -38,6 +38,9 @@
 
 namespace gbcc {
 
+// test hook: triplets per batch (0: as many as keep the t3 slice in L2)
+int64_t g_triples_chunk = 0;
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -56,19 +59,19 @@ __device__ __forceinline__ double block_sum_det(double v, double* sh) {
   return r;
 }
 
-// One batch (i, j; k = j + kk): block (a, kk) sums over (b, c) and writes the
+// One batch (i, j; k = k0 + kk): block (a, kk) sums over (b, c) and writes the
 // weighted partial to partial[kk * v + a].  R: the arithmetic of the terms
 // (double for the FP64-grade precisions; float for MIXED, whose contractions
 // already carry ~1e-6 relative error), summed per thread in FP64.
 template <typename R>
 __global__ void __launch_bounds__(kThreads) triples_energy_kernel(
-    const double* __restrict__ W, int64_t o, int64_t v, int i, int j, int nk, const double* __restrict__ Gijab,
+    const double* __restrict__ W, int64_t o, int64_t v, int i, int j, int k0, int nk, const double* __restrict__ Gijab,
     const double* __restrict__ t1, const double* __restrict__ eps_o, const double* __restrict__ eps_v,
     double* __restrict__ partial) {
   __shared__ double sh[kThreads];
   const int64_t a = blockIdx.x;
   const int kk = blockIdx.y;
-  const int k = j + kk;
+  const int k = k0 + kk;
   if (kk >= nk) return;
   const double mult = (i < j && j < k) ? 6.0 : ((i == j && j == k) ? 1.0 : 3.0);
   const int64_t v2 = v * v;
@@ -425,17 +428,6 @@ double Triples::run() {
   const int64_t* cm6 = kqp_table(v, 1);
   const int64_t* cn5 = r_table(v);
   const int64_t* cn6 = r_table(v2);
-  {
-    // largest offset each term writes, for the largest batch (k - j < o)
-    const int64_t last = v - 1, kmax = o - 1;
-    const int64_t worst[] = {last * (v2 + v) + kmax * v3 + last,       // 1, 3
-                             last * (v2 + 1) + kmax * v3 + last * v,   // 2
-                             last * (v + 1) + kmax * v3 + last * v2,   // 4
-                             kmax * v3 + last * (v2 + 1) + last * v,   // 5
-                             kmax * v3 + last * (v + 1) + last * v2};  // 6
-    for (int64_t w : worst)
-      if (w >= o * v3) throw Error(GBCC_ERR_STATE, "(T): output offsets outside W");
-  }
 
   // K-split workspace: a split happens only with fewer output tiles than
   // SMs, ks <= ceil(SMs / tiles), so ks Mpad Npad < 2 SMs x one 128 x 256 tile
@@ -443,7 +435,24 @@ double Triples::run() {
     partk_elems_ = static_cast<size_t>(num_sms()) * 2 * kTcBM * 256;
     partk_ = static_cast<double*>(alloc(partk_elems_ * sizeof(double)));
   }
-  W_ = static_cast<double*>(alloc(static_cast<size_t>(o) * v3 * sizeof(double)));
+  // triplets per batch: all k >= j, unless their slice of t3 would pass
+  // 8 GB (then chunks of k).  Chunks small enough to keep the slice in L2
+  // measured slower (the batches' GEMMs shrink and multiply: (H2O)10 mixed
+  // 18 s -> 28 s), so chunking only bounds memory.
+  int64_t kc = std::max<int64_t>(1, std::min<int64_t>(o, (static_cast<int64_t>(8) << 30) / (v3 * 8)));
+  if (g_triples_chunk > 0) kc = std::min<int64_t>(o, g_triples_chunk);
+  {
+    // largest offset each term writes, for the largest batch (kk < kc)
+    const int64_t last = v - 1, kmax = kc - 1;
+    const int64_t worst[] = {last * (v2 + v) + kmax * v3 + last,       // 1, 3
+                             last * (v2 + 1) + kmax * v3 + last * v,   // 2
+                             last * (v + 1) + kmax * v3 + last * v2,   // 4
+                             kmax * v3 + last * (v2 + 1) + last * v,   // 5
+                             kmax * v3 + last * (v + 1) + last * v2};  // 6
+    for (int64_t w : worst)
+      if (w >= kc * v3) throw Error(GBCC_ERR_STATE, "(T): output offsets outside W");
+  }
+  W_ = static_cast<double*>(alloc(static_cast<size_t>(kc) * v3 * sizeof(double)));
   const int64_t npair = o * (o + 1) / 2;
   double* partial = static_cast<double*>(alloc(static_cast<size_t>(npair) * o * v * sizeof(double)));
   GBCC_CK(cudaMemsetAsync(partial, 0, static_cast<size_t>(npair) * o * v * sizeof(double), st_));
@@ -452,23 +461,27 @@ double Triples::run() {
   int64_t slot = 0;
   for (int i = 0; i < o; ++i) {
     for (int j = i; j < o; ++j, ++slot) {
-      const int nk = static_cast<int>(o - j);
-      const int64_t rj = (static_cast<int64_t>(j) * o + j) * v;  // rows (j, k = j.., r)
-      const int64_t ri = (static_cast<int64_t>(i) * o + j) * v;  // rows (i, k = j.., r); also (i, j, r)
-      const int64_t nkv = static_cast<int64_t>(nk) * v;
-      gemm(A, i * v2, v2, B, rj, nkv, cm1, cn13, false, 0.0);
-      gemm(A, i * v2, v2, B2, rj, nkv, cm2, cn2, true, 1.0);
-      gemm(A, j * v2, v2, B, ri, nkv, cm3, cn13, false, 1.0);
-      gemm(A, j * v2, v2, B2, ri, nkv, cm4, cn4, true, 1.0);
-      gemm(At, j * v2, nk * v2, B, ri, v, cm5, cn5, true, 1.0);
-      gemm(At, j * v2, nk * v2, B2, ri, v, cm6, cn6, true, 1.0);
-      const dim3 grid(static_cast<unsigned>(v), static_cast<unsigned>(nk));
-      if (prec_ == GBCC_PREC_MIXED)
-        triples_energy_kernel<float><<<grid, kThreads, 0, st_>>>(W_, o, v, i, j, nk, in_.Gijab, in_.t1, in_.eps_o,
-                                                                  in_.eps_v, partial + slot * o * v);
-      else
-        triples_energy_kernel<double><<<grid, kThreads, 0, st_>>>(W_, o, v, i, j, nk, in_.Gijab, in_.t1, in_.eps_o,
-                                                                   in_.eps_v, partial + slot * o * v);
+      const int64_t pij = (static_cast<int64_t>(i) * o + j) * v;  // rows (i, j, r)
+      for (int k0 = j; k0 < o; k0 += static_cast<int>(kc)) {
+        const int nk = static_cast<int>(std::min<int64_t>(kc, o - k0));
+        const int64_t rj = (static_cast<int64_t>(j) * o + k0) * v;  // rows (j, k = k0.., r)
+        const int64_t ri = (static_cast<int64_t>(i) * o + k0) * v;  // rows (i, k = k0.., r)
+        const int64_t nkv = static_cast<int64_t>(nk) * v;
+        gemm(A, i * v2, v2, B, rj, nkv, cm1, cn13, false, 0.0);
+        gemm(A, i * v2, v2, B2, rj, nkv, cm2, cn2, true, 1.0);
+        gemm(A, j * v2, v2, B, ri, nkv, cm3, cn13, false, 1.0);
+        gemm(A, j * v2, v2, B2, ri, nkv, cm4, cn4, true, 1.0);
+        gemm(At, static_cast<int64_t>(k0) * v2, nk * v2, B, pij, v, cm5, cn5, true, 1.0);
+        gemm(At, static_cast<int64_t>(k0) * v2, nk * v2, B2, pij, v, cm6, cn6, true, 1.0);
+        const dim3 grid(static_cast<unsigned>(v), static_cast<unsigned>(nk));
+        double* part = partial + slot * o * v + static_cast<int64_t>(k0 - j) * v;
+        if (prec_ == GBCC_PREC_MIXED)
+          triples_energy_kernel<float><<<grid, kThreads, 0, st_>>>(W_, o, v, i, j, k0, nk, in_.Gijab, in_.t1,
+                                                                    in_.eps_o, in_.eps_v, part);
+        else
+          triples_energy_kernel<double><<<grid, kThreads, 0, st_>>>(W_, o, v, i, j, k0, nk, in_.Gijab, in_.t1,
+                                                                     in_.eps_o, in_.eps_v, part);
+      }
     }
   }
   sum_kernel<<<1, kThreads, 0, st_>>>(partial, npair * o * v, 1.0 / 3.0, d_e);
@@ -487,3 +500,9 @@ double triples_energy(const TriplesInputs& in, int precision, cudaStream_t st, i
 }
 
 }  // namespace gbcc
+
+extern "C" int gbcc_testing_triples_chunk(int64_t k) {
+  if (k < 0) return GBCC_ERR_INVALID_ARG;
+  gbcc::g_triples_chunk = k;
+  return GBCC_OK;
+}

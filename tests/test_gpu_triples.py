@@ -97,3 +97,21 @@ def test_keyval_ccsd_t_front_end(water_t):
     e = w.compute(g["eps_o"], g["eps_v"], ints)
     assert abs(w.triples_energy - float(g["ref_e_t"])) < 1e-11
     assert abs(e - float(g["ref_e_ccsd"]) - float(g["ref_e_t"])) < 1e-9
+
+
+@pytest.mark.parametrize("chunk", [1, 2, 4])
+def test_triplet_chunks_give_the_same_energy(chunk):
+    """Batches of `chunk` triplets (the size large v takes to keep each t3 slice
+    in L2) give the energy of whole batches."""
+    from mpqc_gb300 import _lib as L
+    lib = L.load()
+    inp = synth.make_inputs(5, 19, 16, seed=3, t1_scale=1e-2)
+    ref = T.triples_energy_by_triplet(inp.t1, inp.t2, inp.Gijab, inp.Gijka, inp.Giabc, inp.eps_o, inp.eps_v)
+    try:
+        assert lib.gbcc_testing_triples_chunk(chunk) == 0
+        with _solver(inp) as s:
+            e = {p: s.triples(p, inp.t1, inp.t2) for p in ("fp64", "mixed")}
+    finally:
+        lib.gbcc_testing_triples_chunk(0)
+    assert abs(e["fp64"] - ref) <= 1e-12 * abs(ref)
+    assert abs(e["mixed"] - ref) <= 2e-5 * abs(ref)
