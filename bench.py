@@ -360,7 +360,10 @@ def ours(args):
         peak = pk.get("bf16_tflops_sustained") or 1700.0
         ach = executed / (lp["gemm_ms"] * 1e-3) / 1e12
         roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "traffic": ncu_traffic(), "kernel": "gemm_tc_kernel (particle-particle ladder, G+ tau+ pair products)",
+                "traffic": ncu_traffic(),
+                "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of this launch "
+                                  "(profiles/ladder_gemm_o32_v320.md), not measured in this run",
+                "kernel": "gemm_tc_kernel (particle-particle ladder, G+ tau+ pair products)",
                 "executed_flops_per_launch": executed, "launch_ms": lp["gemm_ms"],
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"}
     terms = {}
