@@ -384,6 +384,8 @@ void build_solve_graph(gbcc_handle* h) {
   d.v = c.v;
   d.eps_o = S.eps_o->d;
   d.eps_v = S.eps_v->d;
+  d.dinv1 = S.Dinv1->d;
+  d.dinv2 = S.Dinv2->d;
   d.t1 = S.t1->d;
   d.t2 = S.t2->d;
   d.r1 = S.r1->d;
@@ -1031,6 +1033,8 @@ gbcc_status gbcc_solve(gbcc_handle* h, double* t1_ai, double* t2_abij, double* e
       d.v = c.v;
       d.eps_o = S.eps_o->d;
       d.eps_v = S.eps_v->d;
+      d.dinv1 = S.Dinv1->d;
+      d.dinv2 = S.Dinv2->d;
       d.t1 = S.t1->d;
       d.t2 = S.t2->d;
       d.r1 = S.r1->d;

@@ -25,7 +25,13 @@
 //  - h_kc(k,c) (2 t2(c,a,k,i) - t2(c,a,i,k) + t1(c,i) t1(a,k)) is not
 //    materialised: the t1 t1 part is t1(a,k) (h_kc(k,c) t1(c,i));
 //  - nor is T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l): the ring
-//    contractions pack its two terms directly.
+//    contractions pack its two terms directly;
+//  - the hole-hole ladder W(k,l,i,j) tau(a,b,k,l) runs as pair products over
+//    k <= l and i <= j (like the particle-particle ladder, kernels.cu), and
+//    adds to that ladder's B+-; one pass then writes r2: r2u(a,b,i,j) +
+//    r2u(b,a,j,i) with the tmp terms folded in (-0.5 tmp(a,b,i,j) -
+//    tmp(b,a,i,j) of r2u and their images), g_abij and the unpacked B+-
+//    (integral-direct: W and r2 = W tau as written, the pass adds to r2).
 #include "ccsd_program.h"
 
 namespace gbcc {
@@ -69,6 +75,8 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df, int64
   eps_v = &E.tensor("eps_v", {v}, true);
   f_ai = &E.tensor("f_ai", {v, o}, true);
   g_abij = &E.tensor("g_abij", {v, v, o, o}, true);
+  Dinv1 = &E.tensor("Dinv1", {v, o}, true);
+  Dinv2 = &E.tensor("Dinv2", {v, v, o, o}, true);
   t1 = &E.tensor("t1", {v, o});
   t2 = &E.tensor("t2", {v, v, o, o});
   tau = &E.tensor("tau", {v, v, o, o});
@@ -83,7 +91,7 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df, int64
   Y2 = &E.tensor("Y2", {o, o, v, o});
   gki = &E.tensor("gki", {o, o});
   gac = &E.tensor("gac", {v, v});
-  J = &E.tensor("J", {v, o, o, v});
+  P = &E.tensor("P", {v, o, o, v});
   K = &E.tensor("K", {o, v, o, v});
   tmp = &E.tensor("tmp", {v, v, o, o});
   W = &E.tensor("W", {o, o, o, o});
@@ -118,6 +126,10 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df, int64
   Bm = &E.tensor("Bm", {nm, std::max<int64_t>(sm, 1)});
   Xp = &E.tensor("Xp", {o * v, sp});
   Xm = &E.tensor("Xm", {o * v, sm});
+  Gtp = &E.tensor("Gtp", {sp, np}, true);
+  Gtm = &E.tensor("Gtm", {std::max<int64_t>(sm, 1), std::max<int64_t>(nm, 1)}, true);
+  Wt = &E.tensor("Wt", {sp, sp});
+  Wm = &E.tensor("Wm", {std::max<int64_t>(sm, 1), std::max<int64_t>(sm, 1)});
   if (naux > 0) {
     Xai = &E.tensor("Xai", {naux, v, o}, true);
     Xab = &E.tensor("Xab", {naux, v, v}, true);
@@ -151,12 +163,18 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df, int64
   }
 }
 
-// f_ai(a,i) = Fia(i,a), g_abij(a,b,i,j) = Gijab(i,j,a,b)  (ccsd.h:325-330);
+// f_ai(a,i) = Fia(i,a), g_abij(a,b,i,j) = Gijab(i,j,a,b)  (ccsd.h:325-330); the
+// reciprocal Jacobi denominators;
 // G+/G- of Gabcd and Giabc for the pair-symmetric ladder (kernels.cu)
 void setup_program(Engine& E, const CcsdTensors& S) {
   E.assign(ix(*S.f_ai, "ai"), 0.0, {f1(1.0, ix(*S.Fia, "ia"))});
   E.assign(ix(*S.g_abij, "abij"), 0.0, {f1(1.0, ix(*S.Gijab, "ijab"))});
   const int64_t v = S.t1->dim[0], o = S.t1->dim[1];
+  {
+    const double *eo = S.eps_o->d, *ev = S.eps_v->d;
+    double *d1 = S.Dinv1->d, *d2 = S.Dinv2->d;
+    E.custom([=](cudaStream_t st) { launch_denominators(o, v, eo, ev, d1, d2, st); }, 1);
+  }
   if (S.nao > 0) {
     const int64_t n = S.nao;
     const double* Gao = S.Gao->d;
@@ -176,6 +194,9 @@ void setup_program(Engine& E, const CcsdTensors& S) {
   const double* Giabc = S.Giabc->d;
   double *Gip = S.Gip->d, *Gim = S.Gim->d;
   E.custom([=](cudaStream_t st) { launch_build_gpm(o, v, false, Giabc, Gip, Gim, st); }, 1);
+  const double* Gijab = S.Gijab->d;
+  double *Gtp = S.Gtp->d, *Gtm = (o > 1 && v > 1) ? S.Gtm->d : nullptr;
+  E.custom([=](cudaStream_t st) { launch_build_gpm_oo(o, v, Gijab, Gtp, Gtm, st); }, 1);
 }
 
 void residual_program(Engine& E, const CcsdTensors& S) {
@@ -260,7 +281,7 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   // product that stores C runs ~0.5 ms faster at o=32 v=320 than one that
   // reads and adds to it, while an elementwise pass pays little for the read.
   const Tensor& r2u = *S.r2u;
-  const Tensor &J = *S.J, &K = *S.K;
+  const Tensor &J = *S.P, &K = *S.K;
   // j and k intermediates (:229-249) with T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l),
   // packed from its two terms where it is used (not stored)
   const std::vector<Lin> T = {{0.5, ix(t2, "dail")}, lin2(1.0, ix(t1, "di"), ix(t1, "al"))};
@@ -303,27 +324,38 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   // tmp(a,b,i,j) = k(k,a,i,c) t2(c,b,j,k); r2 -= 0.5 tmp(a,b,i,j) + tmp(b,a,i,j)   (:254-256)
   // (t2(c,b,j,k) read as t2(b,c,k,j): its rows (b,j) then run along j in storage)
   E.contract(ix(*S.tmp, "abij"), 0.0, 1.0, {{1.0, ix(K, "kaic")}}, {{1.0, ix(t2, "bckj")}}, R);
-  E.assign(ix(r2u, "abij"), 1.0, {f1(-0.5, ix(*S.tmp, "abij")), f1(-1.0, ix(*S.tmp, "baij"))});
-  // r2(a,b,i,j) = r2(a,b,i,j) + r2(b,a,j,i) + Gijab(i,j,a,b)   (:260-262)
-  // (g_abij(a,b,i,j) = Gijab(i,j,a,b), stored in r2's order)
-  E.assign(ix(r2, "abij"), 0.0,
-           {f1(1.0, ix(r2u, "abij")), f1(1.0, ix(r2u, "baji")), f1(1.0, ix(*S.g_abij, "abij"))});
+  // r2(a,b,i,j) = r2u(a,b,i,j) + r2u(b,a,j,i) + Gijab(i,j,a,b)   (:260-262), with the
+  // tmp terms, is added by the assembly pass below (g_abij(a,b,i,j) = Gijab(i,j,a,b),
+  // stored in r2's order)
+  const double *r2u_d = r2u.d, *tmp_d = S.tmp->d, *gab_d = S.g_abij->d;
   // hole-hole ladder: W_oooo (intermediates :182-193), r2 += W(k,l,i,j) tau(a,b,k,l)
   const Tensor& W = *S.W;
   E.assign(ix(W, "klij"), 0.0, {f1(1.0, ix(Gijkl, "klij"))});
   E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijka, "klic")}}, {{1.0, ix(t1, "cj")}}, O);
   E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijka, "lkjc")}}, {{1.0, ix(t1, "ci")}}, O);
-  E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijab, "klcd")}}, {{1.0, ix(tau, "cdij")}}, O);
-  E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(W, "klij")}}, {{1.0, ix(tau, "abkl")}}, O);
-  // particle-particle ladder (:275, :289): r2 += tau(c,d,i,j) Gabcd(a,b,c,d) as sums
-  // over c <= d of the pair-(anti)symmetric combinations (taup / taum from above)
   if (direct) {
+    E.contract(ix(W, "klij"), 1.0, 1.0, {{1.0, ix(Gijab, "klcd")}}, {{1.0, ix(tau, "cdij")}}, O);
+    E.contract(ix(r2, "abij"), 0.0, 1.0, {{1.0, ix(W, "klij")}}, {{1.0, ix(tau, "abkl")}}, O);
+    E.custom([=](cudaStream_t st) { launch_r2_assemble(o, v, r2u_d, tmp_d, gab_d, nullptr, nullptr, true, r2d, st); },
+             1);
     // integral-direct (:282-286): r2 += Ca(p,a) u(p,r,i,j) Ca(r,b); the T1 parts
     // (Ci u terms) are the tmp2 terms of r2u above
     E.contract(ix(*S.U1, "arij"), 0.0, 1.0, {{1.0, ix(*S.Ca, "pa")}}, {{1.0, ix(*S.u, "prij")}}, O);
     E.contract(ix(r2, "abij"), 1.0, 1.0, {{1.0, ix(*S.U1, "arij")}}, {{1.0, ix(*S.Ca, "rb")}}, O);
     return;
   }
+  // otherwise as pair products (kernels.cu): W+- from the Gijkl and Gijka t1
+  // parts of W, plus Gijab's pair factors times tau+-; their products with
+  // tau+- add to the particle-particle ladder's B+- below
+  {
+    const double* Wd = W.d;
+    double *Wt = S.Wt->d, *Wm = minus ? S.Wm->d : nullptr;
+    E.custom([=](cudaStream_t st) { launch_pair_combine_oo(o, Wd, Wt, Wm, st); }, 1);
+    E.contract(ix(*S.Wt, "PS"), 1.0, 1.0, {{1.0, ix(*S.Gtp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, O);
+    if (minus) E.contract(ix(*S.Wm, "XZ"), 1.0, 1.0, {{1.0, ix(*S.Gtm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, O);
+  }
+  // particle-particle ladder (:275, :289): r2 += tau(c,d,i,j) Gabcd(a,b,c,d) as sums
+  // over c <= d of the pair-(anti)symmetric combinations (taup / taum from above)
   double *Bp = S.Bp->d, *Bm = S.Bm->d;
   if (S.naux == 0) {
     E.contract(ix(*S.Bp, "PS"), 0.0, 1.0, {{1.0, ix(*S.Gp, "PQ")}}, {{1.0, ix(*S.taup, "QS")}}, L);
@@ -344,7 +376,12 @@ void residual_program(Engine& E, const CcsdTensors& S) {
         E.contract(ix(B.bm, "XZ"), 0.0, 1.0, {{1.0, ix(B.gm, "XY")}}, {{1.0, ix(*S.taum, "YZ")}}, L);
     }
   }
-  E.custom([=](cudaStream_t st) { launch_pair_unpack(v, v, o, true, Bp, minus ? Bm : nullptr, 1.0, r2d, st); }, 1);
+  E.contract(ix(*S.Bp, "RS"), 1.0, 1.0, {{1.0, ix(*S.taup, "RP")}}, {{1.0, ix(*S.Wt, "PS")}}, O);
+  if (minus) E.contract(ix(*S.Bm, "UZ"), 1.0, 1.0, {{1.0, ix(*S.taum, "UX")}}, {{1.0, ix(*S.Wm, "XZ")}}, O);
+  // r2 = the symmetrised r2u and tmp terms, g_abij and both ladders' pair products
+  E.custom(
+      [=](cudaStream_t st) { launch_r2_assemble(o, v, r2u_d, tmp_d, gab_d, Bp, minus ? Bm : nullptr, false, r2d, st); },
+      1);
 }
 
 }  // namespace gbcc

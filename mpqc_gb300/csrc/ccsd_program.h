@@ -13,14 +13,19 @@ struct CcsdTensors {
   // inputs (constant after set_inputs), MPQC annotation order
   Tensor *Fia, *Fij, *Fab, *Gijab, *Gijkl, *Giajb, *Gijka, *Giabc, *Gabcd, *eps_o, *eps_v;
   Tensor *f_ai, *g_abij;  // Fia("i,a") as (a,i); Gijab("i,j,a,b") as (a,b,i,j)
+  Tensor *Dinv1, *Dinv2;  // reciprocal Jacobi denominators [v][o], [v][v][o][o]
   // amplitudes and residuals
   Tensor *t1, *t2, *tau, *r1, *r2;
   // intermediates
-  Tensor *tki, *FAB, *FIJ, *hkc, *r2u, *Y1, *Y2, *gki, *gac, *J, *K, *tmp, *W, *tmp2;
+  // (P = 2 j - k of the ring terms, k = K)
+  Tensor *tki, *FAB, *FIJ, *hkc, *r2u, *Y1, *Y2, *gki, *gac, *P, *K, *tmp, *W, *tmp2;
   // particle-particle ladder over pair-(anti)symmetric combinations: G+/G- of
   // Gabcd over (a <= b) x (c <= d) and of Giabc over (k a) x (c <= d)
   // (constants), tau+/tau- over (c <= d) x (i <= j), and the pair products
   Tensor *Gp, *Gm, *Gip, *Gim, *taup, *taum, *Bp, *Bm, *Xp, *Xm;
+  // hole-hole ladder over pair combinations (kernels.cu): Gijab's pair
+  // factors over (k <= l) x (c <= d) (constants) and W+- over (k <= l) x (i <= j)
+  Tensor *Gtp = nullptr, *Gtm = nullptr, *Wt = nullptr, *Wm = nullptr;
   // density-fitted inputs (naux > 0): three-index factors in MPQC order
   // Xai[K][a][i] = (K|ai), Xab[K][a][b] = (K|ab) instead of Giabc / Gabcd;
   // Giabc is built from them on the device, (ab|cd) never exists whole: the

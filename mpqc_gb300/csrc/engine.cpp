@@ -137,6 +137,7 @@ struct OperandPlan {
   int64_t rows = 0, K = 0;
   bool constant = false;
   bool direct = false;  // FP64: tensor storage used as the panel
+  bool inplace = false;  // small-K stream kernel: the one source read in place through its gather tables
   const double* dptr = nullptr;
   int64_t ld = 0;
   GatherArgs gather{};  // packing (FP64 panel or split slices)
@@ -653,6 +654,8 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
         OperandPlan& op = p.P[side];
         if (op.direct) {
           panel[side] = op.dptr;
+        } else if (op.inplace) {
+          panel[side] = op.gather.t[0].a;
         } else {
           double* w = side == 0 ? w64a_ : w64b_;
           GatherArgs g = op.gather;
@@ -679,9 +682,14 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       f.k_per_split = p.k_per_split;
       f.partial = wpart_;
       f.m_major = p.m_major ? 1 : 0;
+      if (p.P[0].inplace) {
+        f.a_ra = p.P[0].gather.t[0].ra;
+        f.a_ca = p.P[0].gather.t[0].ca;
+        f.lda = 0;
+      }
       prof_gemm(s);
       if (p.smallk) {
-        launch_gemm_smallk(f, stream_);
+        if (!launch_gemm_smallk(f, stream_)) throw Error(GBCC_ERR_STATE, "engine: in-place small-K operand off the stream kernel");
         ++n_launch_;
       } else {
         launch_gemm_f64(f, stream_);
@@ -736,7 +744,7 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
     // a short contraction into a large output is memory-bound: CUDA cores
     // (measured faster for N > 32; the tensor-core kernel wins below).  The
     // FP64-grade plan keeps such contractions on the FP64 kernel.
-    if (slices > 0 && !emu && K <= kSmallK && std::min(rowsA, rowsB) > 32 &&
+    if (slices > 0 && !emu && K <= kSmallK && std::min(rowsA, rowsB) >= 32 &&
         static_cast<double>(rowsA) * static_cast<double>(rowsB) >= 1048576.0) {
       slices = 0;
       p.smallk = true;
@@ -855,6 +863,11 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
       p.cm = upload(hm).d;
       p.cn = upload(hn).d;
     }
+    // a single-factor M operand contiguous along M (its pack would transpose)
+    // is read in place by the stream kernel: no FP64 panel written and read back
+    if (p.smallk && !p.P[0].direct && p.P[0].gather.plain && p.P[0].gather.transpose &&
+        smallk_streams(p.N, K, p.m_major))
+      p.P[0].inplace = true;
     if (!p.use_tc && !p.smallk) {
       // fewer 64 x 64 output tiles than two per SM: split K over blocks (one SM
       // runs FP64 at ~1/150 of the GPU's already low FP64 rate, so even a

@@ -242,51 +242,77 @@ __global__ void __launch_bounds__(256, 2) gemm_smallk_kernel(GemmF64Args g) {
 }
 
 // Short contractions whose C is contiguous along M (every short-K site of the
-// CCSD residual): B (N x K, rounded to FP32, K padded to 32) stays in shared
-// memory, each thread owns one row m of C and keeps that row of A in
-// registers, and walks C eight columns at a time.  The eight C loads of a
+// CCSD residual): B (N x K, rounded to FP32, K padded to KS = 32 or 64) stays
+// in shared memory, each thread owns one row m of C and keeps that row of A
+// in registers, and walks C eight columns at a time.  The eight C loads of a
 // group are issued before its dot products (which do not need them), and
-// three CTAs per SM keep enough of them in flight to stream C, the dominant
-// traffic (16 bytes per output against 8 per A element).  BETA 0: C = alpha
-// acc, 1: C += alpha acc, 2: C = beta C + alpha acc, one FP64 FMA per output
-// where beta is 0 or 1.
-constexpr int kStreamK = 32;
+// three CTAs per SM (two at KS = 64) keep enough of them in flight to stream
+// C, the dominant traffic (16 bytes per output against 8 per A element).
+// With a_ra set, A is read in place through its row and column offsets (the
+// K offsets staged in shared memory): for a source contiguous along M the
+// lanes of a warp read consecutive elements, and no packed panel is written.
+// BETA 0: C = alpha acc, 1: C += alpha acc, 2: C = beta C + alpha acc, one
+// FP64 FMA per output where beta is 0 or 1.
 constexpr int kStreamCols = 8;
 
-template <int BETA>
-__global__ void __launch_bounds__(256, 3) gemm_smallk_stream_kernel(GemmF64Args g) {
-  extern __shared__ float Bs[];  // [Npad][kStreamK]
+__device__ __forceinline__ void prefetch_l2(const double* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+template <int BETA, int KS, bool INPLACE>
+__global__ void __launch_bounds__(256, KS == 32 ? 3 : 2) gemm_smallk_stream_kernel(GemmF64Args g) {
+  extern __shared__ float Bs[];  // [Npad][KS], then KS K offsets of A
   const int K = static_cast<int>(g.K);
   const int64_t npad = (g.N + kStreamCols - 1) / kStreamCols * kStreamCols;
-  for (int64_t e = threadIdx.x; e < npad * kStreamK; e += blockDim.x) {
-    const int64_t n = e / kStreamK;
-    const int k = static_cast<int>(e % kStreamK);
+  int64_t* aca = reinterpret_cast<int64_t*>(Bs + npad * KS);
+  for (int64_t e = threadIdx.x; e < npad * KS; e += blockDim.x) {
+    const int64_t n = e / KS;
+    const int k = static_cast<int>(e % KS);
     Bs[e] = (n < g.N && k < K) ? d2f_rn(g.B[n * g.ldb + k]) : 0.f;
   }
+  if constexpr (INPLACE)
+    for (int k = threadIdx.x; k < KS; k += blockDim.x) aca[k] = k < K ? g.a_ca[k] : 0;
   __syncthreads();
   const int64_t mtiles = (g.M + blockDim.x - 1) / blockDim.x;
   for (int64_t t = blockIdx.x; t < mtiles; t += gridDim.x) {
     const int64_t m = t * blockDim.x + threadIdx.x;
     if (m >= g.M) continue;
-    float a[kStreamK];
+    float a[KS];
+    if constexpr (INPLACE) {
+      const double* arow = g.A + g.a_ra[m];
 #pragma unroll
-    for (int k = 0; k < kStreamK; ++k) a[k] = k < K ? d2f_rn(g.A[m * g.lda + k]) : 0.f;
+      for (int k = 0; k < KS; ++k) a[k] = k < K ? d2f_rn(arow[aca[k]]) : 0.f;
+    } else {
+#pragma unroll
+      for (int k = 0; k < KS; ++k) a[k] = k < K ? d2f_rn(g.A[m * g.lda + k]) : 0.f;
+    }
     double* crow = g.C + g.cm[m];
+    if constexpr (BETA != 0) {
+#pragma unroll
+      for (int j = kStreamCols; j < 2 * kStreamCols; ++j)
+        if (j < g.N) prefetch_l2(crow + g.cn[j]);
+    }
     for (int64_t n0 = 0; n0 < g.N; n0 += kStreamCols) {
       // (the column offsets are read again at the store, from L1, rather
       // than held: 8 live 64-bit offsets pushed the kernel into spills)
       double c[kStreamCols];
       if constexpr (BETA != 0) {
+        // C two groups ahead into L2, so that each group's loads hit L2
+#pragma unroll
+        for (int j = 0; j < kStreamCols; ++j) {
+          const int64_t n = n0 + 2 * kStreamCols + j;
+          if (n < g.N) prefetch_l2(crow + g.cn[n]);
+        }
 #pragma unroll
         for (int j = 0; j < kStreamCols; ++j) c[j] = n0 + j < g.N ? crow[g.cn[n0 + j]] : 0.0;
       }
       float acc[kStreamCols];
 #pragma unroll
       for (int j = 0; j < kStreamCols; ++j) {
-        const float4* b4 = reinterpret_cast<const float4*>(Bs + (n0 + j) * kStreamK);
+        const float4* b4 = reinterpret_cast<const float4*>(Bs + (n0 + j) * KS);
         float s = 0.f;
 #pragma unroll
-        for (int q = 0; q < kStreamK / 4; ++q) {
+        for (int q = 0; q < KS / 4; ++q) {
           const float4 b = b4[q];
           s = fmaf(a[4 * q], b.x, s);
           s = fmaf(a[4 * q + 1], b.y, s);
@@ -326,32 +352,52 @@ bool allow_stream_smem(K kernel) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024) == cudaSuccess;
 }
 
-void launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st) {
-  if (g.M <= 0 || g.N <= 0) return;
-  const int64_t npad = (g.N + kStreamCols - 1) / kStreamCols * kStreamCols;
-  const size_t smem = static_cast<size_t>(npad) * kStreamK * sizeof(float);
-  if (g.m_major && g.K <= kStreamK && smem <= 64 * 1024) {
-    const int64_t mtiles = (g.M + 255) / 256;
-    const unsigned grid = static_cast<unsigned>(std::min<int64_t>(mtiles, static_cast<int64_t>(num_sms()) * 3));
-    if (g.beta == 0.0) {
-      static const bool attr0 = allow_stream_smem(gemm_smallk_stream_kernel<0>);
-      (void)attr0;
-      gemm_smallk_stream_kernel<0><<<grid, 256, smem, st>>>(g);
-    } else if (g.beta == 1.0) {
-      static const bool attr1 = allow_stream_smem(gemm_smallk_stream_kernel<1>);
-      (void)attr1;
-      gemm_smallk_stream_kernel<1><<<grid, 256, smem, st>>>(g);
+template <int BETA, int KS, bool INPLACE>
+void launch_stream_k(const GemmF64Args& g, unsigned grid, size_t smem, cudaStream_t st) {
+  static const bool attr = allow_stream_smem(gemm_smallk_stream_kernel<BETA, KS, INPLACE>);
+  (void)attr;
+  gemm_smallk_stream_kernel<BETA, KS, INPLACE><<<grid, 256, smem, st>>>(g);
+}
+
+template <int KS, bool INPLACE>
+void launch_stream(const GemmF64Args& g, size_t smem, cudaStream_t st) {
+  const int64_t mtiles = (g.M + 255) / 256;
+  const unsigned grid =
+      static_cast<unsigned>(std::min<int64_t>(mtiles, static_cast<int64_t>(num_sms()) * (KS == 32 ? 3 : 2)));
+  if (g.beta == 0.0) launch_stream_k<0, KS, INPLACE>(g, grid, smem, st);
+  else if (g.beta == 1.0) launch_stream_k<1, KS, INPLACE>(g, grid, smem, st);
+  else launch_stream_k<2, KS, INPLACE>(g, grid, smem, st);
+}
+
+size_t stream_smem(int64_t N, int64_t K) {
+  const int64_t npad = (N + kStreamCols - 1) / kStreamCols * kStreamCols;
+  const int64_t ks = K <= 32 ? 32 : 64;
+  return static_cast<size_t>(npad * ks) * sizeof(float) + static_cast<size_t>(ks) * sizeof(int64_t);
+}
+
+bool smallk_streams(int64_t N, int64_t K, bool m_major) {
+  return m_major && K <= 64 && stream_smem(N, K) <= 64 * 1024;
+}
+
+bool launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st) {
+  if (g.M <= 0 || g.N <= 0) return true;
+  if (smallk_streams(g.N, g.K, g.m_major != 0)) {
+    const size_t smem = stream_smem(g.N, g.K);
+    if (g.K <= 32) {
+      if (g.a_ra) launch_stream<32, true>(g, smem, st);
+      else launch_stream<32, false>(g, smem, st);
     } else {
-      static const bool attr2 = allow_stream_smem(gemm_smallk_stream_kernel<2>);
-      (void)attr2;
-      gemm_smallk_stream_kernel<2><<<grid, 256, smem, st>>>(g);
+      if (g.a_ra) launch_stream<64, true>(g, smem, st);
+      else launch_stream<64, false>(g, smem, st);
     }
-    return;
+    return true;
   }
+  if (g.a_ra) return false;  // A in place: stream kernel only
   if (g.N <= 32)
     launch_smallk_tiles<128, 32>(g, st);
   else
     launch_smallk_tiles<64, 64>(g, st);
+  return true;
 }
 
 void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st) {

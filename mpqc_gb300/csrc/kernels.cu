@@ -239,6 +239,67 @@ __global__ void __launch_bounds__(kThreads) build_gpm_chem_kernel(int64_t n, con
   }
 }
 
+// Hole-hole ladder over pair combinations.  With W(k,l,i,j) = W(l,k,j,i) and
+// pair-symmetric tau, sum_kl tau(a,b,k,l) W(k,l,i,j) splits like the
+// particle-particle ladder: over k <= l into tau+(ab,kl) W+(kl,ij) and over
+// k < l into tau-(ab,kl) W-(kl,ij), where tau+- are the ladder's taup / taum
+// (tau(a,b,l,k) = tau(b,a,k,l)) and W+ = W(kl,ij) + W(lk,ij) (W(kk,ij) on the
+// diagonal), W- = W(kl,ij) - W(lk,ij); the products are symmetric /
+// antisymmetric in a <-> b and in i <-> j, so they add to the ladder's Bp / Bm.
+// The part sum_cd Gijab(k,l,c,d) tau(c,d,i,j) of W+- is itself a pair
+// product: <lk|cd> = <kl|dc> gives W+ = c_kl G+(kl,cd) tau+(cd,ij) and
+// W- = 2 G-(kl,cd) tau-(cd,ij), with G+- = G(kl,cd) +- G(kl,dc) (G(kl,cc) on
+// the diagonal) and c_kl = 2 (k < l) or 1 (k = l).
+//
+// Gtp[sym(k,l)][sym(c,d)] = c_kl G+, Gtm[anti(k,l)][anti(c,d)] = 2 G- from
+// Gijab[k][l][c][d]; one block per k <= l.
+__global__ void __launch_bounds__(kThreads) build_gpm_oo_kernel(int64_t o, int64_t v, const double* __restrict__ G,
+                                                                double* __restrict__ Gtp,
+                                                                double* __restrict__ Gtm) {
+  const int64_t np = v * (v + 1) / 2, nm = v * (v - 1) / 2;
+  for (int64_t row = blockIdx.x; row < o * o; row += gridDim.x) {
+    int64_t k, l;
+    divmod32(row, o, k, l);
+    if (k > l) continue;
+    const double* g = G + row * v * v;
+    double* gp = Gtp + pair_sym(k, l, o) * np;
+    double* gm = (Gtm && k < l) ? Gtm + pair_anti(k, l, o) * nm : nullptr;
+    const int sk = k < l ? 1 : 0;  // c_kl = 2^sk
+    for (int64_t c = 0; c < v; ++c) {
+      for (int64_t d = c + threadIdx.x; d < v; d += blockDim.x) {
+        const double x = g[c * v + d], y = g[d * v + c];
+        gp[pair_sym(c, d, v)] = scale_pow2(c < d ? x + y : x, sk);
+        if (gm && c < d) gm[pair_anti(c, d, v)] = scale_pow2(x - y, 1);
+      }
+    }
+  }
+}
+
+// Wt[sym(k,l)][sym(i,j)] = W(k,l,i,j) + W(l,k,i,j) (W(k,k,i,j) for k = l) and
+// Wm[anti(k,l)][anti(i,j)] = W(k,l,i,j) - W(l,k,i,j), from W[o][o][o][o];
+// one block per k <= l.
+__global__ void __launch_bounds__(kThreads) pair_combine_oo_kernel(int64_t o, const double* __restrict__ W,
+                                                                   double* __restrict__ Wt,
+                                                                   double* __restrict__ Wm) {
+  const int64_t o2 = o * o, sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
+  for (int64_t row = blockIdx.x; row < o2; row += gridDim.x) {
+    int64_t k, l;
+    divmod32(row, o, k, l);
+    if (k > l) continue;
+    const double* x = W + (k * o + l) * o2;
+    const double* y = W + (l * o + k) * o2;
+    double* wt = Wt + pair_sym(k, l, o) * sp;
+    double* wm = (Wm && k < l) ? Wm + pair_anti(k, l, o) * sm : nullptr;
+    for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
+      int64_t i, j;
+      divmod32(ij, o, i, j);
+      if (i > j) continue;
+      wt[pair_sym(i, j, o)] = k < l ? x[ij] + y[ij] : x[ij];
+      if (wm && i < j) wm[pair_anti(i, j, o)] = x[ij] - y[ij];
+    }
+  }
+}
+
 // One block per (c <= d): taup[sym(c,d)][sym(i,j)], taum[anti(c,d)][anti(i,j)].
 __global__ void __launch_bounds__(kThreads) tau_pm_kernel(int64_t o, int64_t v, const double* __restrict__ tau,
                                                           double* __restrict__ taup, double* __restrict__ taum) {
@@ -301,6 +362,85 @@ __global__ void __launch_bounds__(kThreads) pair_unpack_kernel(int64_t rows_v, i
   }
 }
 
+// The last pass of r2 (ccsd_r1_r2.h:254-262 and the ladder's unpack):
+//   r2(a,b,i,j) (+)= Q(a,b,i,j) + g_abij(a,b,i,j) + P(a,b,i,j),
+//   Q(a,b,i,j) = q(a,b,i,j) + q(b,a,j,i),  q = r2u - 0.5 tmp - tmp(b,a,i,j),
+// i.e. the symmetrisation r2u(a,b,i,j) + r2u(b,a,j,i) after r2u -= 0.5
+// tmp(a,b,i,j) + tmp(b,a,i,j), with P the unpack of pair_unpack_kernel (Bp
+// null: none).  Q(b,a,j,i) = Q(a,b,i,j) operand for operand, so one block
+// per pair a <= b and 32 x 32 tile (I, J) of (i, j) stages q of the tile
+// [a][b][I][J] and of [b][a][J][I] in shared memory (coalesced along j and
+// along i) and adds the same Q to r2[a][b][I][J] and to r2[b][a][J][I]: every
+// r2u, tmp and g element is read once, r2 read and written once.  On the
+// diagonal a = b only tiles I <= J are taken, and a tile I = J once.
+__global__ void __launch_bounds__(256) r2_assemble_kernel(int64_t o, int64_t v, const double* __restrict__ r2u,
+                                                          const double* __restrict__ tmp,
+                                                          const double* __restrict__ g,
+                                                          const double* __restrict__ Bp,
+                                                          const double* __restrict__ Bm, bool accumulate,
+                                                          double* __restrict__ r2) {
+  __shared__ double sq[32][33];  // [i][j] of q(a,b,.,.)
+  __shared__ double sr[32][33];  // [j][i] of q(b,a,.,.)
+  const int64_t o2 = o * o, nt = (o + 31) / 32, nt2 = nt * nt;
+  const int64_t sp = o * (o + 1) / 2, sm = o * (o - 1) / 2;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int64_t x = blockIdx.x; x < v * v * nt2; x += gridDim.x) {
+    int64_t p, t, a, b, I, J;
+    divmod32(x, nt2, p, t);
+    divmod32(p, v, a, b);
+    if (a > b) continue;
+    divmod32(t, nt, I, J);
+    if (a == b && I > J) continue;
+    const int64_t i0 = I * 32, j0 = J * 32;
+    const int64_t ab = (a * v + b) * o2, ba = (b * v + a) * o2;
+    for (int k = ty; k < 32; k += 8) {
+      const int64_t i = i0 + k, j = j0 + tx;
+      if (i < o && j < o) {
+        const int64_t e = i * o + j;
+        sq[k][tx] = fma(-0.5, tmp[ab + e], r2u[ab + e]) - tmp[ba + e];
+      }
+      const int64_t jj = j0 + k, ii = i0 + tx;
+      if (jj < o && ii < o) {
+        const int64_t e = jj * o + ii;
+        sr[k][tx] = fma(-0.5, tmp[ba + e], r2u[ba + e]) - tmp[ab + e];
+      }
+    }
+    __syncthreads();
+    const double* bp = Bp ? Bp + pair_sym(a, b, v) * sp : nullptr;
+    const double* bm = (Bp && Bm && a < b) ? Bm + pair_anti(a, b, v) * sm : nullptr;
+    // P(a,b,i,j) = P(b,a,j,i): the B- term changes sign with i > j (a < b)
+    auto unpack = [&](int64_t i, int64_t j) {
+      const int64_t li = i < j ? i : j, hj = i < j ? j : i;
+      double val = bp[pair_sym(li, hj, o)];
+      if (bm && li < hj) val += flip_sign(bm[pair_anti(li, hj, o)], i > j);
+      return val;
+    };
+    // r2[a][b][I][J], lanes along j
+    for (int k = ty; k < 32; k += 8) {
+      const int64_t i = i0 + k, j = j0 + tx;
+      if (i < o && j < o) {
+        double val = (sq[k][tx] + sr[tx][k]) + g[ab + i * o + j];
+        if (bp) val += unpack(i, j);
+        double* out = r2 + ab + i * o + j;
+        *out = accumulate ? *out + val : val;
+      }
+    }
+    // r2[b][a][J][I], lanes along i
+    if (a != b || I != J) {
+      for (int k = ty; k < 32; k += 8) {
+        const int64_t j = j0 + k, i = i0 + tx;
+        if (i < o && j < o) {
+          double val = (sq[tx][k] + sr[k][tx]) + g[ba + j * o + i];
+          if (bp) val += unpack(i, j);
+          double* out = r2 + ba + j * o + i;
+          *out = accumulate ? *out + val : val;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // r1(a,i) += sum_k 2 tmp2(k,a,k,i) - tmp2(k,a,i,k) with tmp2[o][v][o][o]: the
 // (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i) term of r1 read off the
 // ladder's tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j), using
@@ -344,6 +484,30 @@ __global__ void __launch_bounds__(kThreads) jacobi_inplace_kernel(int64_t o, int
     int64_t a, i;
     divmod32(e, o, a, i);
     t1[e] += r1[e] / (eps_o[i] - eps_v[a]);
+  }
+}
+
+// dinv2[a][b][i][j] = 1 / (eps_o[i] + eps_o[j] - eps_v[a] - eps_v[b]),
+// dinv1[a][i] = 1 / (eps_o[i] - eps_v[a])
+__global__ void __launch_bounds__(kThreads) denominators_kernel(int64_t o, int64_t v, const double* eps_o,
+                                                                const double* eps_v, double* dinv1,
+                                                                double* dinv2) {
+  const int64_t o2 = o * o;
+  for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
+    int64_t a, b;
+    divmod32(p, v, a, b);
+    const double eab = eps_v[a] + eps_v[b];
+    for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
+      int64_t i, j;
+      divmod32(ij, o, i, j);
+      dinv2[p * o2 + ij] = 1.0 / (eps_o[i] + eps_o[j] - eab);
+    }
+  }
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < v * o;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int64_t a, i;
+    divmod32(e, o, a, i);
+    dinv1[e] = 1.0 / (eps_o[i] - eps_v[a]);
   }
 }
 
@@ -446,16 +610,10 @@ __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) 
   double* x2n = d.x2 + static_cast<int64_t>(slot) * n2;
   double* e2n = d.e2 + static_cast<int64_t>(slot) * n2;
   for (int64_t p = blockIdx.x; p < v * v; p += gridDim.x) {
-    int64_t a, b;
-    divmod32(p, v, a, b);
-    const double eab = d.eps_v[a] + d.eps_v[b];
     for (int64_t ij = threadIdx.x; ij < o2; ij += blockDim.x) {
-      int64_t i, j;
-      divmod32(ij, o, i, j);
       const int64_t e = p * o2 + ij;
       const double r = d.r2[e];
-      const double den = d.eps_o[i] + d.eps_o[j] - eab;
-      x2n[e] = d.t2[e] + r / den;
+      x2n[e] = fma(r, d.dinv2[e], d.t2[e]);
       e2n[e] = r;
 #pragma unroll
       for (int q = 0; q < kDiisMax; ++q) {
@@ -471,10 +629,8 @@ __global__ void __launch_bounds__(kThreads) diis_jacobi_dots_kernel(DiisArgs d) 
   double* e1n = d.e1 + static_cast<int64_t>(slot) * n1;
   for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n1;
        e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    int64_t a, i;
-    divmod32(e, o, a, i);
     const double r = d.r1[e];
-    x1n[e] = d.t1[e] + r / (d.eps_o[i] - d.eps_v[a]);
+    x1n[e] = fma(r, d.dinv1[e], d.t1[e]);
     e1n[e] = r;
 #pragma unroll
     for (int q = 0; q < kDiisMax; ++q) {
@@ -740,6 +896,14 @@ void launch_build_gpm(int64_t rows_v, int64_t v, bool ab_pairs, const double* G,
   build_gpm_kernel<<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, ab_pairs, G, Gp, Gm);
 }
 
+void launch_build_gpm_oo(int64_t o, int64_t v, const double* Gijab, double* Gtp, double* Gtm, cudaStream_t st) {
+  build_gpm_oo_kernel<<<grid_for(o * o, 1), kThreads, 0, st>>>(o, v, Gijab, Gtp, Gtm);
+}
+
+void launch_pair_combine_oo(int64_t o, const double* W, double* Wt, double* Wm, cudaStream_t st) {
+  pair_combine_oo_kernel<<<grid_for(o * o, 1), kThreads, 0, st>>>(o, W, Wt, Wm);
+}
+
 void launch_build_gpm_chem(int64_t n, const double* G, double* Gp, double* Gm, cudaStream_t st) {
   build_gpm_chem_kernel<<<grid_for(n * n, 1), kThreads, 0, st>>>(n, G, Gp, Gm);
 }
@@ -762,8 +926,20 @@ void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, con
     pair_unpack_kernel<true><<<grid_for(rows_v * v, 1), kThreads, 0, st>>>(rows_v, v, o, ab_pairs, Bp, Bm, out);
 }
 
+void launch_r2_assemble(int64_t o, int64_t v, const double* r2u, const double* tmp, const double* g,
+                        const double* Bp, const double* Bm, bool accumulate, double* r2, cudaStream_t st) {
+  const int64_t nt = (o + 31) / 32;
+  const unsigned grid = static_cast<unsigned>(std::min<int64_t>(v * v * nt * nt, 152LL * 16));
+  r2_assemble_kernel<<<grid, dim3(32, 8), 0, st>>>(o, v, r2u, tmp, g, Bp, Bm, accumulate, r2);
+}
+
 void launch_r1_from_tmp2(int64_t o, int64_t v, const double* tmp2, double* r1, cudaStream_t st) {
   r1_from_tmp2_kernel<<<grid_for(v * o, kThreads), kThreads, 0, st>>>(o, v, tmp2, r1);
+}
+
+void launch_denominators(int64_t o, int64_t v, const double* eps_o, const double* eps_v, double* dinv1,
+                         double* dinv2, cudaStream_t st) {
+  denominators_kernel<<<grid_for(v * v, 1), kThreads, 0, st>>>(o, v, eps_o, eps_v, dinv1, dinv2);
 }
 
 void launch_jacobi_inplace(int64_t o, int64_t v, const double* eps_o, const double* eps_v, const double* r1,

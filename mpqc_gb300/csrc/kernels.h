@@ -160,6 +160,10 @@ struct GemmF64Args {
   const int64_t* cn;
   double alpha, beta;
   int m_major;           // C unit-stride along M (small-K kernel: lanes along M)
+  // small-K stream kernel: A read in place, A[m][k] = A[a_ra[m] + a_ca[k]]
+  // (null: A is an lda-strided panel)
+  const int64_t* a_ra;
+  const int64_t* a_ca;
 };
 void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st);
 
@@ -169,7 +173,11 @@ void launch_gemm_f64(const GemmF64Args& g, cudaStream_t st);
 // instead of the tensor-core pipeline, whose per-tile handshakes leave such
 // outputs latency-bound.  Same argument conventions as launch_gemm_f64 (no K split).
 constexpr int64_t kSmallK = 64;
-void launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st);
+// whether launch_gemm_smallk takes the stream kernel (C contiguous along M,
+// K <= 64, B within 64 KB of shared memory): the only one that reads A in place
+bool smallk_streams(int64_t N, int64_t K, bool m_major);
+// false (nothing launched) when A is read in place and the stream kernel does not apply
+bool launch_gemm_smallk(const GemmF64Args& g, cudaStream_t st);
 
 // ---------------------------------------------------------------------------
 // Split-BF16 tcgen05 GEMM (sm_103a):
@@ -261,9 +269,23 @@ void launch_build_gpm_rows(int64_t a0, int64_t a1, int64_t v, const double* Gblk
                            cudaStream_t st);
 // G+ / G- over n atomic-orbital pairs from G[p][q][r][s] = (pq|rs) (chemists' order)
 void launch_build_gpm_chem(int64_t n, const double* G, double* Gp, double* Gm, cudaStream_t st);
+// Hole-hole ladder pair factors: Gtp[sym(k,l)][sym(c,d)] = c_kl (G(kl,cd) +
+// G(kl,dc)) (c = d: G(kl,cc); c_kl = 2 for k < l, 1 for k = l) and
+// Gtm[anti(k,l)][anti(c,d)] = 2 (G(kl,cd) - G(kl,dc)) from Gijab[k][l][c][d]
+// (Gtm null: not built)
+void launch_build_gpm_oo(int64_t o, int64_t v, const double* Gijab, double* Gtp, double* Gtm, cudaStream_t st);
+// Wt[sym(k,l)][sym(i,j)] = W(klij) + W(lkij) (W(kkij) for k = l), Wm[anti(k,l)][anti(i,j)] =
+// W(klij) - W(lkij) from W[o][o][o][o] (Wm null: not formed)
+void launch_pair_combine_oo(int64_t o, const double* W, double* Wt, double* Wm, cudaStream_t st);
 void launch_tau_pm(int64_t o, int64_t v, const double* tau, double* taup, double* taum, cudaStream_t st);
 void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, const double* Bp, const double* Bm,
                         double beta, double* out, cudaStream_t st);
+
+// r2(a,b,i,j) (+)= q(a,b,i,j) + q(b,a,j,i) + g(a,b,i,j) + unpack(Bp, Bm)(a,b,i,j),
+// q = r2u - 0.5 tmp - tmp(b,a,i,j); Bp null: no unpack, Bm null: no B- part;
+// accumulate: add to r2, else overwrite it
+void launch_r2_assemble(int64_t o, int64_t v, const double* r2u, const double* tmp, const double* g,
+                        const double* Bp, const double* Bm, bool accumulate, double* r2, cudaStream_t st);
 
 // r1(a,i) += sum_k 2 tmp2(k,a,k,i) - tmp2(k,a,i,k), tmp2[o][v][o][o], r1[v][o]
 void launch_r1_from_tmp2(int64_t o, int64_t v, const double* tmp2, double* r1, cudaStream_t st);
@@ -302,6 +324,10 @@ struct DiisArgs {
   int64_t o, v;
   const double* eps_o;
   const double* eps_v;
+  // reciprocal denominators 1 / (eps_o[i] - eps_v[a]) [v][o] and
+  // 1 / (eps_o[i] + eps_o[j] - eps_v[a] - eps_v[b]) [v][v][o][o]
+  const double* dinv1;
+  const double* dinv2;
   const double* t1;
   const double* t2;
   const double* r1;
@@ -322,6 +348,13 @@ struct DiisArgs {
   int* nskip_out;      // device int
 };
 void launch_diis_step(const DiisArgs& d, cudaStream_t st);
+
+// dinv1 = 1 / D1, dinv2 = 1 / D2 (the Jacobi denominators of DiisArgs), once
+// per set of orbital energies: the iteration then multiplies, and the FP64
+// pipe that a division per element would occupy (a sequence of FP64
+// instructions on a GPU whose FP64 rate is 1/64 of FP32) is left to the dots
+void launch_denominators(int64_t o, int64_t v, const double* eps_o, const double* eps_v, double* dinv1,
+                         double* dinv2, cudaStream_t st);
 
 // t1 = sum_j coef[j] x1_j, t2 = sum_j coef[j] x2_j, tau = t2 + t1 t1
 // (dyn non-NULL: nvec and slots read from device memory)

@@ -46,10 +46,13 @@ def test_residual_fp64_random(o, v, naux):
 
 
 @pytest.mark.parametrize("slices", [3, 2, 1])
-@pytest.mark.parametrize("o,v,naux", [(4, 9, 12), (8, 40, 30), (12, 70, 60), (16, 72, 40)])
+@pytest.mark.parametrize("o,v,naux", [(4, 9, 12), (8, 40, 30), (12, 70, 60), (16, 72, 40), (32, 40, 30),
+                                      (40, 48, 30)])
 def test_residual_mixed(o, v, naux, slices):
     """(16, 72): the short (K = o) contractions into o^2 v^2 outputs run on the
-    CUDA-core kernel; every size runs the tensor-core contractions."""
+    CUDA-core stream kernel; (32, 40): also the one with N = o = 32, its t2
+    operand read in place; (40, 48): K = o = 40 (the kernel's 64-wide form).
+    Every size runs the tensor-core contractions."""
     inp = synth.make_inputs(o, v, naux, seed=o * 10 + v, t1_scale=1e-2)
     r1_ref, r2_ref = R.residual(inp.t1, inp.t2, oracle_ints(inp))
     with _solver(inp, precision="mixed", slices=(slices,) * 3) as s:
