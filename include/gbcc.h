@@ -327,6 +327,18 @@ gbcc_status gbcc_slice_policy(gbcc_handle* h, int32_t slices[3], double rel_chan
  * amplitudes gbcc_set_inputs used, e.g. before evaluating residuals at given
  * amplitudes with gbcc_residual.  Same rule as above; leaves t = 0 in the
  * handle.  No reference counterpart. */
+/* The autotune table (config autotune): every tensor-core contraction timed
+ * by any handle of the process is recorded by shape (SM count, term class,
+ * M x N x K, slice count, output orientation), and handles created later take
+ * the recorded tile untimed.  gbcc_autotune_save writes the table as text;
+ * gbcc_autotune_load merges a file written by gbcc_autotune_save
+ * (GBCC_ERR_INVALID_ARG, table unchanged, if it cannot be read or is
+ * malformed); gbcc_autotune_clear empties it.  No counterpart in the
+ * reference (TiledArray picks no tiles at run time). */
+gbcc_status gbcc_autotune_save(const char* path);
+gbcc_status gbcc_autotune_load(const char* path);
+gbcc_status gbcc_autotune_clear(void);
+
 gbcc_status gbcc_calibrate_slices(gbcc_handle* h, const double* t1_ai, const double* t2_abij);
 
 /* Message of the last failing call on this handle ("" if none); with a NULL

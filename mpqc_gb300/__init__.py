@@ -9,8 +9,10 @@ mirror of the reference interface.  Build the library with
 """
 from . import basis, molecules, synth  # noqa: F401
 from ._lib import LIB_PATH, GbccError, load  # noqa: F401
-from .ccsd import CCSD, CCSD_T, FeatureDisabled, InputError, Solver, compute_cs_ccsd_r1_r2, solve_batch  # noqa: F401
+from .ccsd import (CCSD, CCSD_T, FeatureDisabled, InputError, Solver, autotune_clear, autotune_load,  # noqa: F401
+                   autotune_save, compute_cs_ccsd_r1_r2, solve_batch)
 from .scf import RHF, ccsd_energy  # noqa: F401
 
 __all__ = ["CCSD", "Solver", "compute_cs_ccsd_r1_r2", "GbccError", "InputError", "FeatureDisabled",
-           "RHF", "ccsd_energy", "load", "LIB_PATH", "synth", "basis", "molecules"]
+           "RHF", "ccsd_energy", "load", "LIB_PATH", "synth", "basis", "molecules", "autotune_save",
+           "autotune_load", "autotune_clear"]

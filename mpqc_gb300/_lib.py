@@ -28,7 +28,7 @@ EXPORTS = (
     "gbcc_residual_ex", "gbcc_energy", "gbcc_energy_noalloc", "gbcc_solve", "gbcc_destroy",
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error", "gbcc_set_amplitudes",
     "gbcc_save_amplitudes", "gbcc_load_amplitudes", "gbcc_set_df_inputs", "gbcc_set_direct_inputs",
-    "gbcc_solve_batch", "gbcc_triples",
+    "gbcc_solve_batch", "gbcc_triples", "gbcc_autotune_save", "gbcc_autotune_load", "gbcc_autotune_clear",
 )
 # every symbol include/gbcc_scf.h declares
 SCF_EXPORTS = (
@@ -196,6 +196,11 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_destroy.argtypes = [vp]
     lib.gbcc_calibrate_slices.restype = C.c_int
     lib.gbcc_calibrate_slices.argtypes = [vp, vp, vp]
+    for name in ("gbcc_autotune_save", "gbcc_autotune_load"):
+        getattr(lib, name).restype = C.c_int
+        getattr(lib, name).argtypes = [C.c_char_p]
+    lib.gbcc_autotune_clear.restype = C.c_int
+    lib.gbcc_autotune_clear.argtypes = []
     lib.gbcc_slice_policy.restype = C.c_int
     lib.gbcc_slice_policy.argtypes = [vp, vp, vp]
     lib.gbcc_last_error.restype = C.c_char_p

@@ -302,6 +302,26 @@ def _report(rep):
                   rep.seconds_residual_fp64)
 
 
+def autotune_save(path):
+    """Write the process's autotune table (tile choices of every tensor-core
+    contraction timed so far, by shape) to ``path``."""
+    lib = L.load()
+    _check(lib, None, lib.gbcc_autotune_save(str(path).encode()))
+
+
+def autotune_load(path):
+    """Merge a table written by autotune_save: handles created afterwards take
+    the stored tiles of matching contractions without timing them."""
+    lib = L.load()
+    _check(lib, None, lib.gbcc_autotune_load(str(path).encode()))
+
+
+def autotune_clear():
+    """Forget every recorded autotune choice of the process."""
+    lib = L.load()
+    _check(lib, None, lib.gbcc_autotune_clear())
+
+
 def solve_batch(solvers):
     """Solve several independent handles at once (``gbcc_solve_batch``): each
     handle's solve runs on its own stream from its own host thread, so small

@@ -1274,6 +1274,32 @@ gbcc_status gbcc_load_amplitudes(gbcc_handle* h, const char* path, double* e_cor
   });
 }
 
+gbcc_status gbcc_autotune_save(const char* path) {
+  if (!path) {
+    gbcc_set_thread_error("gbcc_autotune_save: NULL path");
+    return GBCC_ERR_INVALID_ARG;
+  }
+  if (!gbcc::tune_save(path)) {
+    gbcc_set_thread_error(std::string("gbcc_autotune_save: cannot write ") + path);
+    return GBCC_ERR_INVALID_ARG;
+  }
+  return GBCC_OK;
+}
+
+gbcc_status gbcc_autotune_load(const char* path) {
+  if (!path || !gbcc::tune_load(path)) {
+    gbcc_set_thread_error(std::string("gbcc_autotune_load: cannot read an autotune table from ") +
+                          (path ? path : "NULL"));
+    return GBCC_ERR_INVALID_ARG;
+  }
+  return GBCC_OK;
+}
+
+gbcc_status gbcc_autotune_clear(void) {
+  gbcc::tune_clear();
+  return GBCC_OK;
+}
+
 gbcc_status gbcc_calibrate_slices(gbcc_handle* h, const double* t1_ai, const double* t2_abij) {
   return guarded(h, [&]() -> gbcc_status {
     if (!h->inputs_set) throw Error(GBCC_ERR_STATE, "gbcc_calibrate_slices: inputs not set");

@@ -276,28 +276,35 @@ void residual_program(Engine& E, const CcsdTensors& S) {
              {{1.0, ix(tau, "cakl")}}, O);
 
   // ----- R2 (ccsd_r1_r2.h:198-293) -----
-  // J, K and r2u each receive their first (beta = 0) value from a ring
+  // K, P and r2u each receive their first (beta = 0) value from a ring
   // contraction and the cheaper terms accumulate after it: a tensor-core
   // product that stores C runs ~0.5 ms faster at o=32 v=320 than one that
   // reads and adds to it, while an elementwise pass pays little for the read.
   const Tensor& r2u = *S.r2u;
-  const Tensor &J = *S.P, &K = *S.K;
+  const Tensor &P = *S.P, &K = *S.K;
   // j and k intermediates (:229-249) with T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l),
-  // packed from its two terms where it is used (not stored)
+  // packed from its two terms where it is used (not stored).  j enters r2 only
+  // as P(a,k,i,c) = 2 j(a,k,i,c) - k(k,a,i,c), whose ring part
+  //   -2 G_cd T + (2 G_cd - G_dc) t2(a,d,i,l) + G_dc T = (2 G_cd - G_dc) (t2(a,d,i,l) - T)
+  // (G_cd = Gijab(k,l,c,d), G_dc = Gijab(k,l,d,c), summed over l, d) is one
+  // contraction instead of j's two and a share of k's
   const std::vector<Lin> T = {{0.5, ix(t2, "dail")}, lin2(1.0, ix(t1, "di"), ix(t1, "al"))};
-  E.contract(ix(J, "akic"), 0.0, -1.0, {{1.0, ix(Gijab, "klcd")}}, T, R);
-  E.contract(ix(J, "akic"), 1.0, 0.5, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "kldc")}},
-             {{1.0, ix(t2, "adil")}}, R);
-  E.assign(ix(J, "akic"), 1.0, {f1(1.0, ix(Gijab, "ikac"))});
-  E.contract(ix(J, "akic"), 1.0, -1.0, {{1.0, ix(Gijka, "lkic")}}, {{1.0, ix(t1, "al")}}, O);
-  E.contract(ix(J, "akic"), 1.0, 1.0, {{1.0, ix(Giabc, "kacd")}}, {{1.0, ix(t1, "di")}}, O);
   E.contract(ix(K, "kaic"), 0.0, -1.0, {{1.0, ix(Gijab, "kldc")}}, T, R);
   E.assign(ix(K, "kaic"), 1.0, {f1(1.0, ix(Giajb, "kaic"))});
   E.contract(ix(K, "kaic"), 1.0, -1.0, {{1.0, ix(Gijka, "klic")}}, {{1.0, ix(t1, "al")}}, O);
   E.contract(ix(K, "kaic"), 1.0, 1.0, {{1.0, ix(Giabc, "kadc")}}, {{1.0, ix(t1, "di")}}, O);
+  E.contract(ix(P, "akic"), 0.0, 1.0, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "kldc")}},
+             {{1.0, ix(t2, "adil")}, {-0.5, ix(t2, "dail")}, lin2(-1.0, ix(t1, "di"), ix(t1, "al"))}, R);
+  // the rest of 2 j - k: 2 Gijab(i,k,a,c) - Giajb(k,a,i,c) - (2 Gijka(l,k,i,c) -
+  // Gijka(k,l,i,c)) t1(a,l) + (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) t1(d,i)
+  E.assign(ix(P, "akic"), 1.0, {f1(2.0, ix(Gijab, "ikac")), f1(-1.0, ix(Giajb, "kaic"))});
+  E.contract(ix(P, "akic"), 1.0, -1.0, {{2.0, ix(Gijka, "lkic")}, {-1.0, ix(Gijka, "klic")}},
+             {{1.0, ix(t1, "al")}}, O);
+  E.contract(ix(P, "akic"), 1.0, 1.0, {{2.0, ix(Giabc, "kacd")}, {-1.0, ix(Giabc, "kadc")}},
+             {{1.0, ix(t1, "di")}}, O);
   // r2 += 0.5 (2 j(a,k,i,c) - k(k,a,i,c)) (2 t2(c,b,k,j) - t2(b,c,k,j))   (:251-252)
-  E.contract(ix(r2u, "abij"), 0.0, 0.5, {{2.0, ix(J, "akic")}, {-1.0, ix(K, "kaic")}},
-             {{2.0, ix(t2, "cbkj")}, {-1.0, ix(t2, "bckj")}}, R);
+  E.contract(ix(r2u, "abij"), 0.0, 0.5, {{1.0, ix(P, "akic")}}, {{2.0, ix(t2, "cbkj")}, {-1.0, ix(t2, "bckj")}},
+             R);
   // permutation part (:206-212)
   // r2u -= Y1(k,a,j,i) t1(b,k) [image of Y1(k,b,i,j) t1(a,k)] + Gijka(j,i,k,a) t1(b,k)
   //        + Y2(i,k,a,j) t1(b,k) + tmp2(k,a,j,i) t1(b,k) [the ladder's t1 terms, :278-280]

@@ -3,10 +3,66 @@
 
 #include <algorithm>
 #include <cstring>
+#include <fstream>
 #include <map>
+#include <mutex>
 #include <sstream>
 
 namespace gbcc {
+
+// Autotune choices shared by every handle of the process, by contraction
+// shape: a handle whose contractions were timed before (by another handle, or
+// in an earlier process whose table was saved and loaded) takes the stored
+// tile instead of timing its candidates again.
+namespace {
+struct TuneChoice {
+  int bn, ksplit, sps, group;
+  int64_t kps;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneChoice>& tune_table() {
+  static std::map<std::string, TuneChoice> t;
+  return t;
+}
+}  // namespace
+
+bool tune_save(const std::string& path) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::ofstream f(path);
+  if (!f) return false;
+  f << "gbcc-autotune 1\n";
+  for (const auto& kv : tune_table())
+    f << kv.first << ' ' << kv.second.bn << ' ' << kv.second.ksplit << ' ' << kv.second.kps << ' '
+      << kv.second.sps << ' ' << kv.second.group << '\n';
+  return static_cast<bool>(f);
+}
+
+bool tune_load(const std::string& path) {
+  std::ifstream f(path);
+  if (!f) return false;
+  std::string line;
+  if (!std::getline(f, line) || line != "gbcc-autotune 1") return false;
+  std::map<std::string, TuneChoice> add;
+  while (std::getline(f, line)) {
+    if (line.empty()) continue;
+    std::istringstream is(line);
+    std::string key;
+    TuneChoice c{};
+    if (!(is >> key >> c.bn >> c.ksplit >> c.kps >> c.sps >> c.group)) return false;
+    std::string extra;
+    if (is >> extra) return false;
+    if (c.bn <= 0 || c.bn > 256 || c.ksplit < 1 || c.kps < 0 || c.sps < 1 || c.sps > 2 || c.group < 1) return false;
+    add[key] = c;
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (const auto& kv : add) tune_table()[kv.first] = kv.second;
+  return true;
+}
+
+void tune_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_table().clear();
+}
 
 void* dev_alloc(size_t bytes) {
   if (bytes == 0) bytes = 256;
@@ -579,6 +635,29 @@ void Engine::autotune(int reps) {
     if (sp->kind != 1) continue;
     GemmPlan& p = sp->plan[1];
     if (!p.use_tc || p.ncand < 2) continue;
+    // shape key: SM count, class, M x N x K, slices, output orientation
+    const std::string key = std::to_string(num_sms()) + ":c" + std::to_string(static_cast<int>(sp->cls)) + ":" +
+                            std::to_string(p.M) + "x" + std::to_string(p.N) + "x" + std::to_string(p.K) + ":s" +
+                            std::to_string(p.slices) + (p.m_major ? ":m" : ":n");
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = tune_table().find(key);
+      int hit = -1;
+      if (it != tune_table().end())
+        for (int c = 0; c < p.ncand && hit < 0; ++c)
+          if (p.cand_bn[c] == it->second.bn && p.cand_ks[c] == it->second.ksplit &&
+              p.cand_kps[c] == it->second.kps && p.cand_sps[c] == it->second.sps &&
+              p.cand_group[c] == it->second.group)
+            hit = c;
+      if (hit >= 0) {
+        p.bn = p.cand_bn[hit];
+        p.ksplit = p.cand_ks[hit];
+        p.k_per_split = p.cand_kps[hit];
+        p.sps = p.cand_sps[hit];
+        p.group = p.cand_group[hit];
+        continue;
+      }
+    }
     __nv_bfloat16* panel[2];
     for (int side = 0; side < 2; ++side) panel[side] = tc_panel(p.P[side], side);
     float best = 0.f;
@@ -612,6 +691,8 @@ void Engine::autotune(int reps) {
       p.k_per_split = p.cand_kps[pick];
       p.sps = p.cand_sps[pick];
       p.group = p.cand_group[pick];
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      tune_table()[key] = TuneChoice{p.bn, p.ksplit, p.sps, p.group, p.k_per_split};
     }
   }
   GBCC_CK(cudaStreamSynchronize(stream_));

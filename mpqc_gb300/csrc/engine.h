@@ -125,6 +125,12 @@ struct SiteStat {
 struct OperandPlan;
 struct GemmPlan;
 
+// The process-wide autotune table: written as text by tune_save, merged from
+// such a file by tune_load (false: unreadable or malformed, table unchanged)
+bool tune_save(const std::string& path);
+bool tune_load(const std::string& path);
+void tune_clear();
+
 class Engine {
  public:
   Engine();
@@ -194,7 +200,9 @@ class Engine {
   // `launches` is the number of kernels it enqueues
   void custom(const std::function<void(cudaStream_t)>& fn, int launches);
   // time the candidate tile widths / K splits of every tensor-core contraction
-  // of the finalised mixed plan on its operands and keep the fastest
+  // of the finalised mixed plan on its operands and keep the fastest; a shape
+  // already in the process's table (tune_load, or an earlier handle) takes
+  // the stored choice untimed
   void autotune(int reps);
 
   // Statistics of the last EXEC pass (FLOPs of the contractions as planned).

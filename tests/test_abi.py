@@ -123,6 +123,31 @@ def test_array_checks():
     assert _ptr(np.zeros(3)) != 0
 
 
+def test_autotune_table_files(lib, tmp_path):
+    """The autotune table's file round trip (no GPU: the table is host state)."""
+    from mpqc_gb300._lib import GBCC_ERR_INVALID_ARG, GBCC_OK
+    assert lib.gbcc_autotune_clear() == GBCC_OK
+    assert lib.gbcc_autotune_load(str(tmp_path / "missing.txt").encode()) == GBCC_ERR_INVALID_ARG
+    assert "autotune" in lib.gbcc_last_error(None).decode()
+    good = tmp_path / "tune.txt"
+    good.write_text("gbcc-autotune 1\n152:c1:10240x10240x10240:s2:n 192 1 0 2 8\n")
+    assert lib.gbcc_autotune_load(str(good).encode()) == GBCC_OK
+    out = tmp_path / "out.txt"
+    assert lib.gbcc_autotune_save(str(out).encode()) == GBCC_OK
+    assert out.read_text() == good.read_text()
+    for bad in ("gbcc-autotune 2\n", "gbcc-autotune 1\nkey 192 1\n", "gbcc-autotune 1\nkey 300 1 0 1 1\n",
+                "gbcc-autotune 1\nkey 64 1 0 3 1\n", "gbcc-autotune 1\nkey 64 1 0 1 1 9\n"):
+        f = tmp_path / "bad.txt"
+        f.write_text(bad)
+        assert lib.gbcc_autotune_load(str(f).encode()) == GBCC_ERR_INVALID_ARG, bad
+    assert lib.gbcc_autotune_save(str(out).encode()) == GBCC_OK
+    assert out.read_text() == good.read_text()  # a rejected file leaves the table unchanged
+    assert lib.gbcc_autotune_save(str(tmp_path / "no" / "dir.txt").encode()) == GBCC_ERR_INVALID_ARG
+    assert lib.gbcc_autotune_clear() == GBCC_OK
+    assert lib.gbcc_autotune_save(str(out).encode()) == GBCC_OK
+    assert out.read_text() == "gbcc-autotune 1\n"
+
+
 def test_energy_noalloc_rejects_sizes_beyond_its_scratch(lib):
     from mpqc_gb300._lib import GBCC_ERR_INVALID_ARG
     st = lib.gbcc_energy_noalloc(4, 513, None, None, None, None, None, None, None, None)
