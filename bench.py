@@ -270,7 +270,9 @@ def ours(args):
     torch.cuda.set_device(dev)
     from mpqc_gb300 import build as gb
     gb.build()
-    from mpqc_gb300 import Solver
+    from mpqc_gb300 import Solver, autotune_load, autotune_save
+    if args.autotune_table and os.path.exists(args.autotune_table):
+        autotune_load(args.autotune_table)
     o, v, naux = args.o, args.v, args.naux
     F = flop_count(o, v)
     log(f"[bench] rank {rank}: building inputs o={o} v={v} naux={naux} on {torch.cuda.get_device_name(dev)}")
@@ -283,6 +285,8 @@ def ours(args):
     # amplitudes (fewest slices within 1e-5 of the 3-slice residual)
     slices_used, slice_err = s.calibrate_slices(t1, t2)
     log(f"[bench] slices (ladder, ring, other) = {slices_used}, rel. change vs 3 slices = {slice_err}")
+    if args.autotune_table:
+        autotune_save(args.autotune_table)
     r1 = torch.empty_like(t1)
     r2 = torch.empty_like(t2)
 
@@ -766,6 +770,9 @@ def main():
                     help="BF16 slices per operand for every class; 0 (default): chosen per class "
                          "from the measured residual error")
     ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--autotune-table", default=None,
+                    help="file of autotuned tiles: loaded if it exists (the contractions it holds are not "
+                         "timed again), written after the set-up (profiling runs reuse the plain run's tiles)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile per contraction (fewer launches before the first residual)")
     ap.add_argument("--fp64-steps", type=int, default=1)
