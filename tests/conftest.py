@@ -69,3 +69,24 @@ def load_molecule(name):
     g = {k: z[k] for k in z.files}
     blocks = {k: np.ascontiguousarray(g[k]) for k in INTEGRAL_NAMES}
     return blocks, g["eps_o"], g["eps_v"], g
+
+
+def build_abi_client(out_dir):
+    """Compile tests/abi_client.cpp (a C++ caller of include/gbcc.h and
+    gbcc_scf.h) against the in-tree libgbcc.so; returns the executable."""
+    import shutil
+    import subprocess
+    from mpqc_gb300 import _lib, build
+    build.build()
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    cuda = Path("/usr/local/cuda")
+    lib_dir = Path(_lib.LIB_PATH).resolve().parent
+    exe = Path(out_dir) / "abi_client"
+    cmd = [cxx, "-std=c++17", "-O1", "-Wall", str(ROOT / "tests" / "abi_client.cpp"), "-I", str(ROOT / "include"),
+           "-I", str(cuda / "include"), "-L", str(lib_dir), "-lgbcc", "-L", str(cuda / "lib64"), "-lcudart",
+           f"-Wl,-rpath,{lib_dir}", f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe

@@ -148,6 +148,20 @@ def test_autotune_table_files(lib, tmp_path):
     assert out.read_text() == "gbcc-autotune 1\n"
 
 
+def test_cxx_client_error_paths(lib, tmp_path):
+    """tests/abi_client.cpp, compiled against the headers and libgbcc.so,
+    calls every entry point and checks the status each reports without a GPU."""
+    import subprocess
+    import torch
+    from conftest import build_abi_client
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present (the gpu test runs the client's device flow)")
+    exe = build_abi_client(tmp_path)
+    r = subprocess.run([str(exe), "cpu"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all checks passed" in r.stdout
+
+
 def test_energy_noalloc_rejects_sizes_beyond_its_scratch(lib):
     from mpqc_gb300._lib import GBCC_ERR_INVALID_ARG
     st = lib.gbcc_energy_noalloc(4, 513, None, None, None, None, None, None, None, None)
