@@ -1,7 +1,10 @@
 // Contraction planner and executor (see engine.h).
 #include "engine.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -248,6 +251,7 @@ struct Site {
   GemmPlan plan[3];  // by plan_index(precision)
   cudaEvent_t e0 = nullptr, e1 = nullptr, eg = nullptr;  // profiling: start, end, GEMM start
   bool has_gemm = false;
+  std::string label;  // NVTX range name: the operation and its operands
   ~Site() {
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
@@ -255,7 +259,19 @@ struct Site {
   }
 };
 
+// NVTX ranges around every operation of an EXEC pass when GBCC_NVTX is set in
+// the environment (a profiler then shows them; graph replays record none, so
+// profile with use_graphs = 0)
+static bool nvtx_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GBCC_NVTX");
+    return e && *e && std::strcmp(e, "0") != 0;
+  }();
+  return on;
+}
+
 void Engine::prof_begin(Site& s) {
+  if (nvtx_enabled()) nvtxRangePushA(s.label.c_str());
   if (!profile_) return;
   if (!s.e0) GBCC_CK(cudaEventCreate(&s.e0));
   if (!s.e1) GBCC_CK(cudaEventCreate(&s.e1));
@@ -272,6 +288,7 @@ void Engine::prof_gemm(Site& s) {
 
 void Engine::prof_end(Site& s) {
   if (profile_) GBCC_CK(cudaEventRecord(s.e1, stream_));
+  if (nvtx_enabled()) nvtxRangePop();
 }
 
 std::vector<SiteStat> Engine::site_stats(int precision) {
@@ -443,6 +460,7 @@ void Engine::assign(const Ix& c, double beta, const std::vector<Factor>& terms) 
     return;
   }
   s.kind = 0;
+  s.label = "assign " + c.t->name + "(" + c.lab + ")";
   check_ix(c);
   if (terms.empty() || terms.size() > static_cast<size_t>(kMaxTerms))
     throw Error(GBCC_ERR_STATE, "engine: assign needs 1..4 terms");
@@ -709,6 +727,7 @@ void Engine::custom(const std::function<void(cudaStream_t)>& fn, int launches) {
     return;
   }
   s.kind = 2;
+  s.label = "kernels (site " + std::to_string(sites_.size() - 1) + ")";
 }
 
 void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<Lin>& A,
@@ -785,6 +804,9 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
   s.kind = 1;
   s.cls = cls;
   check_ix(c);
+  static const char* const kClassName[3] = {"ladder", "ring", "other"};
+  s.label = "contract " + c.t->name + "(" + c.lab + ") <- " + A.at(0).x.t->name + "(" + A.at(0).x.lab + ") " +
+            B.at(0).x.t->name + "(" + B.at(0).x.lab + ") [" + kClassName[static_cast<int>(cls)] + "]";
   if (A.empty() || B.empty() || A.size() > static_cast<size_t>(kMaxTerms) ||
       B.size() > static_cast<size_t>(kMaxTerms))
     throw Error(GBCC_ERR_STATE, "engine: contract needs 1..4 terms per operand");

@@ -222,28 +222,13 @@ void end_to_end() {
   c.precision = GBCC_PREC_FP64;
   gbcc_handle* hf = nullptr;
   CHECK_OK(gbcc_create(&hf, &c));
-  CHECK(gbcc_residual(hf, nullptr, nullptr, nullptr, nullptr) == GBCC_ERR_INVALID_ARG);
+  CHECK(gbcc_residual(hf, nullptr, nullptr, nullptr, nullptr) != GBCC_OK);  // no inputs yet
   CHECK_OK(gbcc_set_inputs(hf, &in));
   std::vector<double> t1(v * o), t2(v * v * o * o);
   gbcc_report rf{};
   const double ef = solve(hf, &t1, &t2, &rf);
   CHECK(rf.converged && rf.mixed_iters == 0);
   CHECK(std::fabs(ef - em) < 1e-8);
-
-  // residual and energy at the converged amplitudes
-  std::vector<double> r1(v * o), r2(v * v * o * o);
-  CHECK_OK(gbcc_residual(hf, t1.data(), t2.data(), r1.data(), r2.data()));
-  double e = 0, err = 1;
-  CHECK_OK(gbcc_energy(hf, t1.data(), t2.data(), r1.data(), r2.data(), &e, &err));
-  CHECK(std::fabs(e - ef) < 1e-9 && err < 1e-8);
-  CHECK_OK(gbcc_residual_ex(hm, GBCC_PREC_FP64, t1.data(), t2.data(), r1.data(), r2.data()));
-  CHECK(gbcc_residual_ex(hm, GBCC_PREC_FP64_TC, t1.data(), t2.data(), r1.data(), r2.data()) == GBCC_ERR_STATE);
-  CHECK(std::strlen(gbcc_last_error(hm)) > 0);
-  int32_t sl[3];
-  double rc[3];
-  CHECK_OK(gbcc_slice_policy(hm, sl, rc));
-  CHECK(sl[0] >= 1 && sl[0] <= 3);
-  CHECK_OK(gbcc_calibrate_slices(hm, t1.data(), t2.data()));
 
   // restarts: checkpoint file and seeded amplitudes
   const std::string path = std::string(std::getenv("GBCC_CLIENT_TMP") ? std::getenv("GBCC_CLIENT_TMP") : ".") +
@@ -262,6 +247,21 @@ void end_to_end() {
   double et = 0;
   CHECK_OK(gbcc_triples(hf, GBCC_PREC_FP64, nullptr, nullptr, &et));
   CHECK(et < 0.0 && et > -0.01);
+
+  // residual and energy at the converged amplitudes
+  std::vector<double> r1(v * o), r2(v * v * o * o);
+  CHECK_OK(gbcc_residual(hf, t1.data(), t2.data(), r1.data(), r2.data()));
+  double e = 0, err = 1;
+  CHECK_OK(gbcc_energy(hf, t1.data(), t2.data(), r1.data(), r2.data(), &e, &err));
+  CHECK(std::fabs(e - ef) < 1e-9 && err < 1e-8);
+  CHECK_OK(gbcc_residual_ex(hm, GBCC_PREC_FP64, t1.data(), t2.data(), r1.data(), r2.data()));
+  CHECK(gbcc_residual_ex(hm, GBCC_PREC_FP64_TC, t1.data(), t2.data(), r1.data(), r2.data()) == GBCC_ERR_STATE);
+  CHECK(std::strlen(gbcc_last_error(hm)) > 0);
+  int32_t sl[3];
+  double rc[3];
+  CHECK_OK(gbcc_slice_policy(hm, sl, rc));
+  CHECK(sl[0] >= 1 && sl[0] <= 3);
+  CHECK_OK(gbcc_calibrate_slices(hm, t1.data(), t2.data()));
 
   // zero-copy inputs: the handle's own device arrays, filled here
   gbcc_handle* hz = nullptr;
