@@ -339,6 +339,22 @@ gbcc_status gbcc_autotune_save(const char* path);
 gbcc_status gbcc_autotune_load(const char* path);
 gbcc_status gbcc_autotune_clear(void);
 
+/* Layout adapters for a caller whose tensors are tiled (MPQC's TiledArray
+ * arrays over TiledRange1 boundaries, e.g. the uneven occupied / virtual
+ * tilings of src/mpqc/chemistry/qc/lcao/expression/trange1_engine.cpp:10-20):
+ * `tiles` holds every tile of a rank-`rank` array one after another, in
+ * row-major order over the tile grid, each tile row-major over its own
+ * extents; `dense` is the row-major array the entry points above take.
+ * bounds[d] lists the nbounds[d] boundaries of dimension d (0 = b0 < b1 <
+ * ... < extent).  Host memory, no GPU; GBCC_ERR_INVALID_ARG for rank outside
+ * 1..8, missing or non-increasing boundaries, or NULL arrays.  The residual
+ * does not depend on the tiling: a caller converts its inputs once and its
+ * amplitudes at the call. */
+gbcc_status gbcc_tiles_to_dense(int32_t rank, const int64_t* const* bounds, const int32_t* nbounds,
+                                const double* tiles, double* dense);
+gbcc_status gbcc_dense_to_tiles(int32_t rank, const int64_t* const* bounds, const int32_t* nbounds,
+                                const double* dense, double* tiles);
+
 gbcc_status gbcc_calibrate_slices(gbcc_handle* h, const double* t1_ai, const double* t2_abij);
 
 /* Message of the last failing call on this handle ("" if none); with a NULL

@@ -29,6 +29,7 @@ EXPORTS = (
     "gbcc_slice_policy", "gbcc_calibrate_slices", "gbcc_last_error", "gbcc_set_amplitudes",
     "gbcc_save_amplitudes", "gbcc_load_amplitudes", "gbcc_set_df_inputs", "gbcc_set_direct_inputs",
     "gbcc_solve_batch", "gbcc_triples", "gbcc_autotune_save", "gbcc_autotune_load", "gbcc_autotune_clear",
+    "gbcc_tiles_to_dense", "gbcc_dense_to_tiles",
 )
 # every symbol include/gbcc_scf.h declares
 SCF_EXPORTS = (
@@ -201,6 +202,9 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         getattr(lib, name).argtypes = [C.c_char_p]
     lib.gbcc_autotune_clear.restype = C.c_int
     lib.gbcc_autotune_clear.argtypes = []
+    for name in ("gbcc_tiles_to_dense", "gbcc_dense_to_tiles"):
+        getattr(lib, name).restype = C.c_int
+        getattr(lib, name).argtypes = [i32, C.POINTER(C.POINTER(C.c_int64)), C.POINTER(C.c_int32), vp, vp]
     lib.gbcc_slice_policy.restype = C.c_int
     lib.gbcc_slice_policy.argtypes = [vp, vp, vp]
     lib.gbcc_last_error.restype = C.c_char_p

@@ -322,6 +322,40 @@ def autotune_clear():
     _check(lib, None, lib.gbcc_autotune_clear())
 
 
+def _tile_bounds(bounds):
+    bounds = [np.ascontiguousarray(b, dtype=np.int64) for b in bounds]
+    ptrs = (C.POINTER(C.c_int64) * len(bounds))(*[b.ctypes.data_as(C.POINTER(C.c_int64)) for b in bounds])
+    counts = (C.c_int32 * len(bounds))(*[b.size for b in bounds])
+    return bounds, ptrs, counts
+
+
+def tiles_to_dense(tiles, bounds):
+    """Dense row-major array from a tile-by-tile buffer (TiledArray order:
+    tiles row-major over the tile grid, each row-major inside) with boundary
+    lists ``bounds`` per dimension, e.g. MPQC's uneven occupied / virtual
+    tilings."""
+    lib = L.load()
+    keep, ptrs, counts = _tile_bounds(bounds)
+    tiles = np.ascontiguousarray(tiles, dtype=np.float64)
+    dense = np.empty(tuple(int(b[-1]) for b in keep))
+    if tiles.size != dense.size:
+        raise InputError("tile buffer size does not match the boundaries")
+    _check(lib, None, lib.gbcc_tiles_to_dense(len(keep), ptrs, counts, tiles.ctypes.data, dense.ctypes.data))
+    return dense
+
+
+def dense_to_tiles(dense, bounds):
+    """The tile-by-tile buffer of a dense array (inverse of tiles_to_dense)."""
+    lib = L.load()
+    keep, ptrs, counts = _tile_bounds(bounds)
+    dense = np.ascontiguousarray(dense, dtype=np.float64)
+    if dense.shape != tuple(int(b[-1]) for b in keep):
+        raise InputError("array shape does not match the boundaries")
+    tiles = np.empty(dense.size)
+    _check(lib, None, lib.gbcc_dense_to_tiles(len(keep), ptrs, counts, dense.ctypes.data, tiles.ctypes.data))
+    return tiles
+
+
 def solve_batch(solvers):
     """Solve several independent handles at once (``gbcc_solve_batch``): each
     handle's solve runs on its own stream from its own host thread, so small

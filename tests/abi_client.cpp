@@ -80,6 +80,21 @@ void error_paths(bool gpu) {
   CHECK(gbcc_autotune_load(nullptr) == GBCC_ERR_INVALID_ARG);
   CHECK(gbcc_autotune_save(nullptr) == GBCC_ERR_INVALID_ARG);
   CHECK(gbcc_autotune_clear() == GBCC_OK);
+  // tile-layout adapters (host only): a 5 x 4 array in tiles of rows {2, 3} x columns {1, 3}
+  {
+    const int64_t b0[] = {0, 2, 5}, b1[] = {0, 1, 4};
+    const int64_t* bounds[] = {b0, b1};
+    const int32_t nb[] = {3, 3};
+    double dense[20], back[20], tiles[20];
+    for (int k = 0; k < 20; ++k) dense[k] = k;
+    CHECK(gbcc_dense_to_tiles(2, bounds, nb, dense, tiles) == GBCC_OK);
+    // first tile: rows 0-1, column 0; second: rows 0-1, columns 1-3
+    CHECK(tiles[0] == 0 && tiles[1] == 4 && tiles[2] == 1 && tiles[3] == 2 && tiles[4] == 3 && tiles[5] == 5);
+    CHECK(gbcc_tiles_to_dense(2, bounds, nb, tiles, back) == GBCC_OK);
+    CHECK(std::memcmp(dense, back, sizeof(dense)) == 0);
+    CHECK(gbcc_tiles_to_dense(0, bounds, nb, tiles, back) == GBCC_ERR_INVALID_ARG);
+    CHECK(gbcc_dense_to_tiles(2, bounds, nb, nullptr, tiles) == GBCC_ERR_INVALID_ARG);
+  }
   // input producer
   gbcc_scf_config sc;
   gbcc_scf_config_default(&sc);

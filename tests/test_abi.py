@@ -162,6 +162,58 @@ def test_cxx_client_error_paths(lib, tmp_path):
     assert "all checks passed" in r.stdout
 
 
+def _uneven_bounds(rng, extent, lo, hi):
+    """TiledRange1-style boundaries with tile sizes drawn in [lo, hi] (the last one
+    takes the remainder)."""
+    b = [0]
+    while b[-1] < extent:
+        b.append(min(extent, b[-1] + int(rng.integers(lo, hi + 1))))
+    return np.array(b, dtype=np.int64)
+
+
+def _tiles_np(dense, bounds):
+    """Restatement of the tile-by-tile order: tiles row-major over the grid,
+    each one row-major inside."""
+    import itertools
+    out = []
+    for idx in itertools.product(*[range(len(b) - 1) for b in bounds]):
+        sl = tuple(slice(b[i], b[i + 1]) for b, i in zip(bounds, idx))
+        out.append(dense[sl].ravel())
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("shape,lo,hi", [((7,), 1, 3), ((5, 9), 2, 4), ((3, 4, 6, 7), 1, 3), ((6, 6, 5, 5), 2, 3),
+                                         ((2, 3, 2, 3, 2), 1, 2)])
+def test_tile_layout_adapters(lib, shape, lo, hi):
+    """TiledArray-style tiled buffers <-> the dense arrays the entry points take
+    (uneven tiles, as MPQC's occupied and virtual tilings are), against numpy."""
+    from mpqc_gb300 import dense_to_tiles, tiles_to_dense
+    rng = np.random.default_rng(len(shape) * 10 + sum(shape))
+    bounds = [_uneven_bounds(rng, n, lo, hi) for n in shape]
+    dense = rng.normal(size=shape)
+    tiles = _tiles_np(dense, bounds)
+    assert np.array_equal(dense_to_tiles(dense, bounds), tiles)
+    assert np.array_equal(tiles_to_dense(tiles, bounds), dense)
+
+
+def test_tile_layout_adapters_reject_bad_bounds(lib):
+    import ctypes as C
+    from mpqc_gb300 import InputError, tiles_to_dense
+    from mpqc_gb300._lib import GbccError
+    for bad in ([np.array([1, 3])], [np.array([0, 2, 2])], [np.array([0])]):
+        with pytest.raises(GbccError):
+            tiles_to_dense(np.zeros(int(bad[0][-1])), bad)
+    with pytest.raises(InputError):
+        tiles_to_dense(np.zeros(5), [np.array([0, 2, 4])])
+    assert lib.gbcc_tiles_to_dense(0, None, None, None, None) == 1
+    assert lib.gbcc_dense_to_tiles(9, None, None, None, None) == 1
+    assert "rank" in lib.gbcc_last_error(None).decode()
+    b = np.array([0, 2], dtype=np.int64)
+    ptrs = (C.POINTER(C.c_int64) * 1)(b.ctypes.data_as(C.POINTER(C.c_int64)))
+    n = (C.c_int32 * 1)(2)
+    assert lib.gbcc_tiles_to_dense(1, ptrs, n, None, None) == 1
+
+
 def test_energy_noalloc_rejects_sizes_beyond_its_scratch(lib):
     from mpqc_gb300._lib import GBCC_ERR_INVALID_ARG
     st = lib.gbcc_energy_noalloc(4, 513, None, None, None, None, None, None, None, None)
