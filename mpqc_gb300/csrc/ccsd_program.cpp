@@ -282,19 +282,20 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   // reads and adds to it, while an elementwise pass pays little for the read.
   const Tensor& r2u = *S.r2u;
   const Tensor &P = *S.P, &K = *S.K;
-  // j and k intermediates (:229-249) with T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l),
-  // packed from its two terms where it is used (not stored).  j enters r2 only
+  // j and k intermediates (:229-249) with T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l)
+  // = tau(d,a,i,l) - 0.5 t2(d,a,i,l), packed from those two arrays where it is used
+  // (not stored; two plain terms pack faster than t2 and a t1 t1 product).  j enters r2 only
   // as P(a,k,i,c) = 2 j(a,k,i,c) - k(k,a,i,c), whose ring part
   //   -2 G_cd T + (2 G_cd - G_dc) t2(a,d,i,l) + G_dc T = (2 G_cd - G_dc) (t2(a,d,i,l) - T)
   // (G_cd = Gijab(k,l,c,d), G_dc = Gijab(k,l,d,c), summed over l, d) is one
   // contraction instead of j's two and a share of k's
-  const std::vector<Lin> T = {{0.5, ix(t2, "dail")}, lin2(1.0, ix(t1, "di"), ix(t1, "al"))};
+  const std::vector<Lin> T = {{1.0, ix(tau, "dail")}, {-0.5, ix(t2, "dail")}};
   E.contract(ix(K, "kaic"), 0.0, -1.0, {{1.0, ix(Gijab, "kldc")}}, T, R);
   E.assign(ix(K, "kaic"), 1.0, {f1(1.0, ix(Giajb, "kaic"))});
   E.contract(ix(K, "kaic"), 1.0, -1.0, {{1.0, ix(Gijka, "klic")}}, {{1.0, ix(t1, "al")}}, O);
   E.contract(ix(K, "kaic"), 1.0, 1.0, {{1.0, ix(Giabc, "kadc")}}, {{1.0, ix(t1, "di")}}, O);
   E.contract(ix(P, "akic"), 0.0, 1.0, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "kldc")}},
-             {{1.0, ix(t2, "adil")}, {-0.5, ix(t2, "dail")}, lin2(-1.0, ix(t1, "di"), ix(t1, "al"))}, R);
+             {{1.0, ix(t2, "adil")}, {0.5, ix(t2, "dail")}, {-1.0, ix(tau, "dail")}}, R);
   // the rest of 2 j - k: 2 Gijab(i,k,a,c) - Giajb(k,a,i,c) - (2 Gijka(l,k,i,c) -
   // Gijka(k,l,i,c)) t1(a,l) + (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) t1(d,i)
   E.assign(ix(P, "akic"), 1.0, {f1(2.0, ix(Gijab, "ikac")), f1(-1.0, ix(Giajb, "kaic"))});
