@@ -26,6 +26,8 @@
 //    materialised: the t1 t1 part is t1(a,k) (h_kc(k,c) t1(c,i));
 //  - nor is T(d,a,i,l) = 0.5 t2(d,a,i,l) + t1(d,i) t1(a,l): the ring
 //    contractions pack its two terms directly;
+//  - g_ac's sum_kd (2 Giabc(k,a,d,c) - Giabc(k,a,c,d)) t1(d,k) is read off the
+//    diagonals i = k of K's and P's Giabc t1 terms (their increments, kernels.cu);
 //  - the hole-hole ladder W(k,l,i,j) tau(a,b,k,l) runs as pair products over
 //    k <= l and i <= j (like the particle-particle ladder, kernels.cu), and
 //    adds to that ladder's B+-; one pass then writes r2: r2u(a,b,i,j) +
@@ -91,6 +93,8 @@ void CcsdTensors::create(Engine& E, int64_t o, int64_t v, int64_t naux_df, int64
   Y2 = &E.tensor("Y2", {o, o, v, o});
   gki = &E.tensor("gki", {o, o});
   gac = &E.tensor("gac", {v, v});
+  diagK = &E.tensor("diagK", {o, v, v});
+  diagP = &E.tensor("diagP", {o, v, v});
   P = &E.tensor("P", {v, o, o, v});
   K = &E.tensor("K", {o, v, o, v});
   tmp = &E.tensor("tmp", {v, v, o, o});
@@ -293,6 +297,9 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.contract(ix(K, "kaic"), 0.0, -1.0, {{1.0, ix(Gijab, "kldc")}}, T, R);
   E.assign(ix(K, "kaic"), 1.0, {f1(1.0, ix(Giajb, "kaic"))});
   E.contract(ix(K, "kaic"), 1.0, -1.0, {{1.0, ix(Gijka, "klic")}}, {{1.0, ix(t1, "al")}}, O);
+  const double *Kd = K.d, *Pd = P.d;
+  double *dK = S.diagK->d, *dP = S.diagP->d;
+  E.custom([=](cudaStream_t st) { launch_diag_snapshot(o, v, 0, Kd, dK, st); }, 1);
   E.contract(ix(K, "kaic"), 1.0, 1.0, {{1.0, ix(Giabc, "kadc")}}, {{1.0, ix(t1, "di")}}, O);
   E.contract(ix(P, "akic"), 0.0, 1.0, {{2.0, ix(Gijab, "klcd")}, {-1.0, ix(Gijab, "kldc")}},
              {{1.0, ix(t2, "adil")}, {0.5, ix(t2, "dail")}, {-1.0, ix(tau, "dail")}}, R);
@@ -301,6 +308,7 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   E.assign(ix(P, "akic"), 1.0, {f1(2.0, ix(Gijab, "ikac")), f1(-1.0, ix(Giajb, "kaic"))});
   E.contract(ix(P, "akic"), 1.0, -1.0, {{2.0, ix(Gijka, "lkic")}, {-1.0, ix(Gijka, "klic")}},
              {{1.0, ix(t1, "al")}}, O);
+  E.custom([=](cudaStream_t st) { launch_diag_snapshot(o, v, 1, Pd, dP, st); }, 1);
   E.contract(ix(P, "akic"), 1.0, 1.0, {{2.0, ix(Giabc, "kacd")}, {-1.0, ix(Giabc, "kadc")}},
              {{1.0, ix(t1, "di")}}, O);
   // r2 += 0.5 (2 j(a,k,i,c) - k(k,a,i,c)) (2 t2(c,b,k,j) - t2(b,c,k,j))   (:251-252)
@@ -324,8 +332,10 @@ void residual_program(Engine& E, const CcsdTensors& S) {
   // (the reference's 4-argument F_VV adds + Fia(k,c) t1(a,k); kept as written)
   E.assign(ix(*S.gac, "ac"), 0.0, {f1(1.0, ix(*S.FAB, "ac"))});
   E.contract(ix(*S.gac, "ac"), 1.0, 1.0, {{1.0, ix(Fia, "kc")}}, {{1.0, ix(t1, "ak")}}, O);
-  E.contract(ix(*S.gac, "ac"), 1.0, 1.0, {{2.0, ix(Giabc, "kadc")}, {-1.0, ix(Giabc, "kacd")}},
-             {{1.0, ix(t1, "dk")}}, O);
+  // the gbar_iabc t1 term from the diagonals i = k of the Giabc t1 terms of K and P
+  // (kernels.cu): no pass over Giabc of its own
+  double* gacd = S.gac->d;
+  E.custom([=](cudaStream_t st) { launch_gac_from_diagonals(o, v, Kd, Pd, dK, dP, gacd, st); }, 1);
   // r2 += g_ac(a,c) t2(c,b,i,j) - g_ki(k,i) t2(a,b,k,j)
   E.contract(ix(r2u, "abij"), 1.0, 1.0, {{1.0, ix(*S.gac, "ac")}}, {{1.0, ix(t2, "cbij")}}, O);
   E.contract(ix(r2u, "abij"), 1.0, -1.0, {{1.0, ix(*S.gki, "ki")}}, {{1.0, ix(t2, "abkj")}}, O);

@@ -19,6 +19,8 @@ struct CcsdTensors {
   // intermediates
   // (P = 2 j - k of the ring terms, k = K)
   Tensor *tki, *FAB, *FIJ, *hkc, *r2u, *Y1, *Y2, *gki, *gac, *P, *K, *tmp, *W, *tmp2;
+  // K(k,a,k,c) and P(a,k,k,c) before their Giabc t1 terms (g_ac reads the increments)
+  Tensor *diagK, *diagP;
   // particle-particle ladder over pair-(anti)symmetric combinations: G+/G- of
   // Gabcd over (a <= b) x (c <= d) and of Giabc over (k a) x (c <= d)
   // (constants), tau+/tau- over (c <= d) x (i <= j), and the pair products

@@ -441,6 +441,48 @@ __global__ void __launch_bounds__(256) r2_assemble_kernel(int64_t o, int64_t v, 
   }
 }
 
+// g_ac's Giabc term (ccsd_intermediates.h F_VV) read off the diagonals i = k
+// of two contractions the residual performs anyway: with
+//   Z(k,a,c,i) = sum_d Giabc(k,a,d,c) t1(d,i)   (added to K(k,a,i,c))
+//   Q(k,a,c,i) = sum_d (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) t1(d,i)   (added to P(a,k,i,c))
+// sum_kd (2 Giabc(k,a,d,c) - Giabc(k,a,c,d)) t1(d,k) = sum_k 1.5 Z(k,a,c,k) - 0.5 Q(k,a,c,k).
+// The increments are the differences of the diagonals after and before
+// those contractions: diag_snapshot stores K(k,a,k,c) (which = 0) or
+// P(a,k,k,c) (which = 1) as d[k][a][c]; gac_from_diagonals adds the sum.
+__global__ void __launch_bounds__(kThreads) diag_snapshot_kernel(int64_t o, int64_t v, int which,
+                                                                 const double* __restrict__ X,
+                                                                 double* __restrict__ d) {
+  const int64_t n = o * v * v;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int64_t ka, c, k, a;
+    divmod32(e, v, ka, c);
+    divmod32(ka, v, k, a);
+    d[e] = which == 0 ? X[((k * v + a) * o + k) * v + c] : X[((a * o + k) * o + k) * v + c];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) gac_from_diagonals_kernel(int64_t o, int64_t v,
+                                                                      const double* __restrict__ K,
+                                                                      const double* __restrict__ P,
+                                                                      const double* __restrict__ dK,
+                                                                      const double* __restrict__ dP,
+                                                                      double* __restrict__ gac) {
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < v * v;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int64_t a, c;
+    divmod32(e, v, a, c);
+    double s = 0.0;
+    for (int64_t k = 0; k < o; ++k) {
+      const int64_t kac = (k * v + a) * v + c;
+      const double z = K[((k * v + a) * o + k) * v + c] - dK[kac];
+      const double q = P[((a * o + k) * o + k) * v + c] - dP[kac];
+      s = fma(1.5, z, fma(-0.5, q, s));
+    }
+    gac[e] += s;
+  }
+}
+
 // r1(a,i) += sum_k 2 tmp2(k,a,k,i) - tmp2(k,a,i,k) with tmp2[o][v][o][o]: the
 // (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i) term of r1 read off the
 // ladder's tmp2(k,a,i,j) = Giabc(k,a,c,d) tau(c,d,i,j), using
@@ -931,6 +973,15 @@ void launch_r2_assemble(int64_t o, int64_t v, const double* r2u, const double* t
   const int64_t nt = (o + 31) / 32;
   const unsigned grid = static_cast<unsigned>(std::min<int64_t>(v * v * nt * nt, 152LL * 16));
   r2_assemble_kernel<<<grid, dim3(32, 8), 0, st>>>(o, v, r2u, tmp, g, Bp, Bm, accumulate, r2);
+}
+
+void launch_diag_snapshot(int64_t o, int64_t v, int which, const double* X, double* d, cudaStream_t st) {
+  diag_snapshot_kernel<<<grid_for(o * v * v, kThreads), kThreads, 0, st>>>(o, v, which, X, d);
+}
+
+void launch_gac_from_diagonals(int64_t o, int64_t v, const double* K, const double* P, const double* dK,
+                               const double* dP, double* gac, cudaStream_t st) {
+  gac_from_diagonals_kernel<<<grid_for(v * v, kThreads), kThreads, 0, st>>>(o, v, K, P, dK, dP, gac);
 }
 
 void launch_r1_from_tmp2(int64_t o, int64_t v, const double* tmp2, double* r1, cudaStream_t st) {

@@ -287,6 +287,11 @@ void launch_pair_unpack(int64_t rows_v, int64_t v, int64_t o, bool ab_pairs, con
 void launch_r2_assemble(int64_t o, int64_t v, const double* r2u, const double* tmp, const double* g,
                         const double* Bp, const double* Bm, bool accumulate, double* r2, cudaStream_t st);
 
+// d[k][a][c] = K[k][a][k][c] (which 0, K[o][v][o][v]) or P[a][k][k][c] (which 1, P[v][o][o][v])
+void launch_diag_snapshot(int64_t o, int64_t v, int which, const double* X, double* d, cudaStream_t st);
+// gac(a,c) += sum_k 1.5 (K(k,a,k,c) - dK[k][a][c]) - 0.5 (P(a,k,k,c) - dP[k][a][c])
+void launch_gac_from_diagonals(int64_t o, int64_t v, const double* K, const double* P, const double* dK,
+                               const double* dP, double* gac, cudaStream_t st);
 // r1(a,i) += sum_k 2 tmp2(k,a,k,i) - tmp2(k,a,i,k), tmp2[o][v][o][o], r1[v][o]
 void launch_r1_from_tmp2(int64_t o, int64_t v, const double* tmp2, double* r1, cudaStream_t st);
 
