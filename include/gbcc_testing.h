@@ -94,6 +94,17 @@ int gbcc_testing_triples_chunk(int64_t k);
  * GFLOP/s, register operands over all SMs. */
 int gbcc_testing_dmma_peak(double* gflops);
 
+/* The solver's DIIS coefficient solve (the bordered system of the stored
+ * vectors, oldest dropped while it is singular) on a given n x n B (n <= 16,
+ * vectors in age order, oldest first): coef[n] and the number of oldest
+ * vectors dropped. */
+int gbcc_testing_diis_coefficients(int32_t n, const double* B, double damping, double* coef, int32_t* nskip);
+
+/* Device allocations of the engine: *count (may be NULL) receives how many
+ * were made so far in the process; from now on `after` more succeed and the
+ * next one fails with GBCC_ERR_OOM as if the device were full (-1: none fails). */
+int gbcc_testing_fail_alloc(int64_t after, int64_t* count);
+
 /* Rows a per block of the density-fitted ladder for handles whose inputs are
  * set from now on (0: the default size, a block of (ab|cd) of at most 4 GB). */
 int gbcc_testing_df_block_rows(int64_t rows);

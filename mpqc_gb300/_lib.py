@@ -37,7 +37,7 @@ SCF_EXPORTS = (
     "gbcc_scf_ccsd_inputs", "gbcc_scf_destroy", "gbcc_last_scf_error",
 )
 # test hooks of include/gbcc_testing.h
-TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_gemm_ex3", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_dmma_peak", "gbcc_testing_fixed_split", "gbcc_testing_gemm_fp64tc", "gbcc_testing_gemm_timeout", "gbcc_testing_triples_chunk", "gbcc_testing_profile_residual",
+TESTING_EXPORTS = ("gbcc_testing_gemm", "gbcc_testing_gemm_ex", "gbcc_testing_gemm_ex2", "gbcc_testing_gemm_ex3", "gbcc_testing_split", "gbcc_testing_scale", "gbcc_testing_fp64_peak", "gbcc_testing_dmma_peak", "gbcc_testing_diis_coefficients", "gbcc_testing_fail_alloc", "gbcc_testing_fixed_split", "gbcc_testing_gemm_fp64tc", "gbcc_testing_gemm_timeout", "gbcc_testing_triples_chunk", "gbcc_testing_profile_residual",
                    "gbcc_testing_last_launches", "gbcc_testing_record", "gbcc_testing_elapsed",
                    "gbcc_testing_profile_gemm_ms", "gbcc_testing_profile_dims",
                    "gbcc_testing_profile_tiles", "gbcc_testing_tc_launches_total", "gbcc_testing_eigh",
@@ -152,6 +152,10 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.gbcc_testing_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     lib.gbcc_testing_dmma_peak.restype = C.c_int
     lib.gbcc_testing_dmma_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.gbcc_testing_diis_coefficients.restype = C.c_int
+    lib.gbcc_testing_diis_coefficients.argtypes = [C.c_int32, vp, C.c_double, vp, C.POINTER(C.c_int32)]
+    lib.gbcc_testing_fail_alloc.restype = C.c_int
+    lib.gbcc_testing_fail_alloc.argtypes = [C.c_int64, C.POINTER(C.c_int64)]
     lib.gbcc_testing_triples_chunk.restype = C.c_int
     lib.gbcc_testing_triples_chunk.argtypes = [C.c_int64]
     lib.gbcc_testing_gemm_timeout.restype = C.c_int

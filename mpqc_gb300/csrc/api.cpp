@@ -34,6 +34,7 @@ struct gbcc_handle {
   std::unique_ptr<gbcc::Engine> aux;  // one-off setup operations
   gbcc::CcsdTensors S{};
   bool inputs_set = false;
+  bool tensors_incomplete = false;  // an allocation failed inside create_tensors
   int* d_err = nullptr;
   double* d_partial = nullptr;  // reduction scratch [kReduceBlocks * 16]
   double* d_out = nullptr;      // reduction results
@@ -90,6 +91,8 @@ gbcc_status fail(gbcc_handle* h, gbcc_status s, const std::string& msg) {
 template <class F>
 gbcc_status guarded(gbcc_handle* h, F&& f) {
   if (!h) return GBCC_ERR_INVALID_ARG;
+  if (h->tensors_incomplete)
+    return fail(h, GBCC_ERR_STATE, "an allocation failure left the handle's tensors incomplete: destroy it");
   try {
     if (cudaSetDevice(h->cfg.device) != cudaSuccess)
       throw Error(GBCC_ERR_CUDA, "cudaSetDevice failed");
@@ -103,6 +106,19 @@ gbcc_status guarded(gbcc_handle* h, F&& f) {
     return fail(h, GBCC_ERR_OOM, "host allocation failed");
   } catch (const std::exception& e) {
     return fail(h, GBCC_ERR_CUDA, e.what());
+  }
+}
+
+// The handle's tensors, on the first input call.  An allocation failure part
+// way leaves them incomplete: the handle then refuses every call but
+// gbcc_destroy (GBCC_ERR_STATE).
+void create_tensors(gbcc_handle* h, int64_t naux, int64_t nao) {
+  if (h->S.t1) return;
+  try {
+    h->S.create(*h->eng, h->cfg.o, h->cfg.v, naux, nao);
+  } catch (...) {
+    h->tensors_incomplete = true;
+    throw;
   }
 }
 
@@ -712,7 +728,7 @@ gbcc_status gbcc_set_inputs(gbcc_handle* h, const gbcc_inputs* in) {
       if (!p) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_inputs: NULL input array");
     const int64_t o = h->cfg.o, v = h->cfg.v;
     validate_eps(in->eps_o, in->eps_v, o, v);
-    if (!h->S.t1) h->S.create(*h->eng, o, v);
+    create_tensors(h, 0, 0);
     if (h->S.naux > 0 || h->S.nao > 0)
       throw Error(GBCC_ERR_STATE, "gbcc_set_inputs: the handle holds density-fitted or integral-direct inputs");
     gbcc::CcsdTensors& S = h->S;
@@ -747,7 +763,7 @@ gbcc_status gbcc_set_df_inputs(gbcc_handle* h, const gbcc_df_inputs* in) {
       throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_df_inputs: naux out of range");
     const int64_t o = h->cfg.o, v = h->cfg.v, nq = in->naux;
     validate_eps(in->eps_o, in->eps_v, o, v);
-    if (!h->S.t1) h->S.create(*h->eng, o, v, nq);
+    create_tensors(h, nq, 0);
     if (h->S.nao > 0) throw Error(GBCC_ERR_STATE, "gbcc_set_df_inputs: the handle holds integral-direct inputs");
     if (h->S.naux != nq)
       throw Error(GBCC_ERR_STATE, h->S.naux == 0 ? "gbcc_set_df_inputs: the handle holds standard inputs"
@@ -782,7 +798,7 @@ gbcc_status gbcc_set_direct_inputs(gbcc_handle* h, const gbcc_direct_inputs* in)
     const int64_t o = h->cfg.o, v = h->cfg.v, n = in->nao;
     if (n < 1 || n > 1024) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_set_direct_inputs: nao must be 1..1024");
     validate_eps(in->eps_o, in->eps_v, o, v);
-    if (!h->S.t1) h->S.create(*h->eng, o, v, 0, n);
+    create_tensors(h, 0, n);
     if (h->S.naux > 0) throw Error(GBCC_ERR_STATE, "gbcc_set_direct_inputs: the handle holds density-fitted inputs");
     if (h->S.nao != n)
       throw Error(GBCC_ERR_STATE, h->S.nao == 0 ? "gbcc_set_direct_inputs: the handle holds standard inputs"
@@ -812,7 +828,7 @@ gbcc_status gbcc_set_direct_inputs(gbcc_handle* h, const gbcc_direct_inputs* in)
 gbcc_status gbcc_device_inputs(gbcc_handle* h, gbcc_inputs* out) {
   return guarded(h, [&]() -> gbcc_status {
     if (!out) throw Error(GBCC_ERR_INVALID_ARG, "gbcc_device_inputs: NULL output");
-    if (!h->S.t1) h->S.create(*h->eng, h->cfg.o, h->cfg.v);
+    create_tensors(h, 0, 0);
     if (h->S.naux > 0 || h->S.nao > 0)
       throw Error(GBCC_ERR_STATE, "gbcc_device_inputs: the handle holds density-fitted or integral-direct inputs");
     gbcc::CcsdTensors& S = h->S;

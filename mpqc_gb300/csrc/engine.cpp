@@ -4,6 +4,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -67,8 +68,19 @@ void tune_clear() {
   tune_table().clear();
 }
 
+// test hooks (gbcc_testing_fail_alloc): device allocations made so far, and
+// how many more succeed before one fails as if the device were full (-1: all)
+std::atomic<int64_t> g_alloc_count{0};
+std::atomic<int64_t> g_fail_alloc_after{-1};
+
 void* dev_alloc(size_t bytes) {
   if (bytes == 0) bytes = 256;
+  ++g_alloc_count;
+  int64_t left = g_fail_alloc_after.load();
+  while (left >= 0 && !g_fail_alloc_after.compare_exchange_weak(left, left - 1)) {
+  }
+  if (left == 0)
+    throw Error(GBCC_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: injected failure (test hook)");
   void* p = nullptr;
   cudaError_t e = cudaMalloc(&p, bytes);
   if (e != cudaSuccess) {
@@ -1123,15 +1135,18 @@ void Engine::contract(const Ix& c, double beta, double alpha, const std::vector<
 
 void Engine::finalize() {
   if (!planned_) throw Error(GBCC_ERR_STATE, "engine: finalize before PLAN");
-  dev_free(w64a_);
-  dev_free(w64b_);
-  dev_free(wbfa_);
-  dev_free(wbfb_);
+  // every old workspace is released and its pointer cleared before the first
+  // new allocation: one that fails leaves no pointer to freed memory behind
+  for (void** p : {reinterpret_cast<void**>(&w64a_), reinterpret_cast<void**>(&w64b_),
+                   reinterpret_cast<void**>(&wbfa_), reinterpret_cast<void**>(&wbfb_),
+                   reinterpret_cast<void**>(&wpart_)}) {
+    dev_free(*p);
+    *p = nullptr;
+  }
   w64a_ = static_cast<double*>(dev_alloc(ws64_a_ * sizeof(double)));
   w64b_ = static_cast<double*>(dev_alloc(ws64_b_ * sizeof(double)));
   wbfa_ = static_cast<__nv_bfloat16*>(dev_alloc(wsbf_a_ * sizeof(__nv_bfloat16)));
   wbfb_ = static_cast<__nv_bfloat16*>(dev_alloc(wsbf_b_ * sizeof(__nv_bfloat16)));
-  dev_free(wpart_);
   wpart_ = static_cast<double*>(dev_alloc(wspart_ * sizeof(double)));
   bytes_ += (ws64_a_ + ws64_b_ + wspart_) * sizeof(double) + (wsbf_a_ + wsbf_b_) * sizeof(__nv_bfloat16);
   // packs shared by several contractions of a residual get their own buffer
@@ -1177,3 +1192,10 @@ void Engine::prepack(int precision) {
 }
 
 }  // namespace gbcc
+
+extern "C" int gbcc_testing_fail_alloc(int64_t after, int64_t* count) {
+  if (after < -1) return GBCC_ERR_INVALID_ARG;
+  if (count) *count = gbcc::g_alloc_count.load();
+  gbcc::g_fail_alloc_after.store(after);
+  return GBCC_OK;
+}

@@ -724,6 +724,55 @@ __device__ double gepp(double* A, double* b, double* x, int n) {
   return det;
 }
 
+// DIIS coefficients (TiledArray's TA::DIIS extrapolation, cc/solvers.h:112-121)
+// from the B matrix of the n stored vectors (slots, oldest first, B by slot
+// with leading dimension nd): the bordered system [[0, -1], [-1, B]] on the
+// newest n - nskip vectors, normalised by the oldest kept <e, e>, damped on
+// the diagonal; the oldest vectors are dropped while |det| < kDiisDetMin (a
+// singular or near-singular B), the newest alone as the last resort.  coef
+// (by slot, nd entries) is written; returns nskip.
+__device__ int diis_coefficients(const double* Bmat, int nd, const int* slots, int n, double damping,
+                                 double* coef) {
+  for (int s = 0; s < nd; ++s) coef[s] = 0.0;
+  double A[(kDiisMax + 1) * (kDiisMax + 1)];
+  double rhs[kDiisMax + 1];
+  double sol[kDiisMax + 1];
+  for (int nskip = 0; nskip < n; ++nskip) {
+    const int m = n - nskip;
+    const int w = m + 1;
+    // normalise by the oldest kept vector's <e, e>
+    const double b0 = fabs(Bmat[slots[nskip] * nd + slots[nskip]]);
+    const double norm = b0 > 0.0 ? 1.0 / b0 : 1.0;
+    for (int r = 0; r < w; ++r) {
+      rhs[r] = (r == 0) ? -1.0 : 0.0;
+      for (int c = 0; c < w; ++c) {
+        double val;
+        if (r == 0 && c == 0) val = 0.0;
+        else if (r == 0 || c == 0) val = -1.0;
+        else val = Bmat[slots[nskip + r - 1] * nd + slots[nskip + c - 1]] * norm;
+        if (r > 0 && r == c) val *= 1.0 + damping;
+        A[r * w + c] = val;
+      }
+    }
+    const double det = gepp(A, rhs, sol, w);
+    if (det > 0.0 && (det >= kDiisDetMin || nskip == n - 1)) {
+      for (int q = 0; q < m; ++q) coef[slots[nskip + q]] = sol[q + 1];
+      return nskip;
+    }
+  }
+  coef[slots[n - 1]] = 1.0;
+  return n - 1;
+}
+
+// test hook: diis_coefficients on a given B (slots 0..n-1 in order)
+__global__ void diis_coefficients_test_kernel(const double* Bmat, int n, double damping, double* coef,
+                                              int* nskip) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int slots[kDiisMax];
+  for (int q = 0; q < n; ++q) slots[q] = q;
+  *nskip = diis_coefficients(Bmat, n, slots, n, damping, coef);
+}
+
 __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
   __shared__ double sh[kThreads];
   __shared__ double dots[kDiisMax];
@@ -744,42 +793,13 @@ __global__ void __launch_bounds__(kThreads) diis_solve_kernel(DiisArgs d) {
     d.Bmat[slot * nd + slots[q]] = dots[q];
     d.Bmat[slots[q] * nd + slot] = dots[q];
   }
-  for (int s = 0; s < nd; ++s) d.coef[s] = 0.0;
-  const int n = meta.nvec;
   if (!meta.extrapolate) {
+    for (int s = 0; s < nd; ++s) d.coef[s] = 0.0;
     d.coef[slot] = 1.0;
     *d.nskip_out = -1;
     return;
   }
-  double A[(kDiisMax + 1) * (kDiisMax + 1)];
-  double rhs[kDiisMax + 1];
-  double sol[kDiisMax + 1];
-  for (int nskip = 0; nskip < n; ++nskip) {
-    const int m = n - nskip;
-    const int w = m + 1;
-    // normalise by the oldest kept vector's <e, e>
-    const double b0 = fabs(d.Bmat[slots[nskip] * nd + slots[nskip]]);
-    const double norm = b0 > 0.0 ? 1.0 / b0 : 1.0;
-    for (int r = 0; r < w; ++r) {
-      rhs[r] = (r == 0) ? -1.0 : 0.0;
-      for (int c = 0; c < w; ++c) {
-        double val;
-        if (r == 0 && c == 0) val = 0.0;
-        else if (r == 0 || c == 0) val = -1.0;
-        else val = d.Bmat[slots[nskip + r - 1] * nd + slots[nskip + c - 1]] * norm;
-        if (r > 0 && r == c) val *= 1.0 + d.damping;
-        A[r * w + c] = val;
-      }
-    }
-    const double det = gepp(A, rhs, sol, w);
-    if (det > 0.0 && (det >= kDiisDetMin || nskip == n - 1)) {
-      for (int q = 0; q < m; ++q) d.coef[slots[nskip + q]] = sol[q + 1];
-      *d.nskip_out = nskip;
-      return;
-    }
-  }
-  d.coef[slot] = 1.0;
-  *d.nskip_out = n - 1;
+  *d.nskip_out = diis_coefficients(d.Bmat, nd, slots, meta.nvec, d.damping, d.coef);
 }
 
 struct ExtrapArgs {
@@ -1010,6 +1030,11 @@ void launch_maxabs_diff(int64_t n, const double* a, const double* b, unsigned lo
 void launch_diis_step(const DiisArgs& d, cudaStream_t st) {
   diis_jacobi_dots_kernel<<<kReduceBlocks, kThreads, 0, st>>>(d);
   diis_solve_kernel<<<1, kThreads, 0, st>>>(d);
+}
+
+void launch_diis_coefficients_test(const double* Bmat, int n, double damping, double* coef, int* nskip,
+                                   cudaStream_t st) {
+  diis_coefficients_test_kernel<<<1, 32, 0, st>>>(Bmat, n, damping, coef, nskip);
 }
 
 void launch_diis_extrapolate(int64_t o, int64_t v, const double* x1, const double* x2,

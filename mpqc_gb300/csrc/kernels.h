@@ -353,6 +353,9 @@ struct DiisArgs {
   int* nskip_out;      // device int
 };
 void launch_diis_step(const DiisArgs& d, cudaStream_t st);
+// test hook: the DIIS coefficients of a given n x n B (n <= 16), coef[n], *nskip
+void launch_diis_coefficients_test(const double* Bmat, int n, double damping, double* coef, int* nskip,
+                                   cudaStream_t st);
 
 // dinv1 = 1 / D1, dinv2 = 1 / D2 (the Jacobi denominators of DiisArgs), once
 // per set of orbital energies: the iteration then multiplies, and the FP64

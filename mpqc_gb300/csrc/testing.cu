@@ -534,3 +534,34 @@ extern "C" int gbcc_testing_gemm_timeout(int64_t M, int64_t N, int64_t K, const 
   for (void* p : owned) dev_free(p);
   return status;
 }
+
+// The DIIS coefficient solve of the solver (diis_coefficients) on a given B:
+// host arrays in and out, its own stream.
+extern "C" int gbcc_testing_diis_coefficients(int32_t n, const double* B, double damping, double* coef,
+                                              int32_t* nskip) {
+  if (n < 1 || n > 16 || !B || !coef || !nskip) return GBCC_ERR_INVALID_ARG;
+  double *dB = nullptr, *dc = nullptr;
+  int* dn = nullptr;
+  cudaStream_t st = nullptr;
+  int status = GBCC_OK;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&dB, sizeof(double) * n * n) != cudaSuccess || cudaMalloc(&dc, sizeof(double) * n) != cudaSuccess ||
+      cudaMalloc(&dn, sizeof(int)) != cudaSuccess ||
+      cudaMemcpyAsync(dB, B, sizeof(double) * n * n, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+    status = GBCC_ERR_CUDA;
+  } else {
+    gbcc::launch_diis_coefficients_test(dB, n, damping, dc, dn, st);
+    int h_n = 0;
+    if (cudaMemcpyAsync(coef, dc, sizeof(double) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&h_n, dn, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      status = GBCC_ERR_CUDA;
+    *nskip = h_n;
+  }
+  cudaGetLastError();
+  cudaFree(dB);
+  cudaFree(dc);
+  cudaFree(dn);
+  if (st) cudaStreamDestroy(st);
+  return status;
+}
