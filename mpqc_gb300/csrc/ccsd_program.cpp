@@ -275,9 +275,11 @@ void residual_program(Engine& E, const CcsdTensors& S) {
              {{1.0, ix(t1, "ck")}}, O);
   // r1 += (2 Giabc(k,a,c,d) - Giabc(k,a,d,c)) tau(c,d,k,i) (:111-114) = 2 tmp2(k,a,k,i) - tmp2(k,a,i,k)
   E.custom([=](cudaStream_t st) { launch_r1_from_tmp2(o, v, tmp2, r1d, st); }, 1);
-  // r1 -= (2 Gijka(l,k,i,c) - Gijka(k,l,i,c)) tau(c,a,k,l)
-  E.contract(ix(r1, "ai"), 1.0, -1.0, {{2.0, ix(Gijka, "lkic")}, {-1.0, ix(Gijka, "klic")}},
-             {{1.0, ix(tau, "cakl")}}, O);
+  // r1 -= (2 Gijka(l,k,i,c) - Gijka(k,l,i,c)) tau(c,a,k,l), read through
+  // tau(c,a,k,l) = tau(a,c,l,k) as (2 Gijka(k,l,i,d) - Gijka(l,k,i,d)) tau(a,d,k,l):
+  // the same pack of tau as F_vv's above, shared
+  E.contract(ix(r1, "ai"), 1.0, -1.0, {{2.0, ix(Gijka, "klid")}, {-1.0, ix(Gijka, "lkid")}},
+             {{1.0, ix(tau, "adkl")}}, O);
 
   // ----- R2 (ccsd_r1_r2.h:198-293) -----
   // K, P and r2u each receive their first (beta = 0) value from a ring
